@@ -1,0 +1,183 @@
+/*
+ * ndfiltrs_gb300 — C-ABI of the GB300 (sm_103a) windowed-statistics library.
+ *
+ * This is the drop-in boundary for ndfiltrs' native module `ndfiltrs._core`
+ * (ysBach/ndfiltrs v0.2.0, a PyO3 extension of a Rust crate). The reference's
+ * Python layer calls three native functions on this path; the first three
+ * entry points below take the same arguments with the same meaning (the
+ * Python objects flattened to plain pointers and sizes) and return the same
+ * error classes as status codes. The plan entry points expose the reference's
+ * Rust plan API (`WindowFilter::new` / `apply_into`) for device-resident and
+ * batched use.
+ *
+ * Conventions
+ *   - Arrays are C-contiguous float32 (dtype 0) or float64 (dtype 1).
+ *   - `shape`, `size` and `origin` have `ndim` entries; `footprint` is NULL
+ *     (rectangular window) or prod(size) bytes, nonzero = selected, C order.
+ *   - Mode names are "reflect", "constant", "nearest", "mirror", "wrap".
+ *   - Every function returns NDF_OK or an error code; ndf_last_error() gives
+ *     the calling thread's message. No exception crosses the ABI.
+ *   - There is no CPU fallback: without a usable CUDA device every compute
+ *     entry point returns NDF_ERR_NO_DEVICE.
+ *   - Host entry points copy the input to the device before computing (the
+ *     snapshot of src/pyapi/filter.rs:219-229) and write a new result into
+ *     `h_out`; input and output never alias.
+ */
+#ifndef NDFILTRS_GB300_H
+#define NDFILTRS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. 1-5 mirror `Error` in src/error.rs:6-18 and map to the same
+ * Python exceptions (src/pyapi/filter.rs:37-44): 1-3 ValueError,
+ * 4 MemoryError, 5 OverflowError. */
+#define NDF_OK 0
+#define NDF_ERR_EMPTY_AXIS 1
+#define NDF_ERR_INVALID_CONFIGURATION 2
+#define NDF_ERR_LENGTH_MISMATCH 3
+#define NDF_ERR_MEMORY 4
+#define NDF_ERR_OVERFLOW 5
+#define NDF_ERR_CUDA 6        /* a CUDA runtime call failed */
+#define NDF_ERR_TIMEOUT 7     /* a bounded device wait gave up */
+#define NDF_ERR_UNSUPPORTED 8 /* a reduction outside this library's scope */
+#define NDF_ERR_NO_DEVICE 9   /* no CUDA device could be used */
+
+#define NDF_FLOAT32 0
+#define NDF_FLOAT64 1
+
+/* Reduction kinds: the `kind` strings of src/pyapi/filter.rs:286-300 plus
+ * the percentile kind of src/pyapi/robust.rs:118-121. */
+#define NDF_KIND_MEDIAN 0
+#define NDF_KIND_MEDIAN_NETWORK 1
+#define NDF_KIND_MEDIAN_HISTOGRAM 2
+#define NDF_KIND_MEAN 3
+#define NDF_KIND_MEAN_ROLLING 4 /* out of scope: returns NDF_ERR_UNSUPPORTED */
+#define NDF_KIND_MIN 5
+#define NDF_KIND_MAX 6
+#define NDF_KIND_VAR 7
+#define NDF_KIND_STD 8
+#define NDF_KIND_RANK 9
+#define NDF_KIND_RANK_HISTOGRAM 10
+#define NDF_KIND_PERCENTILE 11
+
+/* Boundary modes, src/boundary.rs:16-27. */
+#define NDF_MODE_REFLECT 0
+#define NDF_MODE_CONSTANT 1
+#define NDF_MODE_NEAREST 2
+#define NDF_MODE_MIRROR 3
+#define NDF_MODE_WRAP 4
+
+/* Arithmetic of the mean/var/std reductions. */
+#define NDF_MOMENTS_FP32C 0 /* pivot-shifted FP32 compensated sums, FP64 combine */
+#define NDF_MOMENTS_FP64 1  /* the reference's float64 algorithm, bit for bit */
+
+/* Replaces `_core.window_filter(array, kind, size, footprint, origin, mode,
+ * cval, omit_nan, ignore_inf, min_count, parameter)`,
+ * src/pyapi/filter.rs:261-314 (plan: src/plan.rs:260-324, run:
+ * src/plan.rs:370-428). `kind` is one of "median", "median_network",
+ * "median_histogram", "mean", "mean_rolling", "min", "max", "var", "std",
+ * "rank", "rank_histogram"; `parameter` is ddof for var/std and the rank for
+ * the rank kinds. `cval` is cast to the array dtype (src/pyapi/filter.rs:308). */
+int ndf_window_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim,
+                      const uint64_t* shape, const char* kind, const uint64_t* size,
+                      const uint8_t* footprint, const int64_t* origin,
+                      const char* const* modes, double cval, int32_t omit_nan,
+                      int32_t ignore_inf, uint64_t min_count, uint64_t parameter);
+
+/* Replaces `_core.robust_filter(array, size, footprint, origin, mode, cval,
+ * kind, parameter, omit_nan, ignore_inf, min_count, ...)` for
+ * kind = "percentile", src/pyapi/robust.rs:78-171 (plan:
+ * src/robust_plan.rs:55-67, run: src/robust.rs:765-785). `parameter` is the
+ * percentile q in [0, 100]. Other robust kinds return NDF_ERR_UNSUPPORTED. */
+int ndf_robust_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim,
+                      const uint64_t* shape, const uint64_t* size, const uint8_t* footprint,
+                      const int64_t* origin, const char* const* modes, double cval,
+                      const char* kind, double parameter, int32_t omit_nan,
+                      int32_t ignore_inf, uint64_t min_count);
+
+/* Replaces `_core.get_num_threads()`, src/pyapi/filter.rs:378-380. Returns
+ * the number of streaming multiprocessors of the current device (the
+ * library's unit of parallelism), or 0 without a device. */
+int32_t ndf_get_num_threads(void);
+
+/* Thread-local message of the last error on the calling thread. */
+const char* ndf_last_error(void);
+
+/* ---- Plans: WindowFilter::new / RobustFilter::new, src/plan.rs:260-324,
+ * src/robust_plan.rs:55-67. A plan validates the geometry once and applies it
+ * to any number of arrays of its shape. */
+
+typedef struct ndf_plan ndf_plan;
+
+typedef struct ndf_filter_desc {
+  int32_t dtype;             /* NDF_FLOAT32 / NDF_FLOAT64 */
+  int32_t ndim;              /* >= 1 */
+  const uint64_t* shape;     /* ndim */
+  const uint64_t* size;      /* ndim: window box */
+  const uint8_t* footprint;  /* NULL or prod(size) bytes */
+  const int64_t* origin;     /* ndim */
+  const int32_t* modes;      /* ndim: NDF_MODE_* */
+  double cval;               /* cast to dtype by the plan */
+  int32_t kind;              /* NDF_KIND_* */
+  int32_t omit_nan;          /* InvalidPolicy::Omit when nonzero */
+  int32_t ignore_inf;        /* Omit{ignore_inf} */
+  uint64_t min_count;        /* Omit{min_count} */
+  uint64_t parameter;        /* rank or ddof */
+  double percentile;         /* q for NDF_KIND_PERCENTILE */
+  int32_t moments;           /* NDF_MOMENTS_* for mean/var/std */
+} ndf_filter_desc;
+
+int ndf_plan_create(const ndf_filter_desc* desc, ndf_plan** plan);
+int ndf_plan_destroy(ndf_plan* plan);
+
+/* apply_into over device buffers, src/plan.rs:403-428. Enqueues on `stream`
+ * (a cudaStream_t, NULL = the legacy default stream) and returns without
+ * synchronizing. */
+int ndf_plan_run(ndf_plan* plan, const void* d_in, void* d_out, void* stream);
+
+/* apply_into over host buffers: copies h_in to the device, filters, copies
+ * the result to h_out and synchronizes `stream`. Device buffers are owned by
+ * the plan and reused across calls. Pinned host memory gives the fastest
+ * copies. */
+int ndf_plan_run_host(ndf_plan* plan, const void* h_in, void* h_out, void* stream);
+
+/* Split form of ndf_plan_run_host for callers that must take the input
+ * snapshot before releasing a lock (the reference snapshots under the GIL,
+ * src/pyapi/filter.rs:219-242): upload copies h_in to the plan's device
+ * input synchronously; compute filters it and copies the result to h_out. */
+int ndf_plan_upload(ndf_plan* plan, const void* h_in);
+int ndf_plan_compute_download(ndf_plan* plan, void* h_out);
+
+/* Name of the kernel family the plan dispatches to ("tile_network",
+ * "tile_radix", "histogram", "moments_tile", "generic", ...). */
+const char* ndf_plan_algorithm(const ndf_plan* plan);
+
+/* ---- Batched persistent path. Many images of uneven sizes, each with its
+ * own window, footprint and reduction, run as one persistent launch per
+ * kernel family; the launches are captured once into a CUDA graph and
+ * replayed. No counterpart in the reference (its Python callers loop). */
+
+typedef struct ndf_batch ndf_batch;
+
+/* `descs[i]` describes image i (shape, window, reduction; dtype must be
+ * float32). `d_in[i]` / `d_out[i]` are device buffers of image i. */
+int ndf_batch_create(const ndf_filter_desc* descs, int32_t count, ndf_batch** batch);
+int ndf_batch_destroy(ndf_batch* batch);
+int ndf_batch_run(ndf_batch* batch, const void* const* d_in, void* const* d_out, void* stream);
+/* Number of persistent launches one ndf_batch_run enqueues. */
+int32_t ndf_batch_launches(const ndf_batch* batch);
+
+/* Number of SMs, device name and compute capability of device 0. */
+int ndf_device_info(int32_t* sm_count, int32_t* major, int32_t* minor, char* name,
+                    size_t name_capacity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NDFILTRS_GB300_H */

@@ -1,0 +1,52 @@
+"""ndfiltrs_gb300 — GB300-native (CUDA sm_103a) windowed statistics.
+
+A drop-in for the windowed-statistics path of ndfiltrs (ysBach/ndfiltrs
+v0.2.0): NaN-aware median, rank and percentile filters (direct, sortnet and
+histogram methods) and the mean/var/std footprint reductions, for every
+footprint, origin and boundary mode. The public functions keep the
+reference's signatures and NaN/inf/min_count semantics; all computation runs
+on the GPU through the C-ABI library ``libndfiltrs_gb300.so``.
+"""
+
+from . import kernels
+from ._api import (
+    get_num_threads,
+    max_filter,
+    mean_filter,
+    median_filter,
+    min_filter,
+    nanmax_filter,
+    nanmean_filter,
+    nanmedian_filter,
+    nanmin_filter,
+    nanstd_filter,
+    nanvar_filter,
+    rank_filter,
+    std_filter,
+    var_filter,
+)
+from ._core import Plan, device_info
+from ._robust import nanpercentile_filter, percentile_filter
+
+__all__ = [
+    "Plan",
+    "device_info",
+    "get_num_threads",
+    "kernels",
+    "max_filter",
+    "mean_filter",
+    "median_filter",
+    "min_filter",
+    "nanmax_filter",
+    "nanmean_filter",
+    "nanmedian_filter",
+    "nanmin_filter",
+    "nanpercentile_filter",
+    "nanstd_filter",
+    "nanvar_filter",
+    "percentile_filter",
+    "rank_filter",
+    "std_filter",
+    "var_filter",
+]
+__version__ = "0.1.0"

@@ -1,0 +1,444 @@
+"""Native module of ndfiltrs_gb300: the GB300 replacement of ``ndfiltrs._core``.
+
+It exposes the three functions the reference's Python layer calls on the
+windowed-statistics path with the same positional signatures, argument
+meaning and error classes (src/pyapi/filter.rs:261-314,378-380 and
+src/pyapi/robust.rs:78-171 of ysBach/ndfiltrs v0.2.0):
+
+* ``window_filter(array, kind, size, footprint, origin, mode, cval, omit_nan,
+  ignore_inf, min_count, parameter)``
+* ``robust_filter(array, size, footprint, origin, mode, cval, kind, parameter,
+  omit_nan, ignore_inf, min_count, sigma_lower, sigma_upper, maxiters, center,
+  spread, estimator="sex", modify_sample_size=False, pearson=2.5)``
+* ``get_num_threads()``
+
+Every call goes through the C-ABI library ``libndfiltrs_gb300.so`` (CUDA,
+sm_103a). There is no CPU fallback: without the built library or a CUDA
+device the calls raise.
+
+Like the reference, the input is snapshotted (copied to the device) while
+the GIL is held, and the computation runs with the GIL released.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+NDF_OK = 0
+_ERRORS = {
+    1: ValueError,  # EmptyAxis
+    2: ValueError,  # InvalidConfiguration
+    3: ValueError,  # LengthMismatch
+    4: MemoryError,
+    5: OverflowError,
+    6: RuntimeError,  # CUDA runtime failure
+    7: TimeoutError,
+    8: NotImplementedError,
+    9: RuntimeError,  # no CUDA device
+}
+
+KINDS = {
+    "median": 0,
+    "median_network": 1,
+    "median_histogram": 2,
+    "mean": 3,
+    "mean_rolling": 4,
+    "min": 5,
+    "max": 6,
+    "var": 7,
+    "std": 8,
+    "rank": 9,
+    "rank_histogram": 10,
+    "percentile": 11,
+}
+MODES = {"reflect": 0, "constant": 1, "nearest": 2, "mirror": 3, "wrap": 4}
+MOMENTS = {"fp32c": 0, "fp64": 1}
+
+
+class FilterDesc(ctypes.Structure):
+    """``ndf_filter_desc`` of include/ndfiltrs_gb300.h."""
+
+    _fields_ = [
+        ("dtype", ctypes.c_int32),
+        ("ndim", ctypes.c_int32),
+        ("shape", ctypes.POINTER(ctypes.c_uint64)),
+        ("size", ctypes.POINTER(ctypes.c_uint64)),
+        ("footprint", ctypes.POINTER(ctypes.c_uint8)),
+        ("origin", ctypes.POINTER(ctypes.c_int64)),
+        ("modes", ctypes.POINTER(ctypes.c_int32)),
+        ("cval", ctypes.c_double),
+        ("kind", ctypes.c_int32),
+        ("omit_nan", ctypes.c_int32),
+        ("ignore_inf", ctypes.c_int32),
+        ("min_count", ctypes.c_uint64),
+        ("parameter", ctypes.c_uint64),
+        ("percentile", ctypes.c_double),
+        ("moments", ctypes.c_int32),
+    ]
+
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+_pylib: ctypes.PyDLL | None = None
+
+
+def library_path() -> Path:
+    return _build.LIBRARY
+
+
+def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
+    """Load the CUDA library (GIL-releasing and GIL-holding handles)."""
+    global _lib, _pylib
+    if _lib is not None and _pylib is not None:
+        return _lib, _pylib
+    with _lock:
+        if _lib is None:
+            path = library_path()
+            if not path.exists():
+                raise ImportError(
+                    f"the CUDA library {path} is not built; run "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                    "`python -m ndfiltrs_gb300._build`"
+                )
+            lib = ctypes.CDLL(str(path))
+            pylib = ctypes.PyDLL(str(path))
+            vp = ctypes.c_void_p
+            plan_p = ctypes.c_void_p
+            for handle in (lib, pylib):
+                handle.ndf_last_error.restype = ctypes.c_char_p
+                handle.ndf_plan_create.argtypes = [ctypes.POINTER(FilterDesc), ctypes.POINTER(plan_p)]
+                handle.ndf_plan_create.restype = ctypes.c_int
+                handle.ndf_plan_destroy.argtypes = [plan_p]
+                handle.ndf_plan_destroy.restype = ctypes.c_int
+                handle.ndf_plan_run.argtypes = [plan_p, vp, vp, vp]
+                handle.ndf_plan_run.restype = ctypes.c_int
+                handle.ndf_plan_run_host.argtypes = [plan_p, vp, vp, vp]
+                handle.ndf_plan_run_host.restype = ctypes.c_int
+                handle.ndf_plan_upload.argtypes = [plan_p, vp]
+                handle.ndf_plan_upload.restype = ctypes.c_int
+                handle.ndf_plan_compute_download.argtypes = [plan_p, vp]
+                handle.ndf_plan_compute_download.restype = ctypes.c_int
+                handle.ndf_plan_algorithm.argtypes = [plan_p]
+                handle.ndf_plan_algorithm.restype = ctypes.c_char_p
+                handle.ndf_get_num_threads.restype = ctypes.c_int32
+                handle.ndf_device_info.argtypes = [
+                    ctypes.POINTER(ctypes.c_int32),
+                    ctypes.POINTER(ctypes.c_int32),
+                    ctypes.POINTER(ctypes.c_int32),
+                    ctypes.c_char_p,
+                    ctypes.c_size_t,
+                ]
+                handle.ndf_device_info.restype = ctypes.c_int
+                handle.ndf_batch_create.argtypes = [
+                    ctypes.POINTER(FilterDesc),
+                    ctypes.c_int32,
+                    ctypes.POINTER(plan_p),
+                ]
+                handle.ndf_batch_create.restype = ctypes.c_int
+                handle.ndf_batch_destroy.argtypes = [plan_p]
+                handle.ndf_batch_destroy.restype = ctypes.c_int
+                handle.ndf_batch_run.argtypes = [plan_p, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
+                handle.ndf_batch_run.restype = ctypes.c_int
+                handle.ndf_batch_launches.argtypes = [plan_p]
+                handle.ndf_batch_launches.restype = ctypes.c_int32
+            _lib, _pylib = lib, pylib
+    assert _lib is not None and _pylib is not None
+    return _lib, _pylib
+
+
+def _raise(code: int, lib: ctypes.CDLL) -> None:
+    message = lib.ndf_last_error().decode(errors="replace")
+    raise _ERRORS.get(code, RuntimeError)(message)
+
+
+def _check(code: int, lib: ctypes.CDLL) -> None:
+    if code != NDF_OK:
+        _raise(code, lib)
+
+
+def _u64(values) -> ctypes.Array:
+    return (ctypes.c_uint64 * max(len(values), 1))(*[int(v) for v in values])
+
+
+def _i64(values) -> ctypes.Array:
+    return (ctypes.c_int64 * max(len(values), 1))(*[int(v) for v in values])
+
+
+def _i32(values) -> ctypes.Array:
+    return (ctypes.c_int32 * max(len(values), 1))(*[int(v) for v in values])
+
+
+class Plan:
+    """A validated filter plan (``WindowFilter::new``, src/plan.rs:260-324).
+
+    The plan keeps its device tables and, for host-buffer runs, its device
+    input/output buffers until it is closed.
+    """
+
+    def __init__(
+        self,
+        shape,
+        dtype,
+        kind: str,
+        size,
+        footprint=None,
+        origin=None,
+        mode=None,
+        cval: float = 0.0,
+        omit_nan: bool = False,
+        ignore_inf: bool = False,
+        min_count: int = 1,
+        parameter: int = 0,
+        percentile: float = 50.0,
+        moments: str | None = None,
+    ) -> None:
+        lib, _ = _load()
+        shape = tuple(int(v) for v in shape)
+        ndim = len(shape)
+        dtype = np.dtype(dtype)
+        if dtype not in (np.float32, np.float64):
+            raise TypeError("array dtype must be float32 or float64")
+        size = list(size)
+        origin = [0] * ndim if origin is None else list(origin)
+        mode = ["reflect"] * ndim if mode is None else list(mode)
+        if len(size) != ndim or len(origin) != ndim or len(mode) != ndim:
+            raise ValueError("array, window, origin, and mode must have equal rank")
+        modes = []
+        for name in mode:
+            if name not in MODES:
+                raise ValueError("unsupported boundary mode")
+            modes.append(MODES[name])
+        if kind not in KINDS:
+            raise ValueError("unsupported window filter kind")
+        self._keep = []
+        volume = 1
+        for value in size:
+            volume *= int(value)
+        fp_ptr = None
+        if footprint is not None:
+            mask = np.ascontiguousarray(np.asarray(footprint, dtype=bool).ravel(), dtype=np.uint8)
+            if mask.size != volume:
+                raise ValueError("input length does not match the configured shape")
+            self._keep.append(mask)
+            fp_ptr = mask.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+        if moments is None:
+            import os
+
+            moments = os.environ.get("NDF_MOMENTS", "fp32c")
+        if moments not in MOMENTS:
+            raise ValueError("moments must be 'fp32c' or 'fp64'")
+        shape_a, size_a, origin_a, modes_a = _u64(shape), _u64(size), _i64(origin), _i32(modes)
+        self._keep += [shape_a, size_a, origin_a, modes_a]
+        desc = FilterDesc(
+            0 if dtype == np.float32 else 1,
+            ndim,
+            shape_a,
+            size_a,
+            fp_ptr,
+            origin_a,
+            modes_a,
+            float(cval),
+            KINDS[kind],
+            int(bool(omit_nan)),
+            int(bool(ignore_inf)),
+            int(min_count),
+            int(parameter),
+            float(percentile),
+            MOMENTS[moments],
+        )
+        handle = ctypes.c_void_p()
+        _check(lib.ndf_plan_create(ctypes.byref(desc), ctypes.byref(handle)), lib)
+        self._handle = handle
+        self.shape = shape
+        self.dtype = dtype
+        self.kind = kind
+
+    @property
+    def algorithm(self) -> str:
+        lib, _ = _load()
+        return lib.ndf_plan_algorithm(self._handle).decode()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._handle
+
+    def _check_array(self, array: np.ndarray) -> None:
+        if array.shape != self.shape or array.dtype != self.dtype:
+            raise ValueError("input length does not match the configured shape")
+
+    def run_host(self, array: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
+        """Snapshot ``array`` to the device under the GIL, filter, copy back."""
+        lib, pylib = _load()
+        self._check_array(array)
+        if not array.flags.c_contiguous:
+            raise ValueError("native input must be C-contiguous")
+        if out is None:
+            out = np.zeros(self.shape, dtype=self.dtype)
+        if array.size == 0:
+            return out
+        _check(pylib.ndf_plan_upload(self._handle, array.ctypes.data), lib)
+        _check(lib.ndf_plan_compute_download(self._handle, out.ctypes.data), lib)
+        return out
+
+    def run_host_async(self, array: np.ndarray, out: np.ndarray, stream: int = 0) -> None:
+        """H2D + kernel + D2H on ``stream`` (synchronized before returning)."""
+        lib, _ = _load()
+        _check(lib.ndf_plan_run_host(self._handle, array.ctypes.data, out.ctypes.data, stream), lib)
+
+    def run_device(self, d_in: int, d_out: int, stream: int = 0) -> None:
+        """Enqueue the filter over device pointers on ``stream``."""
+        lib, _ = _load()
+        _check(lib.ndf_plan_run(self._handle, d_in, d_out, stream), lib)
+
+    def close(self) -> None:
+        if getattr(self, "_handle", None) is not None and self._handle.value:
+            lib, _ = _load()
+            lib.ndf_plan_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self) -> "Plan":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+
+def _typed_array(array: object) -> np.ndarray:
+    if not isinstance(array, np.ndarray) or array.dtype not in (np.float32, np.float64):
+        raise TypeError("argument 'array': expected a float32 or float64 numpy.ndarray")
+    return array
+
+
+def window_filter(
+    array,
+    kind,
+    size,
+    footprint,
+    origin,
+    mode,
+    cval,
+    omit_nan,
+    ignore_inf,
+    min_count,
+    parameter,
+):
+    """Apply one window reduction (``_core.window_filter``)."""
+    array = _typed_array(array)
+    if not array.flags.c_contiguous:
+        raise ValueError("native input must be C-contiguous")
+    cval = float(np.float32(cval)) if array.dtype == np.float32 else float(cval)
+    with Plan(
+        array.shape,
+        array.dtype,
+        kind,
+        size,
+        footprint=footprint,
+        origin=origin,
+        mode=mode,
+        cval=cval,
+        omit_nan=omit_nan,
+        ignore_inf=ignore_inf,
+        min_count=min_count,
+        parameter=parameter,
+    ) as plan:
+        return plan.run_host(array)
+
+
+_ROBUST_OUT_OF_SCOPE = (
+    "mad",
+    "mode",
+    "biweight_location",
+    "biweight_scale",
+    "sigma_mean",
+    "sigma_median",
+    "sigma_mode",
+)
+
+
+def robust_filter(
+    array,
+    size,
+    footprint,
+    origin,
+    mode,
+    cval,
+    kind,
+    parameter,
+    omit_nan,
+    ignore_inf,
+    min_count,
+    sigma_lower,
+    sigma_upper,
+    maxiters,
+    center,
+    spread,
+    estimator="sex",
+    modify_sample_size=False,
+    pearson=2.5,
+):
+    """Apply one robust window statistic (``_core.robust_filter``).
+
+    Only ``kind="percentile"`` runs on this library; the other robust kinds
+    of the reference (MAD, sigma clipping, mode, biweight) raise
+    NotImplementedError.
+    """
+    if kind in _ROBUST_OUT_OF_SCOPE:
+        raise NotImplementedError(f"robust kind {kind!r} is outside this library's scope")
+    if kind != "percentile":
+        raise ValueError("unsupported robust filter kind")
+    if not omit_nan and (ignore_inf or min_count != 1):
+        raise ValueError("ignore_inf and min_count require NaN omission")
+    array = _typed_array(array)
+    if not array.flags.c_contiguous or not array.flags.aligned:
+        raise ValueError("native input must be aligned and C-contiguous")
+    with Plan(
+        array.shape,
+        array.dtype,
+        "percentile",
+        size,
+        footprint=footprint,
+        origin=origin,
+        mode=mode,
+        cval=float(cval),
+        omit_nan=omit_nan,
+        ignore_inf=ignore_inf,
+        min_count=min_count,
+        percentile=float(parameter),
+    ) as plan:
+        return plan.run_host(array)
+
+
+def get_num_threads() -> int:
+    """Number of streaming multiprocessors the library spreads work over."""
+    lib, _ = _load()
+    count = int(lib.ndf_get_num_threads())
+    if count <= 0:
+        _raise(9, lib)
+    return count
+
+
+def device_info() -> dict:
+    lib, _ = _load()
+    sms, major, minor = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    name = ctypes.create_string_buffer(256)
+    _check(
+        lib.ndf_device_info(ctypes.byref(sms), ctypes.byref(major), ctypes.byref(minor), name, 256),
+        lib,
+    )
+    return {
+        "sm_count": sms.value,
+        "capability": (major.value, minor.value),
+        "name": name.value.decode(),
+    }

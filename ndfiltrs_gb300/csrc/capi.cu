@@ -1,0 +1,677 @@
+// C-ABI of the GB300 windowed-statistics library: plan validation and
+// dispatch, host-buffer runs, and the one-shot entry points that replace the
+// reference's `_core.window_filter` / `_core.robust_filter`.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "../../include/ndfiltrs_gb300.h"
+#include "common.cuh"
+#include "plan.h"
+
+struct ndf_plan {
+  ndf::Plan p;
+};
+
+namespace ndf {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& message) {
+  g_error = message;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(NDF_ERR_CUDA, std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+
+const char* algo_name(Algo a) {
+  switch (a) {
+    case Algo::kEmpty:
+      return "empty";
+    case Algo::kTileNetwork:
+      return "tile_network";
+    case Algo::kTileRadix:
+      return "tile_radix";
+    case Algo::kGenericSelect:
+      return "generic_select";
+    case Algo::kHistogram:
+      return "histogram";
+    case Algo::kMomentsTile:
+      return "moments_tile";
+    case Algo::kMomentsGeneric:
+      return "moments_generic";
+  }
+  return "unknown";
+}
+
+namespace {
+
+struct DeviceState {
+  std::once_flag once;
+  int status = NDF_ERR_NO_DEVICE;
+  std::string message;
+  int sm_count = 0;
+  int smem_optin = 0;
+};
+
+DeviceState& device_state() {
+  static DeviceState s;
+  return s;
+}
+
+// Reads the current device's properties once; every compute entry point
+// fails with NDF_ERR_NO_DEVICE when no CUDA device can be used.
+int ensure_device(int* device, int* sm_count, int* smem_optin) {
+  DeviceState& s = device_state();
+  std::call_once(s.once, [&] {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+      s.status = NDF_ERR_NO_DEVICE;
+      s.message = std::string("no usable CUDA device: ") +
+                  (e != cudaSuccess ? cudaGetErrorString(e) : "device count is zero");
+      cudaGetLastError();
+      return;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&s.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    s.status = NDF_OK;
+  });
+  if (s.status != NDF_OK) return fail(s.status, s.message);
+  cudaGetDevice(device);
+  *sm_count = s.sm_count;
+  *smem_optin = s.smem_optin;
+  return NDF_OK;
+}
+
+bool checked_mul(unsigned long long a, unsigned long long b, unsigned long long* out) {
+  if (a != 0 && b > std::numeric_limits<unsigned long long>::max() / a) return false;
+  *out = a * b;
+  return true;
+}
+
+bool is_selection(int kind) {
+  switch (kind) {
+    case kMedian:
+    case kMedianNetwork:
+    case kMedianHistogram:
+    case kMin:
+    case kMax:
+    case kRank:
+    case kRankHistogram:
+    case kPercentile:
+      return true;
+    default:
+      return false;
+  }
+}
+
+bool is_moment(int kind) { return kind == kMean || kind == kVar || kind == kStd; }
+
+// Canonical 3-D tile geometry for rank 1-3 arrays.
+void setup_tile(Plan& p) {
+  int pad = 3 - p.ndim;
+  long long shape3[3], size3[3], anchor3[3];
+  int mode3[3];
+  for (int a = 0; a < 3; ++a) {
+    int src = a - pad;
+    if (src < 0) {
+      shape3[a] = 1;
+      size3[a] = 1;
+      anchor3[a] = 0;
+      mode3[a] = kNearest;
+    } else {
+      shape3[a] = p.shape[src];
+      size3[a] = p.size[src];
+      anchor3[a] = p.size[src] / 2 + p.origin[src];
+      mode3[a] = p.modes[src];
+    }
+  }
+  Geom3& g = p.tile.g;
+  g.D = shape3[0];
+  g.H = shape3[1];
+  g.W = shape3[2];
+  g.kd = (int)size3[0];
+  g.kh = (int)size3[1];
+  g.kw = (int)size3[2];
+  g.az = (int)anchor3[0];
+  g.ay = (int)anchor3[1];
+  g.ax = (int)anchor3[2];
+  g.mz = mode3[0];
+  g.my = mode3[1];
+  g.mx = mode3[2];
+  Tile& t = p.tile.t;
+  if (g.H == 1) {
+    t.TW = 256;
+    t.TH = 1;
+  } else {
+    t.TW = 32;
+    t.TH = 8;
+  }
+  t.SW = t.TW + g.kw - 1;
+  t.SH = t.TH + g.kh - 1;
+  t.tiles_x = (g.W + t.TW - 1) / t.TW;
+  t.tiles_y = (g.H + t.TH - 1) / t.TH;
+  t.tiles = t.tiles_x * t.tiles_y * g.D;
+  p.tile.r = p.r;
+  // Box positions of the taps in the canonical (z, y, x) box.
+  p.box_taps.clear();
+  long long volume = (long long)g.kd * g.kh * g.kw;
+  for (long long e = 0; e < volume; ++e) {
+    if (!p.footprint.empty() && !p.footprint[e]) continue;
+    int kx = (int)(e % g.kw);
+    int ky = (int)((e / g.kw) % g.kh);
+    int kz = (int)(e / ((long long)g.kw * g.kh));
+    p.box_taps.push_back(kz);
+    p.box_taps.push_back(ky);
+    p.box_taps.push_back(kx);
+  }
+}
+
+int setup_generic(Plan& p) {
+  if (p.ndim > kMaxGenericRank)
+    return fail(NDF_ERR_UNSUPPORTED, "arrays with more than 32 dimensions are not supported");
+  GenericArgs& a = p.generic;
+  a.rank = p.ndim;
+  a.n_out = p.n_out;
+  long long stride = 1;
+  for (int d = p.ndim - 1; d >= 0; --d) {
+    a.shape[d] = p.shape[d];
+    a.stride[d] = stride;
+    stride *= p.shape[d];
+    a.mode[d] = p.modes[d];
+    a.low[d] = std::numeric_limits<long long>::max();
+    a.high[d] = std::numeric_limits<long long>::min();
+  }
+  a.r = p.r;
+  std::vector<long long> table(p.taps);
+  size_t count = (size_t)p.r.count;
+  for (size_t t = 0; t < count; ++t) {
+    long long flat = 0;
+    for (int d = 0; d < p.ndim; ++d) {
+      long long off = p.taps[t * p.ndim + d];
+      flat += off * a.stride[d];
+      a.low[d] = std::min(a.low[d], off);
+      a.high[d] = std::max(a.high[d], off);
+    }
+    table.push_back(flat);
+  }
+  cudaError_t e = cudaMalloc(&p.d_gen_taps, table.size() * sizeof(long long));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(taps)");
+  e = cudaMemcpy(p.d_gen_taps, table.data(), table.size() * sizeof(long long), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(taps)");
+  return NDF_OK;
+}
+
+int upload_tile_taps(Plan& p) {
+  const Tile& t = p.tile.t;
+  std::vector<int32_t> offs((size_t)p.r.count);
+  for (int i = 0; i < p.r.count; ++i) {
+    const int* bt = &p.box_taps[(size_t)i * 3];
+    offs[i] = (bt[0] * t.SH + bt[1]) * t.SW + bt[2];
+  }
+  cudaError_t e = cudaMalloc(&p.d_tile_taps, offs.size() * sizeof(int32_t));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(tile taps)");
+  e = cudaMemcpy(p.d_tile_taps, offs.data(), offs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tile taps)");
+  return NDF_OK;
+}
+
+void release(Plan& p) {
+  if (p.d_tile_taps) cudaFree(p.d_tile_taps);
+  if (p.d_gen_taps) cudaFree(p.d_gen_taps);
+  if (p.d_in) cudaFree(p.d_in);
+  if (p.d_out) cudaFree(p.d_out);
+  if (p.d_scratch) cudaFree(p.d_scratch);
+  if (p.d_status) cudaFree(p.d_status);
+  p.d_tile_taps = nullptr;
+  p.d_gen_taps = nullptr;
+  p.d_in = p.d_out = p.d_scratch = nullptr;
+  p.d_status = nullptr;
+}
+
+// Validation in the reference's order: Window::new (src/window.rs:44-137),
+// FilterConfig::from_window (src/filter_nd.rs:35-51), WindowFilter::new
+// (src/plan.rs:260-324), RobustReduction::validate (src/robust.rs:187-240).
+int build_plan(const ndf_filter_desc* d, Plan& p) {
+  if (!d) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing filter description");
+  if (d->dtype != NDF_FLOAT32 && d->dtype != NDF_FLOAT64)
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "array dtype must be float32 or float64");
+  if (d->ndim <= 0)
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "filtering requires at least one dimension");
+  if (!d->shape || !d->size || !d->origin || !d->modes)
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "missing shape, size, origin or mode");
+  p.dtype = d->dtype;
+  p.ndim = d->ndim;
+  p.shape.assign(d->ndim, 0);
+  p.size.assign(d->ndim, 0);
+  p.origin.assign(d->ndim, 0);
+  p.modes.assign(d->ndim, 0);
+  for (int a = 0; a < d->ndim; ++a) {
+    if (d->shape[a] > (uint64_t)std::numeric_limits<long long>::max() ||
+        d->size[a] > (uint64_t)std::numeric_limits<int32_t>::max())
+      return fail(NDF_ERR_OVERFLOW, "shape or index arithmetic overflowed");
+    p.shape[a] = (long long)d->shape[a];
+    p.size[a] = (long long)d->size[a];
+    p.origin[a] = d->origin[a];
+    p.modes[a] = d->modes[a];
+    if (d->modes[a] < 0 || d->modes[a] > 4)
+      return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported boundary mode");
+  }
+  for (int a = 0; a < d->ndim; ++a)
+    if (p.size[a] == 0) return fail(NDF_ERR_INVALID_CONFIGURATION, "window sizes must be positive");
+  unsigned long long volume = 1;
+  for (int a = 0; a < d->ndim; ++a)
+    if (!checked_mul(volume, (unsigned long long)p.size[a], &volume))
+      return fail(NDF_ERR_OVERFLOW, "shape or index arithmetic overflowed");
+  for (int a = 0; a < d->ndim; ++a) {
+    long long length = p.size[a];
+    if (p.origin[a] < -(length / 2) || p.origin[a] > (length - 1) / 2)
+      return fail(NDF_ERR_INVALID_CONFIGURATION,
+                  "origin must satisfy -(size // 2) <= origin <= (size - 1) // 2");
+  }
+  unsigned long long n_out = 1;
+  for (int a = 0; a < d->ndim; ++a)
+    if (!checked_mul(n_out, (unsigned long long)p.shape[a], &n_out) ||
+        n_out > (unsigned long long)std::numeric_limits<long long>::max())
+      return fail(NDF_ERR_OVERFLOW, "shape or index arithmetic overflowed");
+  p.n_out = (long long)n_out;
+  if (volume > (1ull << 31)) return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+  size_t count = 0;
+  if (d->footprint) {
+    p.footprint.assign(d->footprint, d->footprint + volume);
+    for (auto v : p.footprint) count += v != 0;
+  } else {
+    count = (size_t)volume;
+  }
+  if (count == 0)
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "footprint must select at least one element");
+  const int kind = d->kind;
+  if (kind == kMeanRolling)
+    return fail(NDF_ERR_UNSUPPORTED,
+                "kind 'mean_rolling' (method='boxcar') is outside this library's scope");
+  if (!is_selection(kind) && !is_moment(kind))
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported window filter kind");
+  Reduce& r = p.r;
+  r.kind = kind;
+  r.omit = d->omit_nan != 0;
+  r.drop_inf = r.omit && d->ignore_inf != 0;
+  r.count = (int)count;
+  r.min_count = r.omit ? (long long)d->min_count : 1;
+  r.param = (long long)std::min<uint64_t>(d->parameter, (uint64_t)std::numeric_limits<long long>::max());
+  r.q = d->percentile;
+  r.cval = d->dtype == NDF_FLOAT32 ? (double)(float)d->cval : d->cval;
+  r.moments = d->moments == NDF_MOMENTS_FP64 ? 1 : 0;
+  if (kind == kPercentile) {
+    if (!std::isfinite(r.q) || r.q < 0.0 || r.q > 100.0)
+      return fail(NDF_ERR_INVALID_CONFIGURATION,
+                  "percentile must be finite and between zero and 100");
+    if (r.omit && (d->min_count == 0 || d->min_count > count))
+      return fail(NDF_ERR_INVALID_CONFIGURATION,
+                  "min_count must be between one and the number of window elements");
+  } else if (r.omit && (d->min_count == 0 || d->min_count > count)) {
+    return fail(NDF_ERR_INVALID_CONFIGURATION,
+                "min_count must be between 1 and the number of window elements");
+  }
+  const bool hist_kind = kind == kMedianHistogram || kind == kRankHistogram;
+  if (hist_kind && !p.footprint.empty())
+    return fail(NDF_ERR_INVALID_CONFIGURATION,
+                "histogram reductions require rectangular size, not footprint");
+  // Taps in C order over the footprint (src/window.rs:96-125).
+  p.taps.clear();
+  p.taps.reserve(count * d->ndim);
+  std::vector<long long> index(d->ndim, 0);
+  for (unsigned long long e = 0; e < volume; ++e) {
+    if (p.footprint.empty() || p.footprint[e]) {
+      for (int a = 0; a < d->ndim; ++a)
+        p.taps.push_back(index[a] - (p.size[a] / 2 + p.origin[a]));
+    }
+    for (int a = d->ndim - 1; a >= 0; --a) {
+      if (++index[a] < p.size[a]) break;
+      index[a] = 0;
+    }
+  }
+  return NDF_OK;
+}
+
+int choose_algorithm(Plan& p, int smem_limit) {
+  if (p.n_out == 0) {
+    p.algo = Algo::kEmpty;
+    return NDF_OK;
+  }
+  const bool tileable = p.ndim <= 3 && p.r.count <= (1 << 24);
+  if (tileable) setup_tile(p);
+  if (is_moment(p.r.kind)) {
+    if (tileable) {
+      size_t smem = tile_moments_smem(p, p.tile.t);
+      if (smem <= (size_t)smem_limit) {
+        p.algo = Algo::kMomentsTile;
+        p.smem_bytes = smem;
+        return upload_tile_taps(p);
+      }
+    }
+    p.algo = Algo::kMomentsGeneric;
+    return setup_generic(p);
+  }
+  if (tileable) {
+    const bool hist_kind = p.r.kind == kMedianHistogram || p.r.kind == kRankHistogram;
+    const bool rank_like = p.r.kind == kMedian || p.r.kind == kMedianNetwork ||
+                           p.r.kind == kRank || hist_kind;
+    if (rank_like && p.footprint.empty() && histogram_supported(p) &&
+        (hist_kind || network_width_for(p.dtype, p.r.count) == 0)) {
+      histogram_configure(p);
+      p.algo = Algo::kHistogram;
+      p.smem_bytes = histogram_smem(p);
+      if (p.smem_bytes <= (size_t)smem_limit) return NDF_OK;
+    }
+    size_t smem = tile_select_smem(p, p.tile.t);
+    if (smem <= (size_t)smem_limit) {
+      int width = network_width_for(p.dtype, p.r.count);
+      p.smem_bytes = smem;
+      if (width > 0) {
+        p.algo = Algo::kTileNetwork;
+        p.network = width;
+        return NDF_OK;
+      }
+      p.algo = Algo::kTileRadix;
+      return upload_tile_taps(p);
+    }
+  }
+  p.algo = Algo::kGenericSelect;
+  return setup_generic(p);
+}
+
+int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  switch (p.algo) {
+    case Algo::kEmpty:
+      return NDF_OK;
+    case Algo::kTileNetwork:
+    case Algo::kTileRadix:
+      e = launch_tile_select(p, in, out, s);
+      break;
+    case Algo::kGenericSelect:
+      e = launch_generic_select(p, in, out, s);
+      break;
+    case Algo::kHistogram:
+      e = launch_histogram(p, in, out, s);
+      break;
+    case Algo::kMomentsTile:
+      e = launch_tile_moments(p, in, out, s);
+      break;
+    case Algo::kMomentsGeneric:
+      e = launch_generic_moments(p, in, out, s);
+      break;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, algo_name(p.algo));
+  return NDF_OK;
+}
+
+size_t element_bytes(const Plan& p) { return p.dtype == NDF_FLOAT32 ? 4 : 8; }
+
+int ensure_buffers(Plan& p) {
+  size_t bytes = (size_t)p.n_out * element_bytes(p);
+  if (bytes == 0 || (p.d_in && p.buffer_bytes >= bytes)) return NDF_OK;
+  if (p.d_in) cudaFree(p.d_in);
+  if (p.d_out) cudaFree(p.d_out);
+  p.d_in = p.d_out = nullptr;
+  cudaError_t e = cudaMalloc(&p.d_in, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&p.d_out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    if (p.d_in) cudaFree(p.d_in);
+    p.d_in = nullptr;
+    return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+  }
+  p.buffer_bytes = bytes;
+  return NDF_OK;
+}
+
+int parse_mode(const char* name, int32_t* out) {
+  static const char* names[] = {"reflect", "constant", "nearest", "mirror", "wrap"};
+  for (int i = 0; i < 5; ++i)
+    if (name && std::strcmp(name, names[i]) == 0) {
+      *out = i;
+      return NDF_OK;
+    }
+  return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported boundary mode");
+}
+
+int parse_window_kind(const char* kind, int32_t* out) {
+  static const struct {
+    const char* name;
+    int32_t kind;
+  } table[] = {{"median", kMedian},         {"median_network", kMedianNetwork},
+               {"median_histogram", kMedianHistogram}, {"mean", kMean},
+               {"mean_rolling", kMeanRolling}, {"min", kMin},
+               {"max", kMax},               {"var", kVar},
+               {"std", kStd},               {"rank", kRank},
+               {"rank_histogram", kRankHistogram}};
+  for (const auto& e : table)
+    if (kind && std::strcmp(kind, e.name) == 0) {
+      *out = e.kind;
+      return NDF_OK;
+    }
+  return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported window filter kind");
+}
+
+int moments_default() {
+  const char* env = std::getenv("NDF_MOMENTS");
+  if (env && std::strcmp(env, "fp64") == 0) return NDF_MOMENTS_FP64;
+  return NDF_MOMENTS_FP32C;
+}
+
+int one_shot(const ndf_filter_desc& d, const void* h_in, void* h_out) {
+  ndf_plan* plan = nullptr;
+  int rc = ndf_plan_create(&d, &plan);
+  if (rc != NDF_OK) return rc;
+  rc = ndf_plan_run_host(plan, h_in, h_out, nullptr);
+  std::string message = g_error;
+  ndf_plan_destroy(plan);
+  if (rc != NDF_OK) g_error = message;
+  return rc;
+}
+
+}  // namespace
+}  // namespace ndf
+
+using namespace ndf;
+
+extern "C" {
+
+const char* ndf_last_error(void) { return g_error.c_str(); }
+
+int ndf_device_info(int32_t* sm_count, int32_t* major, int32_t* minor, char* name,
+                    size_t name_capacity) {
+  int dev, sms, smem;
+  int rc = ensure_device(&dev, &sms, &smem);
+  if (rc != NDF_OK) return rc;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
+  if (sm_count) *sm_count = prop.multiProcessorCount;
+  if (major) *major = prop.major;
+  if (minor) *minor = prop.minor;
+  if (name && name_capacity) {
+    std::strncpy(name, prop.name, name_capacity - 1);
+    name[name_capacity - 1] = 0;
+  }
+  return NDF_OK;
+}
+
+int32_t ndf_get_num_threads(void) {
+  int dev, sms, smem;
+  if (ensure_device(&dev, &sms, &smem) != NDF_OK) return 0;
+  return sms;
+}
+
+int ndf_plan_create(const ndf_filter_desc* desc, ndf_plan** out) {
+  if (!out) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan output pointer");
+  *out = nullptr;
+  ndf_plan* plan = new (std::nothrow) ndf_plan();
+  if (!plan) return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+  int rc = build_plan(desc, plan->p);
+  if (rc == NDF_OK && plan->p.n_out > 0) {
+    int smem_limit = 0;
+    rc = ensure_device(&plan->p.device, &plan->p.sm_count, &smem_limit);
+    if (rc == NDF_OK) rc = choose_algorithm(plan->p, smem_limit);
+  } else if (rc == NDF_OK) {
+    plan->p.algo = Algo::kEmpty;
+  }
+  if (rc != NDF_OK) {
+    release(plan->p);
+    delete plan;
+    return rc;
+  }
+  *out = plan;
+  return NDF_OK;
+}
+
+int ndf_plan_destroy(ndf_plan* plan) {
+  if (!plan) return NDF_OK;
+  release(plan->p);
+  delete plan;
+  return NDF_OK;
+}
+
+const char* ndf_plan_algorithm(const ndf_plan* plan) {
+  return plan ? algo_name(plan->p.algo) : "none";
+}
+
+int ndf_plan_run(ndf_plan* plan, const void* d_in, void* d_out, void* stream) {
+  if (!plan) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan");
+  if (plan->p.n_out == 0) return NDF_OK;
+  if (!d_in || !d_out) return fail(NDF_ERR_LENGTH_MISMATCH, "missing input or output buffer");
+  if (d_in == d_out) return fail(NDF_ERR_INVALID_CONFIGURATION, "input and output must not overlap");
+  return run_plan(plan->p, d_in, d_out, (cudaStream_t)stream);
+}
+
+int ndf_plan_upload(ndf_plan* plan, const void* h_in) {
+  if (!plan) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan");
+  Plan& p = plan->p;
+  if (p.n_out == 0) return NDF_OK;
+  int rc = ensure_buffers(p);
+  if (rc != NDF_OK) return rc;
+  cudaError_t e = cudaMemcpy(p.d_in, h_in, (size_t)p.n_out * element_bytes(p), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(input)");
+  return NDF_OK;
+}
+
+int ndf_plan_compute_download(ndf_plan* plan, void* h_out) {
+  if (!plan) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan");
+  Plan& p = plan->p;
+  if (p.n_out == 0) return NDF_OK;
+  if (!p.d_in) return fail(NDF_ERR_INVALID_CONFIGURATION, "no input was uploaded");
+  int rc = run_plan(p, p.d_in, p.d_out, nullptr);
+  if (rc != NDF_OK) return rc;
+  cudaError_t e = cudaMemcpy(h_out, p.d_out, (size_t)p.n_out * element_bytes(p), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(output)");
+  return NDF_OK;
+}
+
+int ndf_plan_run_host(ndf_plan* plan, const void* h_in, void* h_out, void* stream) {
+  if (!plan) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan");
+  Plan& p = plan->p;
+  if (p.n_out == 0) return NDF_OK;
+  int rc = ensure_buffers(p);
+  if (rc != NDF_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t bytes = (size_t)p.n_out * element_bytes(p);
+  cudaError_t e = cudaMemcpyAsync(p.d_in, h_in, bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(input)");
+  rc = run_plan(p, p.d_in, p.d_out, s);
+  if (rc != NDF_OK) return rc;
+  e = cudaMemcpyAsync(h_out, p.d_out, bytes, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(output)");
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  return NDF_OK;
+}
+
+int ndf_window_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim,
+                      const uint64_t* shape, const char* kind, const uint64_t* size,
+                      const uint8_t* footprint, const int64_t* origin,
+                      const char* const* modes, double cval, int32_t omit_nan,
+                      int32_t ignore_inf, uint64_t min_count, uint64_t parameter) {
+  int32_t k;
+  int rc = parse_window_kind(kind, &k);
+  if (rc != NDF_OK) return rc;
+  if (ndim <= 0) return fail(NDF_ERR_INVALID_CONFIGURATION, "filtering requires at least one dimension");
+  std::vector<int32_t> m(ndim);
+  for (int a = 0; a < ndim; ++a) {
+    rc = parse_mode(modes ? modes[a] : nullptr, &m[a]);
+    if (rc != NDF_OK) return rc;
+  }
+  ndf_filter_desc d{};
+  d.dtype = dtype;
+  d.ndim = ndim;
+  d.shape = shape;
+  d.size = size;
+  d.footprint = footprint;
+  d.origin = origin;
+  d.modes = m.data();
+  d.cval = cval;
+  d.kind = k;
+  d.omit_nan = omit_nan;
+  d.ignore_inf = ignore_inf;
+  d.min_count = min_count;
+  d.parameter = parameter;
+  d.percentile = 50.0;
+  d.moments = moments_default();
+  return one_shot(d, h_in, h_out);
+}
+
+int ndf_robust_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim,
+                      const uint64_t* shape, const uint64_t* size, const uint8_t* footprint,
+                      const int64_t* origin, const char* const* modes, double cval,
+                      const char* kind, double parameter, int32_t omit_nan,
+                      int32_t ignore_inf, uint64_t min_count) {
+  static const char* other_kinds[] = {"mad",        "mode",         "biweight_location",
+                                      "biweight_scale", "sigma_mean", "sigma_median",
+                                      "sigma_mode"};
+  if (!kind) return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported robust filter kind");
+  if (std::strcmp(kind, "percentile") != 0) {
+    for (const char* other : other_kinds)
+      if (std::strcmp(kind, other) == 0)
+        return fail(NDF_ERR_UNSUPPORTED,
+                    std::string("robust kind '") + kind + "' is outside this library's scope");
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported robust filter kind");
+  }
+  if (!omit_nan && (ignore_inf || min_count != 1))
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "ignore_inf and min_count require NaN omission");
+  if (ndim <= 0) return fail(NDF_ERR_INVALID_CONFIGURATION, "filtering requires at least one dimension");
+  std::vector<int32_t> m(ndim);
+  for (int a = 0; a < ndim; ++a) {
+    int rc = parse_mode(modes ? modes[a] : nullptr, &m[a]);
+    if (rc != NDF_OK) return rc;
+  }
+  ndf_filter_desc d{};
+  d.dtype = dtype;
+  d.ndim = ndim;
+  d.shape = shape;
+  d.size = size;
+  d.footprint = footprint;
+  d.origin = origin;
+  d.modes = m.data();
+  d.cval = cval;
+  d.kind = kPercentile;
+  d.omit_nan = omit_nan;
+  d.ignore_inf = ignore_inf;
+  d.min_count = min_count;
+  d.percentile = parameter;
+  d.moments = NDF_MOMENTS_FP32C;
+  return one_shot(d, h_in, h_out);
+}
+
+}  // extern "C"

@@ -1,0 +1,306 @@
+// Device-side building blocks shared by every kernel of the GB300 library:
+// order-preserving keys, boundary mapping, the median midpoint and percentile
+// interpolation contracts, compensated sums and canonical-NaN stores.
+//
+// Every float64 operation whose result must match the reference bit for bit
+// uses a round-to-nearest intrinsic (__dadd_rn, __dmul_rn, ...), which nvcc
+// never contracts into an FMA.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ndf {
+
+enum Mode : int32_t { kReflect = 0, kConstant = 1, kNearest = 2, kMirror = 3, kWrap = 4 };
+
+enum Kind : int32_t {
+  kMedian = 0,
+  kMedianNetwork = 1,
+  kMedianHistogram = 2,
+  kMean = 3,
+  kMeanRolling = 4,
+  kMin = 5,
+  kMax = 6,
+  kVar = 7,
+  kStd = 8,
+  kRank = 9,
+  kRankHistogram = 10,
+  kPercentile = 11,
+};
+
+// Error flags a kernel can raise in the plan's device status word.
+enum DeviceError : uint32_t {
+  kDevOk = 0,
+  kDevSupportOverflow = 1u << 0,  // a histogram support exceeded its rank codes
+  kDevScratchOverflow = 1u << 1,  // a kernel ran out of its scratch capacity
+};
+
+// ---------------------------------------------------------------------------
+// Order-preserving unsigned keys. Unsigned key order equals IEEE total order
+// (-0 before +0) for every non-NaN value. The reference encodes the same order
+// as signed integers (src/median_network.rs:21-31); an unsigned key keeps
+// the sentinel (all ones) above +inf, so a dropped sample sorts last.
+
+template <typename T>
+struct KeyOf;
+
+template <>
+struct KeyOf<float> {
+  using K = uint32_t;
+  static constexpr uint32_t kSentinel = 0xFFFFFFFFu;
+  __device__ __forceinline__ static uint32_t key(float v) {
+    uint32_t b = __float_as_uint(v);
+    return b ^ ((uint32_t)((int32_t)b >> 31) | 0x80000000u);
+  }
+  __device__ __forceinline__ static float value(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k ^ 0x80000000u) : ~k;
+    return __uint_as_float(b);
+  }
+};
+
+template <>
+struct KeyOf<double> {
+  using K = unsigned long long;
+  static constexpr unsigned long long kSentinel = ~0ull;
+  __device__ __forceinline__ static unsigned long long key(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return b ^ ((unsigned long long)((long long)b >> 63) | 0x8000000000000000ull);
+  }
+  __device__ __forceinline__ static double value(unsigned long long k) {
+    unsigned long long b = (k & 0x8000000000000000ull) ? (k ^ 0x8000000000000000ull) : ~k;
+    return __longlong_as_double((long long)b);
+  }
+};
+
+// A sample is dropped (keyed as the sentinel) when it is NaN, or infinite
+// while infinities are ignored (src/reduction.rs:85-101,
+// src/median_network.rs:40-63). Under the propagate policy a dropped NaN
+// makes the window NaN; the caller detects it from the retained count.
+template <typename T>
+__device__ __forceinline__ typename KeyOf<T>::K sample_key(T v, bool drop_inf) {
+  bool drop = isnan(v) || (drop_inf && isinf(v));
+  return drop ? KeyOf<T>::kSentinel : KeyOf<T>::key(v);
+}
+
+// ---------------------------------------------------------------------------
+// Canonical NaN stores: 0x7fc00000 / 0x7ff8000000000000 (docs/semantics.md).
+
+__device__ __forceinline__ float canonical(float v) {
+  return isnan(v) ? __uint_as_float(0x7fc00000u) : v;
+}
+__device__ __forceinline__ double canonical(double v) {
+  return isnan(v) ? __longlong_as_double(0x7ff8000000000000ll) : v;
+}
+__device__ __forceinline__ float nan_of(float) { return __uint_as_float(0x7fc00000u); }
+__device__ __forceinline__ double nan_of(double) {
+  return __longlong_as_double(0x7ff8000000000000ll);
+}
+
+// float64 -> T with one round-to-nearest cast (T::from_f64 in the reference).
+template <typename T>
+__device__ __forceinline__ T from_f64(double v);
+template <>
+__device__ __forceinline__ float from_f64<float>(double v) {
+  return __double2float_rn(v);
+}
+template <>
+__device__ __forceinline__ double from_f64<double>(double v) {
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Boundary mapping, src/boundary.rs:29-71. Returns false for a position
+// outside a constant boundary. `length` is nonzero.
+
+__host__ __device__ __forceinline__ long long rem_euclid(long long a, long long b) {
+  long long r = a % b;
+  return r < 0 ? r + b : r;
+}
+
+__host__ __device__ __forceinline__ bool map_index(long long index, long long length, int mode,
+                                                   long long* out) {
+  if (index >= 0 && index < length) {
+    *out = index;
+    return true;
+  }
+  switch (mode) {
+    case kConstant:
+      return false;
+    case kNearest:
+      *out = index < 0 ? 0 : length - 1;
+      return true;
+    case kWrap:
+      *out = rem_euclid(index, length);
+      return true;
+    case kReflect: {
+      if (length == 1) {
+        *out = 0;
+        return true;
+      }
+      long long period = 2 * length;
+      long long r = rem_euclid(index, period);
+      *out = r < length ? r : period - 1 - r;
+      return true;
+    }
+    default: {  // kMirror
+      if (length == 1) {
+        *out = 0;
+        return true;
+      }
+      long long period = 2 * (length - 1);
+      long long r = rem_euclid(index, period);
+      *out = r < length ? r : period - r;
+      return true;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Midpoint of the two middle retained values (lower <= upper in total
+// order), the reducers 0.4.0 contract pinned by docs/semantics.md:74-88,
+// tests/_reference.py:36-47 and src/reduction.rs:214-249.
+
+__device__ __forceinline__ double midpoint(double lower, double upper) {
+  if (signbit(lower) == signbit(upper) && lower == upper) return lower;
+  if (lower == 0.0 && upper == 0.0) return 0.0;
+  if (isinf(lower) || isinf(upper)) {
+    if (isinf(lower) && isinf(upper)) return nan_of(0.0);
+    return isinf(lower) ? lower : upper;
+  }
+  if (signbit(lower) == signbit(upper))
+    return __dadd_rn(lower, __ddiv_rn(__dsub_rn(upper, lower), 2.0));
+  return __ddiv_rn(__dadd_rn(lower, upper), 2.0);
+}
+
+// Neumaier float64 sum, src/mean.rs:7-26.
+struct Sum64 {
+  double value = 0.0, correction = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    double next = __dadd_rn(value, x);
+    if (fabs(value) >= fabs(x))
+      correction = __dadd_rn(correction, __dadd_rn(__dsub_rn(value, next), x));
+    else
+      correction = __dadd_rn(correction, __dadd_rn(__dsub_rn(x, next), value));
+    value = next;
+  }
+  __device__ __forceinline__ double total() const { return __dadd_rn(value, correction); }
+};
+
+__device__ __forceinline__ double clamp64(double x, double lo, double hi) {
+  if (x < lo) return lo;
+  if (x > hi) return hi;
+  return x;
+}
+
+// split / scale_binary / scaled_dot, src/convolution.rs:203-270.
+struct Split {
+  double mantissa;
+  int exponent;
+};
+
+__device__ __forceinline__ Split split64(double value) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(value);
+  int exponent = (int)((b >> 52) & 0x7ff);
+  unsigned long long fraction = b & ((1ull << 52) - 1);
+  if (exponent == 0) {
+    int leading = 63 - __clzll((long long)fraction);
+    double mantissa = __ddiv_rn((double)fraction, (double)(1ull << leading));
+    return {copysign(mantissa, value), leading - 1074};
+  }
+  return {__longlong_as_double((long long)((b & ((1ull << 63) | ((1ull << 52) - 1))) |
+                                           (1023ull << 52))),
+          exponent - 1023};
+}
+
+__device__ __forceinline__ double scale_binary(double value, int exponent) {
+  if (value == 0.0) return value;
+  Split s = split64(value);
+  int target = s.exponent + exponent;
+  if (target > 1023) return copysign(__longlong_as_double(0x7ff0000000000000ll), value);
+  if (target < -1075) return copysign(0.0, value);
+  if (target >= -1022)
+    return __dmul_rn(s.mantissa, __longlong_as_double((long long)(target + 1023) << 52));
+  double remaining = __longlong_as_double((long long)(target + 1022 + 1023) << 52);
+  return __dmul_rn(__dmul_rn(s.mantissa, 2.2250738585072014e-308), remaining);
+}
+
+// finite_weighted(&[(v0, w0), (v1, w1)], false), src/convolution.rs:287-361.
+static __device__ __noinline__ double finite_weighted2(double v0, double w0, double v1, double w1) {
+  const double values[2] = {v0, v1};
+  const double weights[2] = {w0, w1};
+  Sum64 sum;
+  bool fallback = false;
+  for (int i = 0; i < 2; ++i) {
+    double product = __dmul_rn(values[i], weights[i]);
+    if (!isfinite(product) || (values[i] != 0.0 && fabs(product) < 2.2250738585072014e-308)) {
+      fallback = true;
+      break;
+    }
+    sum.add(product);
+  }
+  if (!fallback) {
+    double total = sum.total();
+    if (isfinite(total)) return total;
+  }
+  // scaled_dot over two pairs: count bits of (2 - 1) = 1.
+  bool any = false;
+  int maximum = 0;
+  for (int i = 0; i < 2; ++i) {
+    if (values[i] == 0.0) continue;
+    int e = split64(values[i]).exponent + split64(weights[i]).exponent;
+    maximum = any ? max(maximum, e) : e;
+    any = true;
+  }
+  if (!any) return scale_binary(0.0, 0);
+  int exponent = maximum + 1 + 2;
+  Sum64 scaled;
+  for (int i = 0; i < 2; ++i) {
+    if (values[i] == 0.0) continue;
+    Split a = split64(values[i]);
+    Split b = split64(weights[i]);
+    scaled.add(scale_binary(__dmul_rn(a.mantissa, b.mantissa), a.exponent + b.exponent - exponent));
+  }
+  return scale_binary(scaled.total(), exponent);
+}
+
+// interpolate, src/robust.rs:305-341.
+__device__ __forceinline__ double interpolate(double lower, double upper, double fraction) {
+  if (fraction == 0.0 || __double_as_longlong(lower) == __double_as_longlong(upper)) return lower;
+  if (fraction == 1.0) return upper;
+  if (isinf(lower) || isinf(upper)) {
+    if (lower < 0 && isinf(lower) && upper > 0 && isinf(upper)) return nan_of(0.0);
+    return isinf(lower) ? lower : upper;
+  }
+  if (signbit(lower) != signbit(upper)) {
+    if (!isfinite(__dsub_rn(upper, lower))) {
+      double half_lower = __ddiv_rn(lower, 2.0);
+      double half_upper = __ddiv_rn(upper, 2.0);
+      double r = __dmul_rn(
+          __dadd_rn(half_lower, __dmul_rn(__dsub_rn(half_upper, half_lower), fraction)), 2.0);
+      return clamp64(r, lower, upper);
+    }
+    return finite_weighted2(lower, __dsub_rn(1.0, fraction), upper, fraction);
+  }
+  double difference = __dsub_rn(upper, lower);
+  double result = fraction <= 0.5
+                      ? __dadd_rn(lower, __dmul_rn(difference, fraction))
+                      : __dsub_rn(upper, __dmul_rn(difference, __dsub_rn(1.0, fraction)));
+  return clamp64(result, lower, upper);
+}
+
+// Percentile rank split, src/robust.rs:343-352: returns the lower and upper
+// zero-based ranks and the fraction for `n` retained samples (q < 100).
+struct PercentileRank {
+  long long lower, upper;
+  double fraction;
+};
+
+__device__ __forceinline__ PercentileRank percentile_rank(double q, long long n) {
+  double rank = __dmul_rn(__ddiv_rn(q, 100.0), (double)(n - 1));
+  long long lower = (long long)floor(rank);
+  long long upper = lower + 1 < n - 1 ? lower + 1 : n - 1;
+  return {lower, upper, __dsub_rn(rank, (double)lower)};
+}
+
+}  // namespace ndf

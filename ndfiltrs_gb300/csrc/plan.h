@@ -1,0 +1,128 @@
+// Host-side plan and kernel argument structures shared by the translation
+// units of the GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ndf {
+
+constexpr int kMaxNetwork32 = 128;  // largest register network for float32 keys
+constexpr int kMaxNetwork64 = 64;   // largest register network for float64 keys
+constexpr int kMaxGenericRank = 32; // largest array rank of the generic kernels
+
+// Canonical 3-D view of a rank 1-3 array: axes (z, y, x), x contiguous.
+struct Geom3 {
+  long long D, H, W;  // array extent per axis
+  int kd, kh, kw;     // window box per axis
+  int az, ay, ax;     // anchors: size / 2 + origin
+  int mz, my, mx;     // boundary modes
+};
+
+// Reduction parameters every kernel reads.
+struct Reduce {
+  int kind;            // NDF_KIND_*
+  int omit;            // InvalidPolicy::Omit
+  int drop_inf;        // Omit { ignore_inf: true }
+  int count;           // taps per window (V)
+  long long min_count; // Omit { min_count }
+  long long param;     // rank or ddof
+  double q;            // percentile
+  double cval;         // constant boundary value, already cast to the dtype
+  int moments;         // NDF_MOMENTS_* for mean/var/std
+};
+
+// Halo tile of one thread block: TW x TH outputs of one z slice. The block
+// stages kd x SH x SW samples (SH = TH + kh - 1, SW = TW + kw - 1).
+struct Tile {
+  int TW, TH, SH, SW;
+  long long tiles_x, tiles_y, tiles;  // tiles per row, per slice, total
+};
+
+struct TileArgs {
+  Geom3 g;
+  Tile t;
+  Reduce r;
+};
+
+// Generic N-D gather (any rank): one thread per output.
+struct GenericArgs {
+  int rank;
+  long long n_out;
+  long long shape[kMaxGenericRank];
+  long long stride[kMaxGenericRank];
+  int mode[kMaxGenericRank];
+  long long low[kMaxGenericRank], high[kMaxGenericRank];
+  Reduce r;
+};
+
+enum class Algo {
+  kEmpty,
+  kTileNetwork,
+  kTileRadix,
+  kGenericSelect,
+  kHistogram,
+  kMomentsTile,
+  kMomentsGeneric,
+};
+
+struct Plan {
+  // Validated description.
+  int dtype = 0;
+  int ndim = 0;
+  std::vector<long long> shape, size, origin;
+  std::vector<int> modes;
+  std::vector<uint8_t> footprint;  // empty for a rectangular window
+  Reduce r{};
+  long long n_out = 0;
+
+  // Window taps in C order over the footprint: per-axis offsets
+  // (count x ndim, k - anchor) and, for the tile kernels, (kz, ky, kx) box
+  // positions.
+  std::vector<long long> taps;
+  std::vector<int> box_taps;  // count x 3 (canonical z, y, x), tile kernels
+
+  Algo algo = Algo::kEmpty;
+  int network = 0;  // register-network width (power of two) for kTileNetwork
+  TileArgs tile{};
+  size_t smem_bytes = 0;
+  GenericArgs generic{};
+
+  // Device resources.
+  int device = 0;
+  int sm_count = 0;
+  int32_t* d_tile_taps = nullptr;   // smem offsets of the taps (tile kernels)
+  long long* d_gen_taps = nullptr;  // count x rank offsets + count flat offsets
+  void* d_in = nullptr;             // buffers for host-buffer runs
+  void* d_out = nullptr;
+  size_t buffer_bytes = 0;
+  void* d_scratch = nullptr;        // kernel scratch (histogram ranks, ...)
+  size_t scratch_bytes = 0;
+  unsigned int* d_status = nullptr; // device error flags
+
+  // Histogram kernel geometry (rectangular 1-D/2-D windows).
+  int hist_block_w = 0, hist_block_h = 0;
+  long long hist_blocks_x = 0, hist_blocks_y = 0;
+};
+
+const char* algo_name(Algo a);
+
+// Launchers (one per translation unit). Return a cudaError_t.
+cudaError_t launch_tile_select(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_generic_select(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_tile_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_generic_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStream_t s);
+
+// Shared-memory bytes a tile kernel needs for `t` (0 when it does not fit).
+size_t tile_select_smem(const Plan& p, const Tile& t);
+size_t tile_moments_smem(const Plan& p, const Tile& t);
+size_t histogram_smem(const Plan& p);
+bool histogram_supported(const Plan& p);
+void histogram_configure(Plan& p);
+int network_width_for(int dtype, int count);
+
+}  // namespace ndf

@@ -1,0 +1,436 @@
+// Exact order statistics on the GPU: median (direct / sortnet), rank, min,
+// max and percentile.
+//
+// * tile_network: the window's keys sit in registers and a Batcher
+//   odd-even merge network sorts them (replaces Network::new/apply,
+//   src/median_network.rs:116-209, and the per-output selection of
+//   Reduction::finish, src/reduction.rs:78-130). The network width is a
+//   compile-time power of two; padding wires hold the sentinel key, so the
+//   compiler folds their comparators away, and comparators whose outputs no
+//   rank of the reduction can reach are removed as dead code (the backward
+//   liveness pruning of the reference's Network::new).
+// * tile_radix: windows too wide for a register network run a bit-serial
+//   radix select over the staged keys.
+// * generic: arrays of rank > 3 (or supports that do not fit in shared
+//   memory) gather every tap through the boundary maps from global memory.
+//
+// Dropped samples (NaN, and infinities under ignore_inf) take the sentinel
+// key, the largest key, so a sorted window holds its `nv` retained samples
+// first. Propagate windows are NaN when nv != V.
+#include "common.cuh"
+#include "plan.h"
+#include "staging.cuh"
+
+#include <utility>
+
+namespace ndf {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int N>
+struct TapTable {
+  int32_t off[N];
+};
+
+template <typename K>
+__device__ __forceinline__ void cmpx(K& a, K& b) {
+  K lo = a < b ? a : b;
+  K hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
+// Batcher odd-even merge sort over N (a power of two) wires, generated at
+// compile time as a comparator table and applied by a fold expression, so
+// every wire index is a constant expression and the keys stay in registers.
+template <int N>
+struct Batcher {
+  static constexpr bool same_block(int lo, int hi, int p) { return lo / (2 * p) == hi / (2 * p); }
+  static constexpr int count() {
+    int c = 0;
+    for (int p = 1; p < N; p <<= 1)
+      for (int k = p; k >= 1; k >>= 1)
+        for (int j = k % p; j + k < N; j += 2 * k)
+          for (int i = 0; i < k && i + j + k < N; ++i)
+            if (same_block(i + j, i + j + k, p)) ++c;
+    return c;
+  }
+  static constexpr int kCount = count();
+  struct Table {
+    short lo[kCount];
+    short hi[kCount];
+  };
+  static constexpr Table table() {
+    Table t{};
+    int c = 0;
+    for (int p = 1; p < N; p <<= 1)
+      for (int k = p; k >= 1; k >>= 1)
+        for (int j = k % p; j + k < N; j += 2 * k)
+          for (int i = 0; i < k && i + j + k < N; ++i)
+            if (same_block(i + j, i + j + k, p)) {
+              t.lo[c] = (short)(i + j);
+              t.hi[c] = (short)(i + j + k);
+              ++c;
+            }
+    return t;
+  }
+  static constexpr Table kTable = table();
+};
+
+template <int N, int I, typename K>
+__device__ __forceinline__ void cmpx_at(K (&a)[N]) {
+  constexpr int lo = Batcher<N>::kTable.lo[I];
+  constexpr int hi = Batcher<N>::kTable.hi[I];
+  cmpx(a[lo], a[hi]);
+}
+
+template <int N, typename K, int... Is>
+__device__ __forceinline__ void apply_network(K (&a)[N], std::integer_sequence<int, Is...>) {
+  (cmpx_at<N, Is>(a), ...);
+}
+
+template <int N, typename K>
+__device__ __forceinline__ void batcher_sort(K (&a)[N]) {
+  apply_network<N>(a, std::make_integer_sequence<int, Batcher<N>::kCount>{});
+}
+
+// Register pick a[idx] for a runtime idx < BOUND.
+template <int BOUND, int N, typename K>
+__device__ __forceinline__ K pick(const K (&a)[N], int idx) {
+  K v = a[0];
+#pragma unroll
+  for (int i = 1; i < BOUND; ++i) v = (i == idx) ? a[i] : v;
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T median_of_two(T lower, T upper) {
+  return from_f64<T>(midpoint((double)lower, (double)upper));
+}
+
+// Epilogue of the register network: the statistic from sorted keys.
+// MODE 0: any selection kind, runtime policy. MODE 1: median kinds only.
+template <typename T, int N, int VFIX, int MODE, typename K>
+__device__ __forceinline__ T network_finish(const K (&k)[N], int nv, const Reduce& r) {
+  using KO = KeyOf<T>;
+  const int V = VFIX > 0 ? VFIX : r.count;
+  const bool missing = r.omit ? (nv < r.min_count) : (nv != V);
+  if (missing || nv == 0) return nan_of(T());
+  if (MODE == 1) {
+    if (VFIX > 0 && !r.omit) {
+      // Propagate with a fixed tap count: compile-time ranks.
+      if (VFIX & 1) return KO::value(k[VFIX / 2]);
+      return median_of_two(KO::value(k[VFIX / 2 - 1]), KO::value(k[VFIX / 2]));
+    }
+    constexpr int B = (VFIX > 0 ? VFIX : N) / 2 + 1;
+    if (nv & 1) return KO::value(pick<B>(k, nv / 2));
+    return median_of_two(KO::value(pick<B>(k, nv / 2 - 1)), KO::value(pick<B>(k, nv / 2)));
+  }
+  switch (r.kind) {
+    case kMin:
+      return KO::value(k[0]);
+    case kMax:
+      return KO::value(pick<N>(k, nv - 1));
+    case kRank:
+    case kRankHistogram:
+      if (r.param >= nv) return nan_of(T());
+      return KO::value(pick<N>(k, (int)r.param));
+    case kPercentile: {
+      if (r.q == 100.0) return KO::value(pick<N>(k, nv - 1));
+      PercentileRank pr = percentile_rank(r.q, nv);
+      double lo = (double)KO::value(pick<N>(k, (int)pr.lower));
+      double hi = (double)KO::value(pick<N>(k, (int)pr.upper));
+      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+    }
+    default:
+      if (nv & 1) return KO::value(pick<N>(k, nv / 2));
+      return median_of_two(KO::value(pick<N>(k, nv / 2 - 1)), KO::value(pick<N>(k, nv / 2)));
+  }
+}
+
+__device__ __forceinline__ void tile_coords(const TileArgs& a, long long& z, long long& y0,
+                                            long long& x0) {
+  long long tile = blockIdx.x;
+  long long tx = tile % a.t.tiles_x;
+  long long rest = tile / a.t.tiles_x;
+  long long ty = rest % a.t.tiles_y;
+  z = rest / a.t.tiles_y;
+  y0 = ty * a.t.TH;
+  x0 = tx * a.t.TW;
+}
+
+template <typename T, int N, int VFIX, int MODE>
+__global__ void __launch_bounds__(kThreads, 1)
+    tile_network_kernel(const T* __restrict__ in, T* __restrict__ out,
+                        const __grid_constant__ TileArgs a, const __grid_constant__ TapTable<N> taps) {
+  using K = typename KeyOf<T>::K;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
+  long long z, y0, x0;
+  tile_coords(a, z, y0, x0);
+  build_maps(maps, g, t, z, y0, x0);
+  __syncthreads();
+  const bool drop_inf = a.r.drop_inf;
+  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  __syncthreads();
+
+  const int tx = threadIdx.x % t.TW;
+  const int ty = threadIdx.x / t.TW;
+  const long long y = y0 + ty, x = x0 + tx;
+  if (ty >= t.TH || y >= g.H || x >= g.W) return;
+  const K* base = s + ty * t.SW + tx;
+  const int V = VFIX > 0 ? VFIX : a.r.count;
+  K k[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) k[i] = i < V ? base[taps.off[i]] : KeyOf<T>::kSentinel;
+  int nv = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) nv += (i < V && k[i] != KeyOf<T>::kSentinel) ? 1 : 0;
+  batcher_sort<N>(k);
+  T result = network_finish<T, N, VFIX, MODE>(k, nv, a.r);
+  out[(z * g.H + y) * g.W + x] = canonical(result);
+}
+
+// ---------------------------------------------------------------------------
+// Bit-serial radix select: the k-th smallest retained key (k < nv). Bits
+// shared by every retained key (from their AND and OR) are skipped.
+template <typename K, typename Fetch>
+__device__ __forceinline__ K radix_select(Fetch&& fetch, int V, long long k, K and_v, K or_v) {
+  K diff = and_v ^ or_v;
+  if (diff == 0) return and_v;
+  const int bits = sizeof(K) * 8;
+  int top = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)diff) : __clz((int)diff));
+  K mask = top + 1 >= bits ? K(0) : ~((K(1) << (top + 1)) - 1);
+  K prefix = and_v & mask;
+  for (int b = top; b >= 0; --b) {
+    K bit = K(1) << b;
+    K m = mask | bit;
+    long long c = 0;
+    for (int i = 0; i < V; ++i) c += ((fetch(i) & m) == prefix) ? 1 : 0;
+    if (k >= c) {
+      k -= c;
+      prefix |= bit;
+    }
+    mask = m;
+  }
+  return prefix;
+}
+
+struct KeyStats {
+  int nv;
+};
+
+template <typename T, typename K, typename Fetch>
+__device__ __forceinline__ T radix_finish(Fetch&& fetch, const Reduce& r) {
+  using KO = KeyOf<T>;
+  const K sent = KO::kSentinel;
+  const int V = r.count;
+  int nv = 0;
+  K and_v = sent, or_v = 0, kmin = sent, kmax = 0;
+  for (int i = 0; i < V; ++i) {
+    K key = fetch(i);
+    if (key != sent) {
+      nv += 1;
+      and_v &= key;
+      or_v |= key;
+      kmin = key < kmin ? key : kmin;
+      kmax = key > kmax ? key : kmax;
+    }
+  }
+  const bool missing = r.omit ? (nv < r.min_count) : (nv != V);
+  if (missing || nv == 0) return nan_of(T());
+  auto sel = [&](long long kk) { return radix_select<K>(fetch, V, kk, and_v, or_v); };
+  switch (r.kind) {
+    case kMin:
+      return KO::value(kmin);
+    case kMax:
+      return KO::value(kmax);
+    case kRank:
+    case kRankHistogram:
+      if (r.param >= nv) return nan_of(T());
+      return KO::value(sel(r.param));
+    case kPercentile: {
+      if (r.q == 100.0) return KO::value(kmax);
+      PercentileRank pr = percentile_rank(r.q, nv);
+      double lo = (double)KO::value(sel(pr.lower));
+      double hi = pr.upper == pr.lower ? lo : (double)KO::value(sel(pr.upper));
+      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+    }
+    default:
+      if (nv & 1) return KO::value(sel(nv / 2));
+      return median_of_two(KO::value(sel(nv / 2 - 1)), KO::value(sel(nv / 2)));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    tile_radix_kernel(const T* __restrict__ in, T* __restrict__ out,
+                      const __grid_constant__ TileArgs a, const int32_t* __restrict__ taps) {
+  using K = typename KeyOf<T>::K;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
+  long long z, y0, x0;
+  tile_coords(a, z, y0, x0);
+  build_maps(maps, g, t, z, y0, x0);
+  __syncthreads();
+  const bool drop_inf = a.r.drop_inf;
+  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  __syncthreads();
+  const int tx = threadIdx.x % t.TW;
+  const int ty = threadIdx.x / t.TW;
+  const long long y = y0 + ty, x = x0 + tx;
+  if (ty >= t.TH || y >= g.H || x >= g.W) return;
+  const K* base = s + ty * t.SW + tx;
+  auto fetch = [&](int i) -> K { return base[__ldg(taps + i)]; };
+  T result = radix_finish<T, K>(fetch, a.r);
+  out[(z * g.H + y) * g.W + x] = canonical(result);
+}
+
+// ---------------------------------------------------------------------------
+// Generic N-D gather: one thread per output, taps mapped per axis
+// (Window::prepare / visit_mapped, src/window.rs:254-294).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    generic_select_kernel(const T* __restrict__ in, T* __restrict__ out,
+                          const __grid_constant__ GenericArgs a,
+                          const long long* __restrict__ taps) {
+  using K = typename KeyOf<T>::K;
+  const int rank = a.rank;
+  const long long* flat = taps + (long long)a.r.count * rank;
+  const bool drop_inf = a.r.drop_inf;
+  const T cval = (T)a.r.cval;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < a.n_out;
+       o += (long long)gridDim.x * blockDim.x) {
+    long long coord[kMaxGenericRank];
+    long long rem = o;
+    bool interior = true;
+    for (int d = 0; d < rank; ++d) {
+      coord[d] = rem / a.stride[d];
+      rem -= coord[d] * a.stride[d];
+      interior = interior && coord[d] + a.low[d] >= 0 && coord[d] + a.high[d] < a.shape[d];
+    }
+    auto fetch = [&](int i) -> K {
+      if (interior) return sample_key<T>(__ldg(in + o + flat[i]), drop_inf);
+      const long long* tap = taps + (long long)i * rank;
+      long long src = 0;
+      for (int d = 0; d < rank; ++d) {
+        long long m;
+        if (!map_index(coord[d] + tap[d], a.shape[d], a.mode[d], &m))
+          return sample_key<T>(cval, drop_inf);
+        src += m * a.stride[d];
+      }
+      return sample_key<T>(__ldg(in + src), drop_inf);
+    };
+    out[o] = canonical(radix_finish<T, K>(fetch, a.r));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers.
+
+template <typename T, int N, int VFIX, int MODE>
+cudaError_t launch_network(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  TapTable<N> taps{};
+  const TileArgs& a = p.tile;
+  for (int i = 0; i < N; ++i) {
+    if (i < p.r.count) {
+      const int* bt = &p.box_taps[(size_t)i * 3];
+      taps.off[i] = (bt[0] * a.t.SH + bt[1]) * a.t.SW + bt[2];
+    } else {
+      taps.off[i] = 0;
+    }
+  }
+  auto kernel = tile_network_kernel<T, N, VFIX, MODE>;
+  cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+  if (e != cudaSuccess) return e;
+  kernel<<<(unsigned)a.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, a, taps);
+  return cudaGetLastError();
+}
+
+template <typename T, int N>
+cudaError_t dispatch_network_mode(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork ||
+                      p.r.kind == kMedianHistogram;
+  if (!median) return launch_network<T, N, 0, 0>(p, in, out, s);
+  if constexpr (sizeof(T) == 4) {
+    // Fixed tap counts of the hot configurations: 3x3, 5x5 and 7x7 boxes.
+    if (N == 16 && p.r.count == 9) return launch_network<T, 16, 9, 1>(p, in, out, s);
+    if (N == 32 && p.r.count == 25) return launch_network<T, 32, 25, 1>(p, in, out, s);
+    if (N == 64 && p.r.count == 49) return launch_network<T, 64, 49, 1>(p, in, out, s);
+  }
+  return launch_network<T, N, 0, 1>(p, in, out, s);
+}
+
+template <typename T>
+cudaError_t launch_tile_select_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  if (p.algo == Algo::kTileNetwork) {
+    switch (p.network) {
+      case 8:
+        return dispatch_network_mode<T, 8>(p, in, out, s);
+      case 16:
+        return dispatch_network_mode<T, 16>(p, in, out, s);
+      case 32:
+        return dispatch_network_mode<T, 32>(p, in, out, s);
+      case 64:
+        return dispatch_network_mode<T, 64>(p, in, out, s);
+      case 128:
+        if constexpr (sizeof(T) == 4) return dispatch_network_mode<T, 128>(p, in, out, s);
+        return cudaErrorInvalidValue;
+      default:
+        return cudaErrorInvalidValue;
+    }
+  }
+  auto kernel = tile_radix_kernel<T>;
+  cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+  if (e != cudaSuccess) return e;
+  kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile, p.d_tile_taps);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int network_width_for(int dtype, int count) {
+  int limit = dtype == 0 ? kMaxNetwork32 : kMaxNetwork64;
+  if (count > limit) return 0;
+  int n = 8;
+  while (n < count) n <<= 1;
+  return n;
+}
+
+size_t tile_select_smem(const Plan& p, const Tile& t) {
+  size_t key = p.dtype == 0 ? 4 : 8;
+  return (size_t)(t.SW + t.SH + p.tile.g.kd) * 8 + (size_t)p.tile.g.kd * t.SH * t.SW * key;
+}
+
+cudaError_t launch_tile_select(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  if (p.dtype == 0)
+    return launch_tile_select_t<float>(p, (const float*)in, (float*)out, s);
+  return launch_tile_select_t<double>(p, (const double*)in, (double*)out, s);
+}
+
+cudaError_t launch_generic_select(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  long long blocks = (p.n_out + kThreads - 1) / kThreads;
+  long long cap = (long long)p.sm_count * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  if (p.dtype == 0)
+    generic_select_kernel<float><<<(unsigned)blocks, kThreads, 0, s>>>(
+        (const float*)in, (float*)out, p.generic, p.d_gen_taps);
+  else
+    generic_select_kernel<double><<<(unsigned)blocks, kThreads, 0, s>>>(
+        (const double*)in, (double*)out, p.generic, p.d_gen_taps);
+  return cudaGetLastError();
+}
+
+}  // namespace ndf

@@ -1,0 +1,1367 @@
+// CPU restatement of ndfiltrs' windowed-statistics hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the oracle that the CUDA library is
+// checked against, and the timed CPU baseline of bench.py. Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg load it. The product
+// (ndfiltrs_gb300 and its C-ABI library) never links, loads or calls it.
+//
+// Every function restates the reference algorithm (ysBach/ndfiltrs v0.2.0,
+// Rust crate) and cites the file:line it follows. The order statistics are
+// bit-exact restatements; mean/var/std follow the reference's float64
+// compensated arithmetic operation for operation (no FMA contraction: build
+// with -ffp-contract=off).
+//
+// Parity pin: the reference's own known-answer tests (boundary literals, tap
+// order, reducers midpoint contract, mean/dispersion/percentile literals,
+// zero-one principle) are restated in tests/test_oracle_pins.py, and golden
+// vectors produced by the reference's literal Python oracles
+// (tests/_reference.py, tests/_statistics_reference.py,
+// tests/_mean_reference.py) plus SciPy/NumPy are committed under
+// tests/golden/ together with the script that made them.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <thread>
+#include <utility>
+#include <vector>
+
+namespace {
+
+// Error codes mirror src/error.rs:6-18 (same numbering as the C-ABI).
+constexpr int kOk = 0;
+constexpr int kEmptyAxis = 1;
+constexpr int kInvalid = 2;
+constexpr int kLength = 3;
+constexpr int kMemory = 4;
+constexpr int kOverflow = 5;
+
+thread_local std::string g_message;
+
+int fail(int code, const char* message) {
+  g_message = message;
+  return code;
+}
+
+enum Mode { kReflect = 0, kConstant = 1, kNearest = 2, kMirror = 3, kWrap = 4 };
+
+enum Kind {
+  kMedian = 0,
+  kMedianNetwork = 1,
+  kMedianHistogram = 2,
+  kMean = 3,
+  kMeanRolling = 4,
+  kMin = 5,
+  kMax = 6,
+  kVar = 7,
+  kStd = 8,
+  kRank = 9,
+  kRankHistogram = 10,
+  kPercentile = 11,
+};
+
+// InvalidPolicy, src/reduction.rs:6-18.
+struct Policy {
+  bool omit = false;
+  bool ignore_inf = false;
+  uint64_t min_count = 1;
+};
+
+constexpr double kNaN64 = std::numeric_limits<double>::quiet_NaN();
+
+inline uint64_t bits64(double v) {
+  uint64_t b;
+  std::memcpy(&b, &v, 8);
+  return b;
+}
+inline double from_bits64(uint64_t b) {
+  double v;
+  std::memcpy(&v, &b, 8);
+  return v;
+}
+
+// Total-order key of a float64 (the f64 arm of NetworkFloat::sort_key,
+// src/median_network.rs:21-31, expressed as an unsigned key). Float32 values
+// are handled as their exact float64 conversions, which keeps their order.
+inline uint64_t total_key(double v) {
+  uint64_t b = bits64(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+inline bool retained(double v, const Policy& p) {
+  if (std::isnan(v)) return false;
+  if (p.omit && p.ignore_inf && !std::isfinite(v)) return false;
+  return true;
+}
+
+int64_t rem_euclid(int64_t a, int64_t b) {
+  int64_t r = a % b;
+  return r < 0 ? r + b : r;
+}
+
+// map_index, src/boundary.rs:29-71. Returns 1 with *out set, 0 for a
+// constant-mode position outside the array, -kEmptyAxis on an empty axis.
+int map_index(int64_t index, int64_t length, int mode, int64_t* out) {
+  if (length == 0) return -kEmptyAxis;
+  if (index >= 0 && index < length) {
+    *out = index;
+    return 1;
+  }
+  switch (mode) {
+    case kConstant:
+      return 0;
+    case kNearest:
+      *out = index < 0 ? 0 : length - 1;
+      return 1;
+    case kWrap:
+      *out = rem_euclid(index, length);
+      return 1;
+    case kReflect: {
+      if (length == 1) {
+        *out = 0;
+        return 1;
+      }
+      int64_t period = 2 * length;
+      int64_t reduced = rem_euclid(index, period);
+      *out = reduced < length ? reduced : period - 1 - reduced;
+      return 1;
+    }
+    case kMirror: {
+      if (length == 1) {
+        *out = 0;
+        return 1;
+      }
+      int64_t period = 2 * (length - 1);
+      int64_t reduced = rem_euclid(index, period);
+      *out = reduced < length ? reduced : period - reduced;
+      return 1;
+    }
+    default:
+      return -kInvalid;
+  }
+}
+
+// Window, src/window.rs:11-137: taps in C order over the footprint, offset
+// k - (size/2 + origin) per axis, flat offsets, per-axis low/high.
+struct Window {
+  int rank = 0;
+  std::vector<int64_t> shape, strides, low, high;
+  std::vector<int> modes;
+  std::vector<int64_t> taps;  // count * rank, tap-major
+  std::vector<int64_t> flat;  // count
+  size_t count = 0;
+  size_t out_len = 0;
+};
+
+int window_new(int rank, const uint64_t* shape, const uint64_t* size, const uint8_t* footprint,
+               const int64_t* origin, const int32_t* modes, Window* w, bool build_taps = true) {
+  if (rank <= 0) return fail(kInvalid, "filtering requires at least one dimension");
+  for (int a = 0; a < rank; ++a)
+    if (size[a] == 0) return fail(kInvalid, "window sizes must be positive");
+  for (int a = 0; a < rank; ++a)
+    if (modes[a] < 0 || modes[a] > 4) return fail(kInvalid, "unsupported boundary mode");
+  uint64_t volume = 1;
+  for (int a = 0; a < rank; ++a) {
+    if (size[a] > 0 && volume > UINT64_MAX / size[a])
+      return fail(kOverflow, "shape or index arithmetic overflowed");
+    volume *= size[a];
+  }
+  std::vector<int64_t> anchors(rank);
+  for (int a = 0; a < rank; ++a) {
+    int64_t length = (int64_t)size[a];
+    if (origin[a] < -(length / 2) || origin[a] > (length - 1) / 2)
+      return fail(kInvalid, "origin must satisfy -(size // 2) <= origin <= (size - 1) // 2");
+    anchors[a] = length / 2 + origin[a];
+  }
+  w->rank = rank;
+  w->shape.assign(shape, shape + rank);
+  w->modes.assign(modes, modes + rank);
+  w->strides.assign(rank, 1);
+  uint64_t out_len = 1;
+  for (int a = 0; a < rank; ++a) {
+    if (shape[a] > 0 && out_len > UINT64_MAX / shape[a])
+      return fail(kOverflow, "shape or index arithmetic overflowed");
+    out_len *= shape[a];
+  }
+  w->out_len = out_len;
+  for (int a = rank - 2; a >= 0; --a) w->strides[a] = w->strides[a + 1] * (int64_t)shape[a + 1];
+  size_t count = 0;
+  if (footprint) {
+    for (uint64_t e = 0; e < volume; ++e) count += footprint[e] != 0;
+  } else {
+    count = volume;
+  }
+  if (count == 0) return fail(kInvalid, "footprint must select at least one element");
+  w->count = count;
+  if (!build_taps) return kOk;
+  w->taps.clear();
+  w->flat.clear();
+  w->taps.reserve(count * rank);
+  w->flat.reserve(count);
+  w->low.assign(rank, INT64_MAX);
+  w->high.assign(rank, INT64_MIN);
+  std::vector<uint64_t> index(rank, 0);
+  for (uint64_t e = 0; e < volume; ++e) {
+    if (!footprint || footprint[e]) {
+      int64_t flat = 0;
+      for (int a = 0; a < rank; ++a) {
+        int64_t offset = (int64_t)index[a] - anchors[a];
+        flat += offset * w->strides[a];
+        w->low[a] = std::min(w->low[a], offset);
+        w->high[a] = std::max(w->high[a], offset);
+        w->taps.push_back(offset);
+      }
+      w->flat.push_back(flat);
+    }
+    for (int a = rank - 1; a >= 0; --a) {
+      if (++index[a] < size[a]) break;
+      index[a] = 0;
+    }
+  }
+  return kOk;
+}
+
+// Window::prepare, src/window.rs:254-269.
+inline bool prepare(const Window& w, size_t center, int64_t* index) {
+  size_t remainder = center;
+  bool interior = true;
+  for (int a = 0; a < w.rank; ++a) {
+    index[a] = (int64_t)(remainder / (size_t)w.strides[a]);
+    remainder %= (size_t)w.strides[a];
+    interior = interior && index[a] + w.low[a] >= 0 && index[a] + w.high[a] < w.shape[a];
+  }
+  return interior;
+}
+
+// Window::visit / gather / visit_mapped, src/window.rs:211-294. Samples are
+// delivered in tap order as float64 (exact for float32 input).
+template <class T, class F>
+inline void visit(const Window& w, const T* input, size_t center, double cval, int64_t* index,
+                  F&& consume) {
+  if (prepare(w, center, index)) {
+    const T* base = input + center;
+    for (size_t t = 0; t < w.count; ++t) consume((double)base[w.flat[t]]);
+    return;
+  }
+  for (size_t t = 0; t < w.count; ++t) {
+    const int64_t* tap = &w.taps[t * w.rank];
+    int64_t source = 0;
+    bool outside = false;
+    for (int a = 0; a < w.rank; ++a) {
+      int64_t mapped = 0;
+      int r = map_index(index[a] + tap[a], w.shape[a], w.modes[a], &mapped);
+      if (r == 0) {
+        outside = true;
+        break;
+      }
+      source += mapped * w.strides[a];
+    }
+    consume(outside ? cval : (double)input[source]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Arithmetic contracts.
+
+// Midpoint contract of reducers 0.4.0 median_valid_in_place for two middle
+// values (lower <= upper in total order), pinned by docs/semantics.md:74-88,
+// tests/_reference.py:36-47 and src/reduction.rs:214-249.
+double midpoint(double lower, double upper) {
+  if (std::signbit(lower) == std::signbit(upper) && lower == upper) return lower;
+  if (lower == 0.0 && upper == 0.0) return 0.0;
+  if (std::isinf(lower) || std::isinf(upper)) {
+    if (std::isinf(lower) && std::isinf(upper)) return kNaN64;
+    return std::isinf(lower) ? lower : upper;
+  }
+  if (std::signbit(lower) == std::signbit(upper)) return lower + (upper - lower) / 2.0;
+  return (lower + upper) / 2.0;
+}
+
+// Sum (Neumaier), src/mean.rs:7-26.
+struct Sum {
+  double value = 0.0, correction = 0.0;
+  void add(double x) {
+    double next = value + x;
+    if (std::fabs(value) >= std::fabs(x))
+      correction += (value - next) + x;
+    else
+      correction += (x - next) + value;
+    value = next;
+  }
+  double total() const { return value + correction; }
+};
+
+// Mean, src/mean.rs:28-84.
+struct Mean {
+  Sum sum;
+  uint64_t count = 0;
+  bool nan = false, positive_inf = false, negative_inf = false;
+  void add(double value, const Policy& policy) {
+    if (std::isnan(value)) {
+      nan = nan || !policy.omit;
+      return;
+    }
+    if (policy.omit && policy.ignore_inf && !std::isfinite(value)) return;
+    count += 1;
+    if (std::isinf(value)) {
+      positive_inf = positive_inf || value > 0;
+      negative_inf = negative_inf || value < 0;
+    } else {
+      sum.add(value);
+    }
+  }
+  // Returns false only when finite summation overflowed (src/mean.rs:66-84).
+  bool finish(const Policy& policy, double* out) const {
+    if (nan || count == 0 || (policy.omit && count < policy.min_count)) {
+      *out = kNaN64;
+      return true;
+    }
+    if (positive_inf || negative_inf) {
+      if (positive_inf && negative_inf)
+        *out = kNaN64;
+      else
+        *out = positive_inf ? INFINITY : -INFINITY;
+      return true;
+    }
+    double total = sum.total();
+    if (!std::isfinite(total)) return false;
+    *out = total / (double)count;
+    return true;
+  }
+};
+
+inline double clamp_f64(double x, double lo, double hi) {
+  if (x < lo) return lo;
+  if (x > hi) return hi;
+  return x;
+}
+
+// mean_valid, src/mean.rs:87-113 (retained, non-NaN values).
+double mean_valid(const double* values, size_t n) {
+  Mean mean;
+  Policy propagate;
+  for (size_t i = 0; i < n; ++i) mean.add(values[i], propagate);
+  double result;
+  if (mean.finish(propagate, &result)) return result;
+  double count = (double)n;
+  uint64_t m = (uint64_t)(n - 1);
+  int lz = m == 0 ? 64 : __builtin_clzll(m);
+  int exponent = 64 - lz + 1;
+  double scale = std::ldexp(1.0, exponent);
+  Sum scaled;
+  double lower = INFINITY, upper = -INFINITY;
+  for (size_t i = 0; i < n; ++i) {
+    double v = values[i];
+    lower = std::fmin(lower, v);
+    upper = std::fmax(upper, v);
+    scaled.add(v / scale);
+  }
+  return clamp_f64((scaled.value + scaled.correction) / (count / scale), lower, upper);
+}
+
+// dispersion_valid, src/dispersion.rs:5-61.
+double dispersion_valid(const double* values, size_t n, uint64_t ddof, bool want_std) {
+  if (n <= ddof) return kNaN64;
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(values[i])) return kNaN64;
+  double reference = values[0];
+  bool halve = false;
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(values[i] - reference)) {
+      halve = true;
+      break;
+    }
+  auto delta = [&](double v) { return halve ? v / 2.0 - reference / 2.0 : v - reference; };
+  double scale = 0.0;
+  for (size_t i = 0; i < n; ++i) scale = std::fmax(scale, std::fabs(delta(values[i])));
+  if (scale == 0.0) return 0.0;
+  Sum sum;
+  for (size_t i = 0; i < n; ++i) sum.add(delta(values[i]) / scale);
+  double center = sum.total() / (double)n;
+  Sum squares;
+  for (size_t i = 0; i < n; ++i) {
+    double residual = delta(values[i]) / scale - center;
+    squares.add(residual * residual);
+  }
+  double normalized = squares.total() / (double)(n - ddof);
+  if (want_std) {
+    double result = scale * std::sqrt(normalized);
+    return halve ? result * 2.0 : result;
+  }
+  double result = scale * (scale * normalized);
+  return halve ? result * 4.0 : result;
+}
+
+// split / scale_binary / scaled_dot / WeightedSum / finite_weighted,
+// src/convolution.rs:203-361 (only the two-term, normalize=false use from
+// the percentile interpolation is on this path).
+std::pair<double, int> split(double value) {
+  uint64_t b = bits64(value);
+  int exponent = (int)((b >> 52) & 0x7ff);
+  uint64_t fraction = b & ((1ull << 52) - 1);
+  if (exponent == 0) {
+    int leading = 63 - __builtin_clzll(fraction);
+    double mantissa = (double)fraction / (double)(1ull << leading);
+    return {std::copysign(mantissa, value), leading - 1074};
+  }
+  return {from_bits64((b & ((1ull << 63) | ((1ull << 52) - 1))) | (1023ull << 52)),
+          exponent - 1023};
+}
+
+double scale_binary(double value, int exponent) {
+  if (value == 0.0) return value;
+  auto [mantissa, value_exponent] = split(value);
+  int target = value_exponent + exponent;
+  if (target > 1023) return std::copysign(INFINITY, value);
+  if (target < -1075) return std::copysign(0.0, value);
+  if (target >= -1022) return mantissa * from_bits64((uint64_t)(target + 1023) << 52);
+  double remaining = from_bits64((uint64_t)(target + 1022 + 1023) << 52);
+  return (mantissa * 2.2250738585072014e-308) * remaining;
+}
+
+int count_bits(size_t len) {
+  uint64_t m = (uint64_t)(len - 1);
+  return m == 0 ? 0 : 64 - __builtin_clzll(m);
+}
+
+std::pair<double, int> scaled_dot(const double (*pairs)[2], size_t n) {
+  bool any = false;
+  int maximum = INT32_MIN;
+  for (size_t i = 0; i < n; ++i) {
+    if (pairs[i][0] == 0.0) continue;
+    int e = split(pairs[i][0]).second + split(pairs[i][1]).second;
+    maximum = any ? std::max(maximum, e) : e;
+    any = true;
+  }
+  if (!any) return {0.0, 0};
+  int exponent = maximum + count_bits(n) + 2;
+  Sum sum;
+  for (size_t i = 0; i < n; ++i) {
+    if (pairs[i][0] == 0.0) continue;
+    auto [vm, ve] = split(pairs[i][0]);
+    auto [wm, we] = split(pairs[i][1]);
+    sum.add(scale_binary(vm * wm, ve + we - exponent));
+  }
+  return {sum.total(), exponent};
+}
+
+double finite_weighted2(double v0, double w0, double v1, double w1) {
+  const double pairs[2][2] = {{v0, w0}, {v1, w1}};
+  // WeightedSum::add / finish with normalize = false.
+  Sum sum;
+  bool fallback = false;
+  for (int i = 0; i < 2 && !fallback; ++i) {
+    double value = pairs[i][0], weight = pairs[i][1];
+    double product = value * weight;
+    if (!std::isfinite(product) ||
+        (value != 0.0 && std::fabs(product) < 2.2250738585072014e-308)) {
+      fallback = true;
+      break;
+    }
+    sum.add(product);
+  }
+  if (!fallback) {
+    double total = sum.total();
+    if (std::isfinite(total)) return total;
+  }
+  auto [total, exponent] = scaled_dot(pairs, 2);
+  return scale_binary(total, exponent);
+}
+
+// interpolate, src/robust.rs:305-341.
+double interpolate(double lower, double upper, double fraction) {
+  if (fraction == 0.0 || bits64(lower) == bits64(upper)) return lower;
+  if (fraction == 1.0) return upper;
+  if (std::isinf(lower) || std::isinf(upper)) {
+    if (lower == -INFINITY && upper == INFINITY) return kNaN64;
+    return std::isinf(lower) ? lower : upper;
+  }
+  if (std::signbit(lower) != std::signbit(upper)) {
+    if (!std::isfinite(upper - lower)) {
+      double half_lower = lower / 2.0;
+      double half_upper = upper / 2.0;
+      return clamp_f64((half_lower + (half_upper - half_lower) * fraction) * 2.0, lower, upper);
+    }
+    return finite_weighted2(lower, 1.0 - fraction, upper, fraction);
+  }
+  double difference = upper - lower;
+  double result = fraction <= 0.5 ? lower + difference * fraction
+                                  : upper - difference * (1.0 - fraction);
+  return clamp_f64(result, lower, upper);
+}
+
+inline bool key_less(double a, double b) { return total_key(a) < total_key(b); }
+
+// k-th smallest in total order (select_nth_unstable_by total_cmp).
+double select_nth(std::vector<double>& v, size_t k) {
+  std::nth_element(v.begin(), v.begin() + k, v.end(), key_less);
+  return v[k];
+}
+
+// percentile, src/robust.rs:343-352.
+double percentile(std::vector<double>& values, double q) {
+  std::sort(values.begin(), values.end(), key_less);
+  size_t n = values.size();
+  if (q == 100.0) return values[n - 1];
+  double rank = (q / 100.0) * (double)(n - 1);
+  size_t lower = (size_t)std::floor(rank);
+  size_t upper = std::min(lower + 1, n - 1);
+  return interpolate(values[lower], values[upper], rank - (double)lower);
+}
+
+// Median of retained values: exact middle for odd counts, midpoint of the
+// two middle values (total order) for even counts.
+double median_valid(std::vector<double>& values) {
+  size_t n = values.size();
+  if (n % 2 == 1) return select_nth(values, n / 2);
+  double upper = select_nth(values, n / 2);
+  double lower = *std::max_element(values.begin(), values.begin() + n / 2, key_less);
+  return midpoint(lower, upper);
+}
+
+struct Reduction {
+  int kind = kMedian;
+  Policy policy;
+  uint64_t parameter = 0;  // rank or ddof
+  double q = 50.0;         // percentile
+};
+
+// Reduction::finish, src/reduction.rs:78-130 (and RobustReduction::finish,
+// src/robust.rs:244-299, for the percentile kind). Returns float64; the
+// caller casts once to the output dtype.
+double finish(const Reduction& r, std::vector<double>& values) {
+  if (!r.policy.omit) {
+    for (double v : values)
+      if (std::isnan(v)) return kNaN64;
+  } else {
+    size_t write = 0;
+    for (size_t read = 0; read < values.size(); ++read)
+      if (retained(values[read], r.policy)) values[write++] = values[read];
+    values.resize(write);
+    if (write < r.policy.min_count) return kNaN64;
+  }
+  switch (r.kind) {
+    case kMedian:
+    case kMedianNetwork:
+    case kMedianHistogram:
+      return values.empty() ? kNaN64 : median_valid(values);
+    case kMean:
+    case kMeanRolling:
+      return mean_valid(values.data(), values.size());
+    case kMin:
+      return values.empty() ? kNaN64 : *std::min_element(values.begin(), values.end(), key_less);
+    case kMax:
+      return values.empty() ? kNaN64 : *std::max_element(values.begin(), values.end(), key_less);
+    case kVar:
+      return dispersion_valid(values.data(), values.size(), r.parameter, false);
+    case kStd:
+      return dispersion_valid(values.data(), values.size(), r.parameter, true);
+    case kRank:
+    case kRankHistogram:
+      if (r.parameter >= values.size()) return kNaN64;
+      return select_nth(values, (size_t)r.parameter);
+    case kPercentile:
+      if (values.empty()) return kNaN64;
+      return percentile(values, r.q);
+  }
+  return kNaN64;
+}
+
+template <class T>
+inline T cast_out(double v) {
+  if (std::isnan(v)) return std::numeric_limits<T>::quiet_NaN();
+  return (T)v;
+}
+
+// filter_offsets, src/filter_nd.rs:125-172 (the mean streams through Mean;
+// everything else gathers the window and calls finish).
+template <class T>
+void filter_offsets(const Window& w, const T* input, double cval, const Reduction& r,
+                    size_t start, size_t end, T* output) {
+  std::vector<int64_t> index(w.rank);
+  std::vector<double> scratch;
+  scratch.reserve(w.count);
+  for (size_t center = start; center < end; ++center) {
+    if (r.kind == kMean) {
+      Mean mean;
+      visit(w, input, center, cval, index.data(), [&](double v) { mean.add(v, r.policy); });
+      double result;
+      if (mean.finish(r.policy, &result)) {
+        output[center - start] = cast_out<T>(result);
+        continue;
+      }
+    }
+    scratch.clear();
+    visit(w, input, center, cval, index.data(), [&](double v) { scratch.push_back(v); });
+    output[center - start] = cast_out<T>(finish(r, scratch));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sorting network, src/median_network.rs:9-209.
+
+template <class T>
+struct KeyOf;
+template <>
+struct KeyOf<float> {
+  using K = int32_t;
+  static K key(float v) {
+    int32_t b;
+    std::memcpy(&b, &v, 4);
+    return b ^ (int32_t)((uint32_t)(b >> 31) >> 1);
+  }
+  static float value(K k) {
+    int32_t b = k ^ (int32_t)((uint32_t)(k >> 31) >> 1);
+    float v;
+    std::memcpy(&v, &b, 4);
+    return v;
+  }
+};
+template <>
+struct KeyOf<double> {
+  using K = int64_t;
+  static K key(double v) {
+    int64_t b;
+    std::memcpy(&b, &v, 8);
+    return b ^ (int64_t)((uint64_t)(b >> 63) >> 1);
+  }
+  static double value(K k) {
+    int64_t b = k ^ (int64_t)((uint64_t)(k >> 63) >> 1);
+    double v;
+    std::memcpy(&v, &b, 8);
+    return v;
+  }
+};
+
+struct Comparator {
+  uint32_t lower, upper;
+  bool keep_lower, keep_upper;
+};
+
+void net_merge(size_t start, size_t length, size_t stride, size_t count,
+               std::vector<Comparator>& out) {
+  if (start >= count) return;
+  size_t step = stride * 2;
+  if (step < length) {
+    net_merge(start, length, step, count, out);
+    net_merge(start + stride, length, step, count, out);
+    for (size_t lower = start + stride; lower + stride < start + length; lower += step)
+      if (lower + stride < count) out.push_back({(uint32_t)lower, (uint32_t)(lower + stride), true, true});
+  } else if (start + stride < count) {
+    out.push_back({(uint32_t)start, (uint32_t)(start + stride), true, true});
+  }
+}
+
+void net_sort(size_t start, size_t length, size_t count, std::vector<Comparator>& out) {
+  if (length > 1 && start < count) {
+    size_t half = length / 2;
+    net_sort(start, half, count, out);
+    net_sort(start + half, half, count, out);
+    net_merge(start, length, 1, count, out);
+  }
+}
+
+// Network::new, src/median_network.rs:116-155.
+std::vector<Comparator> network_new(size_t count, const Policy& policy) {
+  size_t wires = 1;
+  while (wires < count) wires <<= 1;
+  std::vector<Comparator> comparisons;
+  net_sort(0, wires, count, comparisons);
+  std::vector<bool> live(count, false);
+  if (!policy.omit) {
+    live[count / 2] = true;
+    live[(count - 1) / 2] = true;
+  } else {
+    std::fill(live.begin(), live.end(), true);
+  }
+  std::vector<Comparator> kept;
+  for (auto it = comparisons.rbegin(); it != comparisons.rend(); ++it) {
+    Comparator c = *it;
+    if (!live[c.lower] && !live[c.upper]) continue;
+    c.keep_lower = live[c.lower];
+    c.keep_upper = live[c.upper];
+    live[c.lower] = true;
+    live[c.upper] = true;
+    kept.push_back(c);
+  }
+  std::reverse(kept.begin(), kept.end());
+  return kept;
+}
+
+// Window::row_run, src/window.rs:164-191.
+bool row_run(const Window& w, size_t center, size_t limit, int64_t* index, size_t* width) {
+  bool interior = prepare(w, center, index);
+  int last = w.rank - 1;
+  size_t row_left = (size_t)(w.shape[last] - index[last]);
+  if (!interior) {
+    bool other_inside = true;
+    for (int a = 0; a < last; ++a)
+      other_inside = other_inside && index[a] + w.low[a] >= 0 && index[a] + w.high[a] < w.shape[a];
+    int64_t left_edge = index[last] + w.low[last];
+    size_t wd = (other_inside && left_edge < 0) ? std::min(row_left, (size_t)(-left_edge)) : row_left;
+    *width = std::min(limit, wd);
+    return false;
+  }
+  size_t end = (size_t)(w.shape[last] - std::max<int64_t>(w.high[last], 0));
+  *width = std::min(limit, end - (size_t)index[last]);
+  return true;
+}
+
+// filter_range with the network, src/filter_nd.rs:62-123, encode_plane
+// src/median_network.rs:40-63 and Network::apply :157-209.
+template <class T>
+void filter_range_network(const Window& w, const T* input, double cval, const Reduction& r,
+                          const std::vector<Comparator>& net, size_t start, size_t end,
+                          T* output) {
+  using KO = KeyOf<T>;
+  using K = typename KO::K;
+  const K nan_key = KO::key(std::numeric_limits<T>::quiet_NaN());
+  std::vector<int64_t> index(w.rank);
+  std::vector<K> keys;
+  std::vector<uint32_t> valid;
+  size_t offset = start;
+  const size_t count = w.count;
+  while (offset < end) {
+    size_t width;
+    bool interior = row_run(w, offset, end - offset, index.data(), &width);
+    if (!interior) {
+      filter_offsets(w, input, cval, r, offset, offset + width, output + (offset - start));
+      offset += width;
+      continue;
+    }
+    keys.assign(count * width, nan_key);
+    valid.assign(width, 0);
+    for (size_t tap = 0; tap < count; ++tap) {
+      const T* plane = input + offset + w.flat[tap];
+      K* kp = keys.data() + tap * width;
+      for (size_t c = 0; c < width; ++c) {
+        T v = plane[c];
+        bool drop = std::isnan(v) || (r.policy.omit && r.policy.ignore_inf && !std::isfinite(v));
+        kp[c] = drop ? nan_key : KO::key(v);
+        valid[c] += drop ? 0u : 1u;
+      }
+    }
+    for (const Comparator& cmp : net) {
+      K* lo = keys.data() + (size_t)cmp.lower * width;
+      K* hi = keys.data() + (size_t)cmp.upper * width;
+      if (cmp.keep_lower && cmp.keep_upper) {
+        for (size_t c = 0; c < width; ++c) {
+          K a = lo[c], b = hi[c];
+          lo[c] = a < b ? a : b;
+          hi[c] = a < b ? b : a;
+        }
+      } else if (cmp.keep_lower) {
+        for (size_t c = 0; c < width; ++c) lo[c] = lo[c] < hi[c] ? lo[c] : hi[c];
+      } else {
+        for (size_t c = 0; c < width; ++c) hi[c] = lo[c] < hi[c] ? hi[c] : lo[c];
+      }
+    }
+    T* out = output + (offset - start);
+    for (size_t c = 0; c < width; ++c) {
+      size_t v = valid[c];
+      bool missing = !r.policy.omit ? v != count : v < r.policy.min_count;
+      if (missing || v == 0) {
+        out[c] = std::numeric_limits<T>::quiet_NaN();
+      } else if (v % 2 == 1) {
+        out[c] = KO::value(keys[(v / 2) * width + c]);
+      } else {
+        double lower = (double)KO::value(keys[(v / 2 - 1) * width + c]);
+        double upper = (double)KO::value(keys[(v / 2) * width + c]);
+        out[c] = cast_out<T>(midpoint(lower, upper));
+      }
+    }
+    offset += width;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Block histogram, src/histogram.rs:37-631.
+
+constexpr uint32_t kOmitted = UINT32_MAX;
+constexpr uint32_t kPropagatedNaN = UINT32_MAX - 1;
+constexpr int kGroupShift = 12;
+constexpr uint64_t kMinBlock = 32;
+constexpr int64_t kOutside = INT64_MIN;
+
+std::vector<uint64_t> block_lengths(const std::vector<int64_t>& shape, const uint64_t* size) {
+  std::vector<uint64_t> out(shape.size());
+  for (size_t a = 0; a < shape.size(); ++a) {
+    uint64_t length = (uint64_t)shape[a];
+    uint64_t blocks = std::max<uint64_t>(length / std::max<uint64_t>(size[a], kMinBlock), 1);
+    out[a] = std::max<uint64_t>((length + blocks - 1) / blocks, 1);
+  }
+  return out;
+}
+
+int validate_support(const std::vector<int64_t>& shape, const uint64_t* size) {
+  auto block = block_lengths(shape, size);
+  uint64_t support = 1;
+  for (size_t a = 0; a < shape.size(); ++a) {
+    uint64_t length = block[a] + size[a] - 1;
+    if (length != 0 && support > UINT64_MAX / length)
+      return fail(kOverflow, "shape or index arithmetic overflowed");
+    support *= length;
+  }
+  if (support > kPropagatedNaN) return fail(kOverflow, "shape or index arithmetic overflowed");
+  return kOk;
+}
+
+inline uint32_t select_in_word(uint64_t word, uint32_t k) {
+  uint32_t position = 0;
+  for (int width : {32, 16, 8, 4, 2, 1}) {
+    uint32_t low = (uint32_t)__builtin_popcountll(word & ((1ull << width) - 1));
+    if (k >= low) {
+      k -= low;
+      word >>= width;
+      position += width;
+    }
+  }
+  return position;
+}
+
+struct Histogram {
+  std::vector<uint64_t> words;
+  std::vector<uint32_t> groups;
+  size_t count = 0, nan = 0;
+  void add(uint32_t code) {
+    if (code < kPropagatedNaN) {
+      words[code >> 6] |= 1ull << (code & 63);
+      groups[code >> kGroupShift] += 1;
+      count += 1;
+    } else if (code == kPropagatedNaN) {
+      nan += 1;
+    }
+  }
+  void remove(uint32_t code) {
+    if (code < kPropagatedNaN) {
+      words[code >> 6] &= ~(1ull << (code & 63));
+      groups[code >> kGroupShift] -= 1;
+      count -= 1;
+    } else if (code == kPropagatedNaN) {
+      nan -= 1;
+    }
+  }
+  size_t select(size_t k) const {
+    size_t group = 0;
+    while (k >= groups[group]) {
+      k -= groups[group];
+      group += 1;
+    }
+    size_t index = group << (kGroupShift - 6);
+    while (true) {
+      size_t c = (size_t)__builtin_popcountll(words[index]);
+      if (k < c) break;
+      k -= c;
+      index += 1;
+    }
+    return (index << 6) + select_in_word(words[index], (uint32_t)k);
+  }
+};
+
+// for_each_in_box, src/histogram.rs:199-240.
+template <class F>
+void for_each_in_box(const std::vector<size_t>& low, const std::vector<size_t>& lengths,
+                     const std::vector<size_t>& strides, F&& visit_fn) {
+  int rank = (int)low.size();
+  int inner = rank - 1;
+  for (int a = rank - 1; a >= 0; --a)
+    if (lengths[a] > 1) {
+      inner = a;
+      break;
+    }
+  std::vector<size_t> counter(rank, 0);
+  size_t base = 0;
+  for (int a = 0; a < rank; ++a) base += low[a] * strides[a];
+  while (true) {
+    size_t idx = base;
+    for (size_t i = 0; i < lengths[inner]; ++i) {
+      visit_fn(idx);
+      idx += strides[inner];
+    }
+    int axis = rank;
+    while (true) {
+      if (axis == 0) return;
+      axis -= 1;
+      if (axis == inner) continue;
+      counter[axis] += 1;
+      base += strides[axis];
+      if (counter[axis] < lengths[axis]) break;
+      base -= strides[axis] * lengths[axis];
+      counter[axis] = 0;
+    }
+  }
+}
+
+template <class T>
+struct HistGeometry {
+  const T* input;
+  std::vector<int64_t> shape;
+  std::vector<uint64_t> size;
+  std::vector<int> modes;
+  std::vector<int64_t> anchors, strides;
+  std::vector<uint64_t> block;
+  std::vector<int> order;
+  double cval;
+  Policy policy;
+  bool median;
+  uint64_t rank_k;
+};
+
+// Geometry::block, src/histogram.rs:302-486. Writes outputs in place.
+template <class T>
+void hist_block(const HistGeometry<T>& g, const std::vector<size_t>& start,
+                const std::vector<size_t>& extent, T* output) {
+  using KO = KeyOf<T>;
+  using K = typename KO::K;
+  int rank = (int)g.shape.size();
+  std::vector<size_t> lengths(rank), sstr(rank, 1);
+  for (int a = 0; a < rank; ++a) lengths[a] = extent[a] + g.size[a] - 1;
+  for (int a = rank - 2; a >= 0; --a) sstr[a] = sstr[a + 1] * lengths[a + 1];
+  size_t total = sstr[0] * lengths[0];
+  std::vector<std::vector<int64_t>> maps(rank);
+  for (int a = 0; a < rank; ++a) {
+    int64_t first = (int64_t)start[a] - g.anchors[a];
+    maps[a].resize(lengths[a]);
+    for (size_t s = 0; s < lengths[a]; ++s) {
+      int64_t m;
+      int rr = map_index(first + (int64_t)s, g.shape[a], g.modes[a], &m);
+      maps[a][s] = rr == 1 ? m * g.strides[a] : kOutside;
+    }
+  }
+  std::vector<uint32_t> codes(total, kOmitted);
+  std::vector<std::pair<K, uint32_t>> pairs;
+  pairs.reserve(total);
+  int last = rank - 1;
+  std::vector<size_t> counter(rank, 0);
+  size_t sidx = 0;
+  while (true) {
+    int64_t base = 0;
+    bool outside = false;
+    for (int a = 0; a < last; ++a) {
+      int64_t off = maps[a][counter[a]];
+      outside = outside || off == kOutside;
+      base += off == kOutside ? 0 : off;
+    }
+    for (size_t s = 0; s < lengths[last]; ++s) {
+      int64_t off = maps[last][s];
+      T value = (outside || off == kOutside) ? (T)g.cval : g.input[base + off];
+      bool keep = !std::isnan(value) &&
+                  !(g.policy.omit && g.policy.ignore_inf && !std::isfinite(value));
+      if (keep)
+        pairs.push_back({KO::key(value), (uint32_t)sidx});
+      else if (!g.policy.omit)
+        codes[sidx] = kPropagatedNaN;
+      sidx += 1;
+    }
+    int axis = last;
+    bool done = false;
+    while (true) {
+      if (axis == 0) {
+        done = true;
+        break;
+      }
+      axis -= 1;
+      if (++counter[axis] < lengths[axis]) break;
+      counter[axis] = 0;
+    }
+    if (done) break;
+  }
+  std::sort(pairs.begin(), pairs.end());
+  std::vector<T> values(pairs.size());
+  for (size_t i = 0; i < pairs.size(); ++i) {
+    codes[pairs[i].second] = (uint32_t)i;
+    values[i] = KO::value(pairs[i].first);
+  }
+  size_t ranks = pairs.size();
+  Histogram h;
+  h.words.assign((ranks + 63) / 64, 0);
+  h.groups.assign((ranks + (1u << kGroupShift) - 1) >> kGroupShift, 0);
+
+  std::vector<size_t> position(rank, 0), low(rank, 0), box(g.size.begin(), g.size.end());
+  std::vector<bool> direction(rank, true);
+  for_each_in_box(position, box, sstr, [&](size_t i) { h.add(codes[i]); });
+  while (true) {
+    size_t offset = 0;
+    for (int a = 0; a < rank; ++a) offset += (start[a] + position[a]) * (size_t)g.strides[a];
+    // Histogram::finish, src/histogram.rs:145-190.
+    T result;
+    if ((!g.policy.omit && h.nan > 0) || (g.policy.omit && h.count < g.policy.min_count)) {
+      result = std::numeric_limits<T>::quiet_NaN();
+    } else if (g.median) {
+      if (h.count % 2 == 1) {
+        result = values[h.select(h.count / 2)];
+      } else {
+        double lo = (double)values[h.select(h.count / 2 - 1)];
+        double hi = (double)values[h.select(h.count / 2)];
+        result = cast_out<T>(midpoint(lo, hi));
+      }
+    } else {
+      result = g.rank_k < h.count ? values[h.select((size_t)g.rank_k)]
+                                  : std::numeric_limits<T>::quiet_NaN();
+    }
+    output[offset] = result;
+    int moved = -1;
+    for (int oi = rank - 1; oi >= 0; --oi) {
+      int axis = g.order[oi];
+      bool can_move = direction[axis] ? position[axis] + 1 < extent[axis] : position[axis] > 0;
+      if (can_move) {
+        moved = axis;
+        break;
+      }
+      direction[axis] = !direction[axis];
+    }
+    if (moved < 0) break;
+    int axis = moved;
+    size_t removed, added;
+    if (direction[axis]) {
+      removed = position[axis];
+      added = position[axis] + g.size[axis];
+    } else {
+      removed = position[axis] + g.size[axis] - 1;
+      added = position[axis] - 1;
+    }
+    low = position;
+    box[axis] = 1;
+    low[axis] = removed;
+    for_each_in_box(low, box, sstr, [&](size_t i) { h.remove(codes[i]); });
+    low[axis] = added;
+    for_each_in_box(low, box, sstr, [&](size_t i) { h.add(codes[i]); });
+    box[axis] = g.size[axis];
+    if (direction[axis])
+      position[axis] += 1;
+    else
+      position[axis] -= 1;
+  }
+}
+
+template <class Fn>
+void run_parallel(size_t items, int threads, Fn&& fn) {
+  if (threads <= 1 || items <= 1) {
+    fn(0, items);
+    return;
+  }
+  size_t chunk = (items + (size_t)threads - 1) / (size_t)threads;
+  std::vector<std::thread> pool;
+  for (size_t s = 0; s < items; s += chunk) {
+    size_t e = std::min(items, s + chunk);
+    pool.emplace_back([&fn, s, e] { fn(s, e); });
+  }
+  for (auto& t : pool) t.join();
+}
+
+// order_statistic_into, src/histogram.rs:494-566 (blocks in parallel).
+template <class T>
+int histogram_filter(const Window& w, const uint64_t* size, const int64_t* origin,
+                     const T* input, double cval, const Policy& policy, bool median,
+                     uint64_t rank_k, int threads, T* output) {
+  HistGeometry<T> g;
+  g.input = input;
+  g.shape = w.shape;
+  g.size.assign(size, size + w.rank);
+  g.modes = w.modes;
+  g.strides = w.strides;
+  g.cval = cval;
+  g.policy = policy;
+  g.median = median;
+  g.rank_k = rank_k;
+  int rank = w.rank;
+  int rc = validate_support(g.shape, size);
+  if (rc) return rc;
+  for (int a = 0; a < rank; ++a) g.anchors.push_back((int64_t)size[a] / 2 + origin[a]);
+  int fastest = 0;
+  for (int a = 0; a < rank; ++a)
+    if (size[a] >= size[fastest]) fastest = a;
+  for (int a = 0; a < rank; ++a)
+    if (a != fastest) g.order.push_back(a);
+  g.order.push_back(fastest);
+  g.block = block_lengths(g.shape, size);
+  std::vector<size_t> blocks(rank);
+  size_t nblocks = 1;
+  for (int a = 0; a < rank; ++a) {
+    blocks[a] = (size_t)((g.shape[a] + g.block[a] - 1) / g.block[a]);
+    nblocks *= blocks[a];
+  }
+  std::atomic<size_t> next{0};
+  auto worker = [&](size_t, size_t) {
+    std::vector<size_t> start(rank), extent(rank);
+    while (true) {
+      size_t b = next.fetch_add(1);
+      if (b >= nblocks) break;
+      size_t rem = b;
+      for (int a = rank - 1; a >= 0; --a) {
+        start[a] = (rem % blocks[a]) * g.block[a];
+        rem /= blocks[a];
+        extent[a] = std::min<size_t>(g.block[a], (size_t)g.shape[a] - start[a]);
+      }
+      hist_block(g, start, extent, output);
+    }
+  };
+  if (threads <= 1) {
+    worker(0, 0);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back([&] { worker(0, 0); });
+    for (auto& t : pool) t.join();
+  }
+  return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Exact window moments for the precision study (not a reference algorithm:
+// the FP64 "exact-sum" oracle). Double-double accumulation of pivot-shifted
+// sums with error-free transformations gives about 104 significant bits.
+
+struct DD {
+  double hi = 0.0, lo = 0.0;
+};
+inline DD two_sum(double a, double b) {
+  double s = a + b;
+  double bb = s - a;
+  double e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+inline DD two_prod(double a, double b) {
+  double p = a * b;
+  double e = std::fma(a, b, -p);
+  return {p, e};
+}
+inline DD dd_add(DD a, DD b) {
+  DD s = two_sum(a.hi, b.hi);
+  DD t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return two_sum(s.hi, s.lo);
+}
+inline DD dd_mul(DD a, DD b) {
+  DD p = two_prod(a.hi, b.hi);
+  p.lo += a.hi * b.lo + a.lo * b.hi;
+  return two_sum(p.hi, p.lo);
+}
+inline DD dd_div_d(DD a, double b) {
+  double q1 = a.hi / b;
+  DD p = two_prod(q1, b);
+  DD r = dd_add(a, DD{-p.hi, -p.lo});
+  double q2 = r.hi / b;
+  DD p2 = two_prod(q2, b);
+  DD r2 = dd_add(r, DD{-p2.hi, -p2.lo});
+  double q3 = r2.hi / b;
+  DD q = two_sum(q1, q2);
+  return dd_add(q, DD{q3, 0.0});
+}
+
+// Mean, variance and standard deviation of retained finite values with
+// about 100-bit accuracy, rounded to float64 once.
+double exact_moment(const std::vector<double>& values, int which, uint64_t ddof) {
+  size_t n = values.size();
+  if (which == kMean) {
+    bool pinf = false, ninf = false;
+    for (double v : values) {
+      pinf = pinf || v == INFINITY;
+      ninf = ninf || v == -INFINITY;
+    }
+    if (n == 0) return kNaN64;
+    if (pinf && ninf) return kNaN64;
+    if (pinf) return INFINITY;
+    if (ninf) return -INFINITY;
+  } else {
+    if (n <= ddof) return kNaN64;
+    for (double v : values)
+      if (!std::isfinite(v)) return kNaN64;
+  }
+  if (n == 0) return kNaN64;
+  double pivot = values[0];
+  DD s1, s2;
+  for (double v : values) {
+    DD d = two_sum(v, -pivot);
+    s1 = dd_add(s1, d);
+    s2 = dd_add(s2, dd_mul(d, d));
+  }
+  if (which == kMean) {
+    DD m = dd_add(dd_div_d(s1, (double)n), DD{pivot, 0.0});
+    return m.hi + m.lo;
+  }
+  // SS = S2 - S1^2 / n
+  DD s1sq = dd_mul(s1, s1);
+  DD corr = dd_div_d(s1sq, (double)n);
+  DD ss = dd_add(s2, DD{-corr.hi, -corr.lo});
+  DD var = dd_div_d(ss, (double)(n - ddof));
+  if (which == kVar) return var.hi + var.lo;
+  if (var.hi <= 0.0) return 0.0;
+  double root = std::sqrt(var.hi);
+  // One Newton step in double-double: r + (var - r^2) / (2r).
+  DD r2 = two_prod(root, root);
+  DD diff = dd_add(var, DD{-r2.hi, -r2.lo});
+  return root + (diff.hi + diff.lo) / (2.0 * root);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C-ABI of the oracle (ctypes from tests/ and bench.py only).
+
+extern "C" {
+
+const char* ndfo_last_error() { return g_message.c_str(); }
+
+int ndfo_map_index(int64_t index, uint64_t length, int32_t mode, int64_t* out) {
+  int r = map_index(index, (int64_t)length, mode, out);
+  return r;
+}
+
+double ndfo_midpoint(double lower, double upper) { return midpoint(lower, upper); }
+double ndfo_interpolate(double lower, double upper, double fraction) {
+  return interpolate(lower, upper, fraction);
+}
+double ndfo_mean_valid(const double* values, uint64_t n) { return mean_valid(values, n); }
+double ndfo_dispersion_valid(const double* values, uint64_t n, uint64_t ddof, int32_t want_std) {
+  return dispersion_valid(values, n, ddof, want_std != 0);
+}
+double ndfo_percentile(const double* values, uint64_t n, double q) {
+  std::vector<double> v(values, values + n);
+  return percentile(v, q);
+}
+
+// Window taps (count * rank offsets, tap-major) for geometry tests.
+int ndfo_window_taps(int32_t rank, const uint64_t* shape, const uint64_t* size,
+                     const uint8_t* footprint, const int64_t* origin, const int32_t* modes,
+                     int64_t* taps_out, uint64_t capacity, uint64_t* count_out) {
+  Window w;
+  int rc = window_new(rank, shape, size, footprint, origin, modes, &w);
+  if (rc) return rc;
+  *count_out = w.count;
+  if (capacity < w.count * (uint64_t)rank) return kLength;
+  std::memcpy(taps_out, w.taps.data(), w.taps.size() * sizeof(int64_t));
+  return kOk;
+}
+
+// Network comparator count (for the zero-one and pruning tests).
+uint64_t ndfo_network_size(uint64_t count, int32_t omit) {
+  Policy p;
+  p.omit = omit != 0;
+  return network_new(count, p).size();
+}
+
+// window_filter / robust_filter(kind="percentile") over one C-contiguous
+// array; `dtype` 0 = float32, 1 = float64. `kind` uses the C-ABI numbering.
+int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* input,
+                void* output, const uint64_t* size, const uint8_t* footprint,
+                const int64_t* origin, const int32_t* modes, double cval, int32_t kind,
+                int32_t omit_nan, int32_t ignore_inf, uint64_t min_count, uint64_t parameter,
+                double q, int32_t threads) {
+  Window w;
+  // Histogram plans validate the rectangle without materializing taps
+  // (src/plan.rs:294-312 calls validate_rectangular, not Window::new).
+  bool hist_plan = kind == kMedianHistogram || kind == kRankHistogram;
+  int rc = window_new(rank, shape, size, footprint, origin, modes, &w, !hist_plan);
+  if (rc) return rc;
+  Reduction r;
+  r.kind = kind;
+  r.policy.omit = omit_nan != 0;
+  r.policy.ignore_inf = ignore_inf != 0;
+  r.policy.min_count = min_count;
+  r.parameter = parameter;
+  r.q = q;
+  if (r.policy.omit && (min_count == 0 || min_count > w.count))
+    return fail(kInvalid, kind == kPercentile
+                              ? "min_count must be between one and the number of window elements"
+                              : "min_count must be between 1 and the number of window elements");
+  if (kind == kPercentile && (!std::isfinite(q) || q < 0.0 || q > 100.0))
+    return fail(kInvalid, "percentile must be finite and between zero and 100");
+  if (kind == kMeanRolling) return fail(kInvalid, "rolling means are not part of this oracle");
+  bool hist = kind == kMedianHistogram || kind == kRankHistogram;
+  if (hist) {
+    if (footprint)
+      return fail(kInvalid, "histogram reductions require rectangular size, not footprint");
+    rc = validate_support(w.shape, size);
+    if (rc) return rc;
+  }
+  size_t n = w.out_len;
+  if (n == 0) return kOk;
+  if (threads < 1) threads = 1;
+  bool f32 = dtype == 0;
+  if (f32) cval = (double)(float)cval;
+  if (hist) {
+    bool median = kind == kMedianHistogram;
+    if (f32)
+      return histogram_filter(w, size, origin, (const float*)input, cval, r.policy, median,
+                              parameter, threads, (float*)output);
+    return histogram_filter(w, size, origin, (const double*)input, cval, r.policy, median,
+                            parameter, threads, (double*)output);
+  }
+  if (kind == kMedianNetwork) {
+    auto net = network_new(w.count, r.policy);
+    if (f32) {
+      run_parallel(n, threads, [&](size_t s, size_t e) {
+        filter_range_network(w, (const float*)input, cval, r, net, s, e, (float*)output + s);
+      });
+    } else {
+      run_parallel(n, threads, [&](size_t s, size_t e) {
+        filter_range_network(w, (const double*)input, cval, r, net, s, e, (double*)output + s);
+      });
+    }
+    return kOk;
+  }
+  if (f32) {
+    run_parallel(n, threads, [&](size_t s, size_t e) {
+      filter_offsets(w, (const float*)input, cval, r, s, e, (float*)output + s);
+    });
+  } else {
+    run_parallel(n, threads, [&](size_t s, size_t e) {
+      filter_offsets(w, (const double*)input, cval, r, s, e, (double*)output + s);
+    });
+  }
+  return kOk;
+}
+
+// Exact (double-double) mean/var/std of every window, rounded to float64,
+// for the precision study. `kind` is kMean, kVar or kStd. Output is float64.
+int ndfo_exact_moments(int32_t dtype, int32_t rank, const uint64_t* shape, const void* input,
+                       double* output, const uint64_t* size, const uint8_t* footprint,
+                       const int64_t* origin, const int32_t* modes, double cval, int32_t kind,
+                       int32_t omit_nan, int32_t ignore_inf, uint64_t min_count, uint64_t ddof,
+                       int32_t threads) {
+  Window w;
+  int rc = window_new(rank, shape, size, footprint, origin, modes, &w);
+  if (rc) return rc;
+  Policy p;
+  p.omit = omit_nan != 0;
+  p.ignore_inf = ignore_inf != 0;
+  p.min_count = min_count;
+  if (dtype == 0) cval = (double)(float)cval;
+  size_t n = w.out_len;
+  auto body = [&](auto tag, size_t s, size_t e) {
+    using T = decltype(tag);
+    const T* in = (const T*)input;
+    std::vector<int64_t> index(w.rank);
+    std::vector<double> values;
+    for (size_t c = s; c < e; ++c) {
+      values.clear();
+      bool nan = false;
+      visit(w, in, c, cval, index.data(), [&](double v) {
+        if (std::isnan(v)) {
+          nan = nan || !p.omit;
+          return;
+        }
+        if (p.omit && p.ignore_inf && !std::isfinite(v)) return;
+        values.push_back(v);
+      });
+      if (nan || (p.omit && values.size() < p.min_count)) {
+        output[c] = kNaN64;
+        continue;
+      }
+      output[c] = exact_moment(values, kind, ddof);
+    }
+  };
+  if (dtype == 0)
+    run_parallel(n, threads, [&](size_t s, size_t e) { body(float{}, s, e); });
+  else
+    run_parallel(n, threads, [&](size_t s, size_t e) { body(double{}, s, e); });
+  return kOk;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+"""Public API semantics on the GPU: layouts, ownership, canonical NaN, signed
+zeros, SciPy agreement, footprints and origins (the reference's
+tests/test_layout.py, test_semantics.py, test_boundaries.py and
+test_footprint.py restated)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.conftest import bits
+
+pytestmark = pytest.mark.gpu
+
+
+def test_layouts_return_owned_c_arrays(gpu) -> None:
+    nf = gpu
+    source = np.arange(24.0, dtype=np.float64).reshape(4, 6)
+    for view in (source[::-1, ::2], np.asfortranarray(source), source.T, source.copy()):
+        view.flags.writeable = False
+        result = nf.median_filter(view, size=1)
+        np.testing.assert_array_equal(result, view)
+        assert result.flags.c_contiguous and result.flags.owndata and result.flags.writeable
+        assert result.base is None
+
+
+def test_strided_inputs_match_and_are_not_modified(gpu) -> None:
+    nf = gpu
+    for dtype in (np.float32, np.float64):
+        source = np.arange(80, dtype=dtype).reshape(8, 10) - 40
+        source[2, :5] = [np.nan, np.inf, -np.inf, -0.0, 0.0]
+        for array in (source.T, source[::-1, ::2], np.asfortranarray(source)):
+            original = array.copy()
+            options = dict(size=(2, 3), origin=(-1, 1), mode=("mirror", "constant"))
+            for fn in (nf.median_filter, nf.nanmedian_filter):
+                direct = fn(array, method="direct", **options)
+                sortnet = fn(array, method="sortnet", **options)
+                hist = fn(array, method="histogram", **options)
+                np.testing.assert_array_equal(bits(sortnet), bits(direct))
+                np.testing.assert_array_equal(bits(hist), bits(direct))
+            np.testing.assert_array_equal(bits(array), bits(original))
+
+
+def test_canonical_nan_and_signed_zero(gpu) -> None:
+    nf = gpu
+    for dtype, canonical in ((np.float32, 0x7FC00000), (np.float64, 0x7FF8000000000000)):
+        propagated = nf.median_filter(np.array([np.nan], dtype=dtype), size=1)
+        below = nf.nanmedian_filter(np.array([1.0, np.nan, np.nan], dtype=dtype), size=3,
+                                    mode="nearest", min_count=2)
+        assert bits(propagated)[0] == canonical and bits(below)[1] == canonical
+    zero = nf.median_filter(np.array([-0.0, -0.0, 0.0]), size=3, mode="nearest")
+    assert np.signbit(zero[1])
+    midpoint = nf.nanmedian_filter(np.asarray([-0.0, 0.0, np.nan]), 3, mode="constant", cval=np.nan)
+    assert bits(midpoint)[1] == 0
+
+
+def test_constant_values_follow_policy(gpu) -> None:
+    nf = gpu
+    values = np.array([np.nan], dtype=np.float64)
+    assert nf.nanmedian_filter(values, 3, mode="constant", cval=2.0, min_count=2)[0] == 2.0
+    assert np.isnan(nf.nanmedian_filter(values, 3, mode="constant", cval=np.inf, ignore_inf=True)[0])
+
+
+def test_scipy_median_on_finite_odd_windows(gpu) -> None:
+    ndimage = pytest.importorskip("scipy.ndimage")
+    nf = gpu
+    for dtype in (np.float32, np.float64):
+        for mode in ("reflect", "constant", "nearest", "mirror", "wrap"):
+            values = np.random.default_rng(1).normal(size=(31, 37)).astype(dtype)
+            expected = ndimage.median_filter(values, size=(3, 5), mode=mode, cval=-7.0)
+            np.testing.assert_array_equal(nf.median_filter(values, (3, 5), mode=mode, cval=-7.0), expected)
+            fp = np.array([[0, 1, 0], [1, 1, 1], [0, 1, 0]], dtype=bool)
+            expected = ndimage.rank_filter(values, 1, footprint=fp, mode=mode, cval=1.5, origin=(1, -1))
+            actual = nf.rank_filter(values, 1, footprint=fp, mode=mode, cval=1.5, origin=(1, -1))
+            np.testing.assert_array_equal(actual, expected)
+            for q in (0.0, 100.0):
+                expected = ndimage.percentile_filter(values, q, footprint=fp, mode=mode, cval=1.5)
+                actual = nf.percentile_filter(values, q, footprint=fp, mode=mode, cval=1.5)
+                np.testing.assert_array_equal(actual, expected)
+
+
+def test_validation_errors_before_device_work(gpu) -> None:
+    nf = gpu
+    with pytest.raises(ValueError, match="requires size, not footprint"):
+        nf.median_filter(np.zeros((5, 5)), footprint=np.ones((3, 3)), method="histogram")
+    with pytest.raises(ValueError, match="method"):
+        nf.median_filter(np.zeros((5, 5)), method="boxcar")
+    with pytest.raises(ValueError, match="min_count"):
+        nf.nanmedian_filter(np.ones(3), size=3, min_count=4)
+    with pytest.raises(NotImplementedError):
+        nf.mean_filter(np.ones((5, 5)), 3, method="boxcar")
+
+
+def test_get_num_threads_is_device_parallelism(gpu) -> None:
+    assert gpu.get_num_threads() == gpu.device_info()["sm_count"]

@@ -1,0 +1,214 @@
+"""CUDA library vs the CPU oracle on seeded inputs.
+
+Order statistics (median / sortnet / histogram, rank, min, max, percentile)
+must be bit-identical. Mean/var/std are bit-identical on the FP64 path and
+within the stated tolerance on the FP32-compensated path: 2 ulp of float32
+output, and 1e-12 relative for float64 output (relative to the window's
+deviation scale, see ``_moment_tolerance``).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.conftest import bits
+
+pytestmark = pytest.mark.gpu
+
+MODES = ("reflect", "constant", "nearest", "mirror", "wrap")
+SELECTIONS = ("median", "median_network", "rank", "min", "max", "percentile")
+
+
+def _special_values(shape, dtype, seed, fraction=0.12):
+    """Values with ties, signed zeros, infinities and NaN payloads
+    (tests/test_histogram_median.py:29-43 style)."""
+    rng = np.random.default_rng(seed)
+    values = (rng.integers(-6, 7, size=shape) / 4).astype(dtype)
+    if values.size:
+        values += rng.normal(size=shape).astype(dtype) * dtype(0.01)
+    payload = np.array([0xFFC01234 if dtype == np.float32 else 0xFFF8000000001234],
+                       dtype=np.uint32 if dtype == np.float32 else np.uint64).view(dtype)[0]
+    special = np.array([np.nan, np.inf, -np.inf, -0.0, 0.0, np.finfo(dtype).max, payload], dtype=dtype)
+    chosen = rng.random(shape) < fraction
+    values[chosen] = rng.choice(special, size=int(chosen.sum()))
+    return values
+
+
+def _gpu(kind, array, size, footprint, origin, mode, cval, omit, ignore_inf, min_count, parameter=0, q=50.0,
+         moments=None):
+    from ndfiltrs_gb300 import _core
+
+    if kind == "percentile":
+        return _core.robust_filter(array, size, footprint, origin, mode, cval, "percentile", q, omit,
+                                   ignore_inf if omit else False, min_count if omit else 1,
+                                   3.0, 3.0, 5, "median", "std")
+    with _core.Plan(array.shape, array.dtype, kind, size, footprint=footprint, origin=origin,
+                    mode=mode, cval=cval, omit_nan=omit, ignore_inf=ignore_inf,
+                    min_count=min_count, parameter=parameter, moments=moments) as plan:
+        return plan.run_host(np.ascontiguousarray(array))
+
+
+def _oracle(oracle, kind, array, size, footprint, origin, mode, cval, omit, ignore_inf, min_count,
+            parameter=0, q=50.0):
+    return oracle.window_filter(array, kind, size, footprint=footprint, origin=origin, mode=mode,
+                                cval=cval, omit_nan=omit, ignore_inf=ignore_inf, min_count=min_count,
+                                parameter=parameter, q=q)
+
+
+def _assert_bits(actual, expected, context):
+    np.testing.assert_array_equal(bits(actual), bits(expected), err_msg=str(context))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("mode", MODES)
+def test_selection_kinds_all_policies_2d(gpu, oracle, dtype, mode) -> None:
+    values = _special_values((37, 45), dtype, seed=11)
+    for size, origin in (((3, 3), (0, 0)), ((5, 4), (1, -2)), ((2, 7), (-1, 3)), ((1, 1), (0, 0))):
+        volume = int(np.prod(size))
+        for omit, ignore_inf, min_count in ((False, False, 1), (True, False, 1),
+                                            (True, True, (volume + 1) // 2), (True, True, volume)):
+            for kind in SELECTIONS:
+                params = [0]
+                if kind == "rank":
+                    params = sorted({0, volume // 3, volume - 1})
+                for parameter in params:
+                    for q in ((16.0, 84.0, 100.0) if kind == "percentile" else (50.0,)):
+                        args = (kind, values, size, None, origin, (mode, mode), 0.5, omit,
+                                ignore_inf, min_count, parameter, q)
+                        _assert_bits(_gpu(*args), _oracle(oracle, *args), args[:1] + args[2:])
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_histogram_kinds_match_direct(gpu, oracle, dtype) -> None:
+    values = _special_values((70, 66), dtype, seed=5)
+    for size, origin, mode in (((3, 3), (0, 0), "reflect"), ((6, 5), (-3, 2), "wrap"),
+                               ((2, 41), (0, -20), "mirror"), ((35, 3), (0, 0), "constant"),
+                               ((33, 31), (0, 0), "nearest"), ((1, 9), (0, 4), "reflect")):
+        volume = int(np.prod(size))
+        for omit, ignore_inf, min_count in ((False, False, 1), (True, False, 1), (True, True, volume // 2 + 1)):
+            for kind, parameter in (("median_histogram", 0), ("rank_histogram", 0),
+                                    ("rank_histogram", volume // 3), ("rank_histogram", volume - 1)):
+                args = (kind, values, size, None, origin, (mode, mode), -0.0, omit, ignore_inf,
+                        min_count, parameter)
+                expected = _oracle(oracle, kind.replace("_histogram", "") if kind != "median_histogram"
+                                   else "median", *args[1:])
+                _assert_bits(_gpu(*args), expected, (kind, size, origin, mode, omit, ignore_inf))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_every_network_width_and_radix(gpu, oracle, dtype) -> None:
+    """Tap counts around each register-network width (8..128) and beyond it
+    (the radix-select kernel), with footprints."""
+    rng = np.random.default_rng(7)
+    values = _special_values((29, 41), dtype, seed=3)
+    for count in (1, 2, 5, 8, 9, 16, 17, 25, 32, 33, 49, 64, 65, 68, 100, 128, 129, 200, 300):
+        side = int(np.ceil(np.sqrt(count))) + 1
+        flat = np.zeros(side * side, dtype=bool)
+        flat[rng.choice(side * side, size=count, replace=False)] = True
+        footprint = flat.reshape(side, side)
+        for omit, min_count in ((False, 1), (True, max(1, count // 3))):
+            for kind in ("median", "rank", "percentile"):
+                parameter = count // 2 if kind == "rank" else 0
+                args = (kind, values, None, footprint, (0, 0), ("reflect", "wrap"), 1.5, omit, False,
+                        min_count, parameter, 84.0)
+                _assert_bits(_gpu(*args), _oracle(oracle, *args), (count, kind, omit))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_ranks_one_to_five(gpu, oracle, dtype) -> None:
+    cases = [
+        ((150,), (7,), (2,), ("mirror",)),
+        ((1, 90), (4, 7), (1, 0), ("wrap", "nearest")),
+        ((9, 40, 37), (3, 2, 5), (-1, 0, 2), ("mirror", "reflect", "constant")),
+        ((6, 20, 21), (3, 5, 5), (0, 0, 0), ("reflect",) * 3),
+        ((3, 4, 5, 6), (3, 1, 3, 2), (0, 0, 1, 0), ("reflect", "constant", "wrap", "nearest")),
+        ((2, 2, 2, 2, 3), (3, 3, 3, 3, 5), (0,) * 5, ("reflect", "constant", "nearest", "mirror", "wrap")),
+    ]
+    for shape, size, origin, mode in cases:
+        values = _special_values(shape, dtype, seed=len(shape))
+        for kind in ("median", "median_network", "rank", "percentile", "max"):
+            for omit in (False, True):
+                args = (kind, values, size, None, origin, mode, -4.0, omit, False, 1,
+                        int(np.prod(size)) // 4, 16.0)
+                _assert_bits(_gpu(*args), _oracle(oracle, *args), (shape, kind, omit))
+
+
+def _moment_tolerance(actual, expected, dtype, context):
+    """FP32-compensated moments: <= 2 ulp (float32 output) or <= 1e-12
+    relative (float64 output) where the result is a normal number."""
+    np.testing.assert_array_equal(np.isnan(actual), np.isnan(expected), err_msg=str(context))
+    finite = np.isfinite(expected) & (np.abs(expected) > np.finfo(dtype).tiny * 1e6)
+    a = actual[finite].astype(np.float64)
+    e = expected[finite].astype(np.float64)
+    if dtype == np.float32:
+        ulp = np.spacing(np.abs(expected[finite])).astype(np.float64)
+        assert np.all(np.abs(a - e) <= 2 * ulp), context
+    else:
+        rel = np.abs(a - e) / np.abs(e)
+        assert np.all(rel <= 1e-12), (context, float(rel.max(initial=0)))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("mode", MODES)
+def test_moments_fp64_bit_exact_and_fp32c_tolerance(gpu, oracle, dtype, mode) -> None:
+    rng = np.random.default_rng(4)
+    base = (1e4 + rng.normal(size=(33, 47))).astype(dtype)
+    base[rng.random(base.shape) < 0.05] = np.nan
+    specials = _special_values((33, 47), dtype, seed=9)
+    for values, tol_ok in ((base, True), (specials, False)):
+        for size, footprint, origin in (((5, 5), None, (0, 0)), ((3, 7), None, (1, -2)),
+                                        (None, np.array([[0, 1, 0], [1, 1, 1], [0, 1, 0]]), (0, 0))):
+            for kind in ("mean", "var", "std"):
+                for omit, ignore_inf, min_count, ddof in ((False, False, 1, 0), (True, True, 3, 1),
+                                                          (True, False, 1, 1)):
+                    args = (kind, values, size, footprint, origin, (mode, mode), 2.0, omit, ignore_inf,
+                            min_count, ddof)
+                    expected = _oracle(oracle, *args)
+                    exact = _gpu(*args, moments="fp64")
+                    _assert_bits(exact, expected, (kind, size, omit, "fp64"))
+                    fast = _gpu(*args, moments="fp32c")
+                    if tol_ok:
+                        _moment_tolerance(fast, expected, dtype, (kind, size, omit, "fp32c"))
+                    else:
+                        np.testing.assert_array_equal(np.isnan(fast), np.isnan(expected))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_moments_generic_rank4(gpu, oracle, dtype) -> None:
+    values = _special_values((3, 4, 5, 6), dtype, seed=21)
+    for kind in ("mean", "var", "std"):
+        for omit in (False, True):
+            args = (kind, values, (3, 1, 3, 2), None, (0, 0, 1, 0),
+                    ("reflect", "constant", "wrap", "nearest"), -1.0, omit, False, 1, 1)
+            _assert_bits(_gpu(*args, moments="fp64"), _oracle(oracle, *args), (kind, omit))
+
+
+def test_empty_and_degenerate_shapes(gpu, oracle) -> None:
+    for shape in ((0, 3), (2, 0, 3), (2, 3, 0)):
+        for kind in ("median", "mean", "rank"):
+            out = _gpu(kind, np.empty(shape, np.float32), (3,) * len(shape), None, (0,) * len(shape),
+                       ("wrap",) * len(shape), 0.0, False, False, 1)
+            assert out.shape == shape and out.size == 0
+    # Windows much larger than the array (multi-period boundary mapping).
+    values = _special_values((3, 4), np.float64, seed=2)
+    for mode in MODES:
+        for kind in ("median", "percentile", "mean"):
+            args = (kind, values, (9, 11), None, (0, 0), (mode, mode), 3.0, True, False, 1, 0, 84.0)
+            expected = _oracle(oracle, *args)
+            actual = _gpu(*args, moments="fp64") if kind == "mean" else _gpu(*args)
+            _assert_bits(actual, expected, (mode, kind))
+
+
+def test_large_window_medians(gpu, oracle) -> None:
+    """A 65x65 window (histogram / radix paths) on a sky-like image crop."""
+    rng = np.random.default_rng(3)
+    y, x = np.mgrid[0:160, 0:170]
+    sky = 500 + 0.01 * x - 0.005 * y
+    image = (sky + rng.normal(size=sky.shape) * np.sqrt(sky)).astype(np.float32)
+    image[:, 37] = np.nan
+    for kind in ("median", "median_histogram"):
+        for dtype in (np.float32, np.float64):
+            args = (kind, image.astype(dtype), (65, 65), None, (0, 0), ("nearest", "nearest"), 0.0,
+                    True, False, 1)
+            _assert_bits(_gpu(*args), _oracle(oracle, "median", *args[1:]), (kind, dtype))
