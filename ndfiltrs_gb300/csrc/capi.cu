@@ -365,15 +365,23 @@ int choose_algorithm(Plan& p, int smem_limit) {
     return setup_generic(p);
   }
   if (tileable) {
+    // Rectangular 1-D/2-D windows: the sliding rank histogram for the
+    // histogram kinds, and for every order statistic whose window is too
+    // wide for a register network.
     const bool hist_kind = p.r.kind == kMedianHistogram || p.r.kind == kRankHistogram;
-    const bool rank_like = p.r.kind == kMedian || p.r.kind == kMedianNetwork ||
-                           p.r.kind == kRank || hist_kind;
-    if (rank_like && p.footprint.empty() && histogram_supported(p) &&
+    if (p.footprint.empty() && histogram_supported(p) &&
         (hist_kind || network_width_for(p.dtype, p.r.count) == 0)) {
       histogram_configure(p);
-      p.algo = Algo::kHistogram;
       p.smem_bytes = histogram_smem(p);
-      if (p.smem_bytes <= (size_t)smem_limit) return NDF_OK;
+      if (p.smem_bytes <= (size_t)smem_limit) {
+        p.algo = Algo::kHistogram;
+        cudaError_t e = histogram_allocate(p);
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+        }
+        return NDF_OK;
+      }
     }
     size_t smem = tile_select_smem(p, p.tile.t);
     if (smem <= (size_t)smem_limit) {

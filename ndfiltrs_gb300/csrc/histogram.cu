@@ -1,15 +1,538 @@
-// Sliding-window histogram median and rank for rectangular 1-D/2-D windows.
-// (Kernel under construction: plans fall back to the tile kernels.)
+// Sliding rank-histogram median and rank for rectangular 1-D/2-D windows
+// (method="histogram"; also the large-window path of "direct").
+//
+// Replaces order_statistic_into / Geometry::block / Histogram
+// (src/histogram.rs:93-631). As in the reference, each block of outputs
+// ranks its support (the block plus the window halo, through the boundary
+// modes) so that every retained sample gets a unique block-local rank; a
+// window is then a set of ranks, kept as a bit histogram, and a k-th
+// order statistic is the k-th set bit. Results equal direct selection bit
+// for bit: equal keys are interchangeable, so the tie order of the ranks
+// does not matter.
+//
+// GB300 design:
+//  * one thread block per output tile (persistent grid over tiles);
+//  * ranking: a block-level LSD radix sort of the support's keys (8-bit
+//    digits, warp match_any ranking for stability, digits on which every
+//    retained key agrees are skipped) through a per-block scratch slot in
+//    global memory (L2-resident); rank codes are u16 (support <= 65534);
+//  * sliding: each warp owns a strip of output columns and walks it in
+//    boustrophedon order; a vertical step removes one support row segment
+//    (kw codes) and adds another, spread over the 32 lanes with shared-memory
+//    atomics on the warp's private bitset and per-1024-rank group counts; a
+//    selection is two warp scans (groups, then words) and a 5-step select in
+//    the final word.
+#include <algorithm>
+
 #include "common.cuh"
 #include "plan.h"
 
 namespace ndf {
+namespace {
 
-bool histogram_supported(const Plan&) { return false; }
-void histogram_configure(Plan&) {}
-size_t histogram_smem(const Plan&) { return 0; }
-cudaError_t launch_histogram(const Plan&, const void*, void*, cudaStream_t) {
-  return cudaErrorNotSupported;
+constexpr int kHThreads = 512;
+constexpr int kHWarps = kHThreads / 32;
+constexpr uint16_t kOmitted = 0xFFFF;
+constexpr uint16_t kPropagated = 0xFFFE;
+constexpr int kMaxSupport = 65534;
+
+struct HistArgs {
+  Geom3 g;
+  int TW, TH, SW, SH, S;
+  long long tiles_x, tiles;
+  int cols_per_warp;
+  int words, groups;        // per-warp bit histogram: 32-bit words, 1024-rank groups
+  long long slot_bytes;     // scratch bytes per block slot
+  Reduce r;
+};
+
+template <typename K>
+struct Slot {
+  K* keys_a;
+  K* keys_b;
+  uint32_t* pay_a;
+  uint32_t* pay_b;
+  uint16_t* codes;
+};
+
+__host__ __device__ inline long long align16(long long v) { return (v + 15) & ~15ll; }
+
+template <typename K>
+__host__ __device__ inline long long slot_bytes_for(int S) {
+  return 2 * align16((long long)S * sizeof(K)) + 2 * align16((long long)S * 4) + align16((long long)S * 2);
+}
+
+template <typename K>
+__device__ inline Slot<K> slot_at(unsigned char* base, int S) {
+  Slot<K> s;
+  long long off = 0;
+  s.keys_a = reinterpret_cast<K*>(base + off);
+  off += align16((long long)S * sizeof(K));
+  s.keys_b = reinterpret_cast<K*>(base + off);
+  off += align16((long long)S * sizeof(K));
+  s.pay_a = reinterpret_cast<uint32_t*>(base + off);
+  off += align16((long long)S * 4);
+  s.pay_b = reinterpret_cast<uint32_t*>(base + off);
+  off += align16((long long)S * 4);
+  s.codes = reinterpret_cast<uint16_t*>(base + off);
+  return s;
+}
+
+// One stable counting pass over 8-bit digits. `table` holds kHWarps x 256
+// counters, `totals` 256. Each warp owns a contiguous segment and ranks its
+// 32-key chunks in order with match_any, so equal digits keep their order.
+template <typename K, typename Digit>
+__device__ void radix_pass(const K* src_k, const uint32_t* src_p, K* dst_k, uint32_t* dst_p, int S,
+                           unsigned int* table, unsigned int* totals, Digit digit) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kHWarps * 256; i += blockDim.x) table[i] = 0;
+  __syncthreads();
+  const int chunk = (((S + kHWarps - 1) / kHWarps) + 31) & ~31;
+  const int begin = warp * chunk;
+  const int end = min(S, begin + chunk);
+  unsigned int* wt = table + warp * 256;
+  for (int i = begin + lane; i < end; i += 32) atomicAdd(&wt[digit(src_k[i])], 1u);
+  __syncthreads();
+  if (threadIdx.x < 256) {
+    unsigned int sum = 0;
+    for (int w = 0; w < kHWarps; ++w) sum += table[w * 256 + threadIdx.x];
+    totals[threadIdx.x] = sum;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    // Exclusive scan of 256 totals by one warp (8 per lane).
+    unsigned int local[8];
+    unsigned int run = 0;
+    for (int j = 0; j < 8; ++j) {
+      local[j] = run;
+      run += totals[lane * 8 + j];
+    }
+    unsigned int inc = run;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned int t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    unsigned int excl = inc - run;
+    for (int j = 0; j < 8; ++j) totals[lane * 8 + j] = excl + local[j];
+  }
+  __syncthreads();
+  if (threadIdx.x < 256) {
+    unsigned int run = totals[threadIdx.x];
+    for (int w = 0; w < kHWarps; ++w) {
+      unsigned int c = table[w * 256 + threadIdx.x];
+      table[w * 256 + threadIdx.x] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  for (int i0 = begin; i0 < end; i0 += 32) {
+    const int i = i0 + lane;
+    const bool valid = i < end;
+    K key = valid ? src_k[i] : K(0);
+    uint32_t pay = valid ? src_p[i] : 0u;
+    const int d = valid ? (int)digit(key) : 256 + lane;
+    const unsigned int peers = __match_any_sync(0xffffffffu, d);
+    const int before = __popc(peers & ((1u << lane) - 1u));
+    unsigned int pos = 0;
+    if (valid) pos = wt[d] + before;
+    __syncwarp();
+    if (valid && lane == 31 - __clz(peers)) wt[d] += __popc(peers);
+    __syncwarp();
+    if (valid) {
+      dst_k[pos] = key;
+      dst_p[pos] = pay;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int select_in_word32(unsigned int word, int k) {
+  int position = 0;
+#pragma unroll
+  for (int width = 16; width >= 1; width >>= 1) {
+    int low = __popc(word & ((1u << width) - 1u));
+    if (k >= low) {
+      k -= low;
+      word >>= width;
+      position += width;
+    }
+  }
+  return position;
+}
+
+// Rank (0-based position in the block's sorted keys) of the k-th set bit.
+__device__ __forceinline__ int hist_select(const unsigned int* words, const unsigned int* groups,
+                                           int nwords, int ngroups, int k) {
+  const int lane = threadIdx.x & 31;
+  unsigned int g0 = lane < ngroups ? groups[lane] : 0u;
+  unsigned int g1 = lane + 32 < ngroups ? groups[lane + 32] : 0u;
+  unsigned int tot0 = __reduce_add_sync(0xffffffffu, g0);
+  unsigned int v = g0;
+  int base = 0;
+  if ((unsigned int)k >= tot0) {
+    k -= (int)tot0;
+    v = g1;
+    base = 32;
+  }
+  unsigned int s = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned int t = __shfl_up_sync(0xffffffffu, s, o);
+    if (lane >= o) s += t;
+  }
+  int L = max(__ffs(__ballot_sync(0xffffffffu, s > (unsigned int)k)) - 1, 0);
+  k -= (int)__shfl_sync(0xffffffffu, s - v, L);
+  const int g = base + L;
+  const int wi = g * 32 + lane;
+  unsigned int w = wi < nwords ? words[wi] : 0u;
+  unsigned int pc = __popc(w);
+  unsigned int s2 = pc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned int t = __shfl_up_sync(0xffffffffu, s2, o);
+    if (lane >= o) s2 += t;
+  }
+  int L2 = max(__ffs(__ballot_sync(0xffffffffu, s2 > (unsigned int)k)) - 1, 0);
+  k -= (int)__shfl_sync(0xffffffffu, s2 - pc, L2);
+  unsigned int word = __shfl_sync(0xffffffffu, w, L2);
+  return (g * 32 + L2) * 32 + select_in_word32(word, k);
+}
+
+struct WarpHist {
+  unsigned int* words;
+  unsigned int* groups;
+  int count;  // retained samples in the window
+  int nan;    // propagated NaN samples in the window
+};
+
+// Add (sign = +1) or remove (-1) n codes starting at `start` with `stride`.
+// The codes were written earlier in this kernel, so they are read through
+// the coherent path (no const __restrict__ / __ldg).
+__device__ __forceinline__ void face(const uint16_t* codes, int start, int n, int stride,
+                                     int sign, WarpHist& h) {
+  const int lane = threadIdx.x & 31;
+  int kept = 0, nans = 0;
+  for (int i = lane; i < n; i += 32) {
+    const unsigned int c = codes[start + i * stride];
+    if (c < kPropagated) {
+      atomicXor(&h.words[c >> 5], 1u << (c & 31));
+      atomicAdd(&h.groups[c >> 10], (unsigned int)sign);
+      ++kept;
+    } else if (c == kPropagated) {
+      ++nans;
+    }
+  }
+  kept = __reduce_add_sync(0xffffffffu, kept);
+  nans = __reduce_add_sync(0xffffffffu, nans);
+  h.count += sign * kept;
+  h.nan += sign * nans;
+  __syncwarp();
+}
+
+template <typename T>
+__device__ __forceinline__ T hist_finish(const WarpHist& h, const HistArgs& a,
+                                         const typename KeyOf<T>::K* sorted) {
+  using KO = KeyOf<T>;
+  const Reduce& r = a.r;
+  if ((!r.omit && h.nan > 0) || (r.omit && h.count < r.min_count) || h.count == 0) return nan_of(T());
+  auto value_at = [&](int k) {
+    return KO::value(sorted[hist_select(h.words, h.groups, a.words, a.groups, k)]);
+  };
+  switch (r.kind) {
+    case kRank:
+    case kRankHistogram:
+      if (r.param >= h.count) return nan_of(T());
+      return value_at((int)r.param);
+    case kMin:
+      return value_at(0);
+    case kMax:
+      return value_at(h.count - 1);
+    case kPercentile: {
+      if (r.q == 100.0) return value_at(h.count - 1);
+      PercentileRank pr = percentile_rank(r.q, h.count);
+      double lo = (double)value_at((int)pr.lower);
+      double hi = pr.upper == pr.lower ? lo : (double)value_at((int)pr.upper);
+      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+    }
+    default:
+      break;
+  }
+  if (h.count & 1) return value_at(h.count / 2);
+  double lower = (double)value_at(h.count / 2 - 1);
+  double upper = (double)value_at(h.count / 2);
+  return from_f64<T>(midpoint(lower, upper));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kHThreads)
+    histogram_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ HistArgs a,
+                     unsigned char* scratch) {
+  using K = typename KeyOf<T>::K;
+  const K kSent = KeyOf<T>::kSentinel;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ unsigned int totals[256];
+  __shared__ K red_and[kHWarps], red_or[kHWarps];
+  __shared__ int red_sent[kHWarps];
+  const Geom3& g = a.g;
+  const int S = a.S;
+  unsigned int* work = reinterpret_cast<unsigned int*>(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Slot<K> slot = slot_at<K>(scratch + (long long)blockIdx.x * a.slot_bytes, S);
+  const bool drop_inf = a.r.drop_inf;
+  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+
+  for (long long tile = blockIdx.x; tile < a.tiles; tile += gridDim.x) {
+    const long long y0 = (tile / a.tiles_x) * a.TH;
+    const long long x0 = (tile % a.tiles_x) * a.TW;
+    // Gather the support as keys (payload = support index), mapping each
+    // coordinate through the boundary modes.
+    K k_and = kSent, k_or = 0;
+    int sent = 0;
+    for (int e = threadIdx.x; e < S; e += blockDim.x) {
+      const int sy = e / a.SW;
+      const int sx = e - sy * a.SW;
+      long long my, mx;
+      const bool inside = map_index(y0 + sy - g.ay, g.H, g.my, &my) &&
+                          map_index(x0 + sx - g.ax, g.W, g.mx, &mx);
+      const K key = inside ? sample_key<T>(__ldg(in + my * g.W + mx), drop_inf) : outside;
+      slot.keys_a[e] = key;
+      slot.pay_a[e] = (uint32_t)e;
+      if (key != kSent) {
+        k_and &= key;
+        k_or |= key;
+      } else {
+        ++sent;
+      }
+    }
+    for (int o = 16; o >= 1; o >>= 1) {
+      k_and &= __shfl_xor_sync(0xffffffffu, k_and, o);
+      k_or |= __shfl_xor_sync(0xffffffffu, k_or, o);
+      sent += __shfl_xor_sync(0xffffffffu, sent, o);
+    }
+    if (lane == 0) {
+      red_and[warp] = k_and;
+      red_or[warp] = k_or;
+      red_sent[warp] = sent;
+    }
+    __syncthreads();
+    k_and = kSent;
+    k_or = 0;
+    sent = 0;
+    for (int w = 0; w < kHWarps; ++w) {
+      k_and &= red_and[w];
+      k_or |= red_or[w];
+      sent += red_sent[w];
+    }
+    // Sort keys (LSD, 8-bit digits over the varying bits, then sentinels last).
+    K* src_k = slot.keys_a;
+    K* dst_k = slot.keys_b;
+    uint32_t* src_p = slot.pay_a;
+    uint32_t* dst_p = slot.pay_b;
+    const K varying = sent == S ? K(0) : (k_and ^ k_or);
+    if (varying != 0) {
+      const int bits = (int)sizeof(K) * 8;
+      const int lo = sizeof(K) == 8 ? __ffsll((long long)varying) - 1 : __ffs((int)varying) - 1;
+      const int hi = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)varying) : __clz((int)varying));
+      for (int shift = lo; shift <= hi; shift += 8) {
+        radix_pass(src_k, src_p, dst_k, dst_p, S, work, totals,
+                   [shift](K key) { return (unsigned int)((key >> shift) & 0xFFu); });
+        K* tk = src_k;
+        src_k = dst_k;
+        dst_k = tk;
+        uint32_t* tp = src_p;
+        src_p = dst_p;
+        dst_p = tp;
+      }
+    }
+    if (sent > 0 && sent < S) {
+      radix_pass(src_k, src_p, dst_k, dst_p, S, work, totals,
+                 [kSent](K key) { return key == kSent ? 1u : 0u; });
+      K* tk = src_k;
+      src_k = dst_k;
+      dst_k = tk;
+      uint32_t* tp = src_p;
+      src_p = dst_p;
+      dst_p = tp;
+    }
+    const uint16_t dropped = a.r.omit ? kOmitted : kPropagated;
+    for (int pos = threadIdx.x; pos < S; pos += blockDim.x) {
+      const K key = src_k[pos];
+      slot.codes[src_p[pos]] = key == kSent ? dropped : (uint16_t)pos;
+    }
+    __syncthreads();
+
+    // Slide: each warp walks its columns in boustrophedon order.
+    const int th_eff = (int)min((long long)a.TH, g.H - y0);
+    const int tw_eff = (int)min((long long)a.TW, g.W - x0);
+    const int c_begin = warp * a.cols_per_warp;
+    const int c_end = min(tw_eff, c_begin + a.cols_per_warp);
+    WarpHist h;
+    h.words = work + warp * (a.words + a.groups);
+    h.groups = h.words + a.words;
+    h.count = 0;
+    h.nan = 0;
+    for (int i = lane; i < a.words + a.groups; i += 32) h.words[i] = 0u;
+    __syncwarp();
+    const uint16_t* codes = slot.codes;
+    const int kh = g.kh, kw = g.kw, SW = a.SW;
+    if (c_begin < c_end) {
+      for (int ky = 0; ky < kh; ++ky) face(codes, ky * SW + c_begin, kw, 1, +1, h);
+      int row = 0;
+      int dir = 1;
+      for (int c = c_begin; c < c_end; ++c) {
+        for (int step = 0; step < th_eff; ++step) {
+          T result = hist_finish<T>(h, a, src_k);
+          if (lane == 0) out[(y0 + row) * g.W + x0 + c] = canonical(result);
+          if (step + 1 < th_eff) {
+            if (dir > 0) {
+              face(codes, row * SW + c, kw, 1, -1, h);
+              face(codes, (row + kh) * SW + c, kw, 1, +1, h);
+              ++row;
+            } else {
+              face(codes, (row + kh - 1) * SW + c, kw, 1, -1, h);
+              face(codes, (row - 1) * SW + c, kw, 1, +1, h);
+              --row;
+            }
+          }
+        }
+        if (c + 1 < c_end) {
+          face(codes, row * SW + c, kh, SW, -1, h);
+          face(codes, row * SW + c + kw, kh, SW, +1, h);
+        }
+        dir = -dir;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+struct HistChoice {
+  int TW = 0, TH = 0;
+};
+
+HistChoice choose_tile(const Geom3& g) {
+  HistChoice c;
+  if (g.kd != 1 || g.D != 1) return c;
+  if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport) return c;
+  if (g.H == 1 && g.kh == 1) {
+    for (int tw : {4096, 2048, 1024, 512, 256, 128, 64, 32, 16}) {
+      if (tw + g.kw - 1 <= kMaxSupport && (tw <= 16 || tw / 2 < g.W)) {
+        c.TW = tw;
+        c.TH = 1;
+        return c;
+      }
+    }
+    return c;
+  }
+  int tw = g.W >= 64 ? 64 : (int)(((g.W + 15) / 16) * 16);
+  for (int th : {256, 128, 64, 32, 16, 8, 4, 2, 1}) {
+    if (th > 1 && th / 2 >= g.H) continue;
+    long long s = (long long)(tw + g.kw - 1) * (th + g.kh - 1);
+    if (s <= kMaxSupport) {
+      c.TW = tw;
+      c.TH = th;
+      return c;
+    }
+  }
+  for (int w : {32, 16}) {
+    if (w >= tw) continue;
+    long long s = (long long)(w + g.kw - 1) * g.kh;
+    if (s <= kMaxSupport) {
+      c.TW = w;
+      c.TH = 1;
+      return c;
+    }
+  }
+  return c;
+}
+
+HistArgs make_args(const Plan& p) {
+  HistArgs a{};
+  a.g = p.tile.g;
+  a.TW = p.hist_block_w;
+  a.TH = p.hist_block_h;
+  a.SW = a.TW + a.g.kw - 1;
+  a.SH = a.TH + a.g.kh - 1;
+  a.S = a.SW * a.SH;
+  a.tiles_x = (a.g.W + a.TW - 1) / a.TW;
+  a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
+  a.cols_per_warp = (a.TW + kHWarps - 1) / kHWarps;
+  a.words = (a.S + 31) / 32;
+  a.groups = (a.S + 1023) / 1024;
+  a.slot_bytes = p.dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
+  a.r = p.r;
+  return a;
+}
+
+size_t smem_for(const HistArgs& a) {
+  size_t sort = (size_t)kHWarps * 256 * 4;
+  size_t hist = (size_t)kHWarps * (a.words + a.groups) * 4;
+  return std::max(sort, hist);
+}
+
+template <typename T>
+cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  HistArgs a = make_args(p);
+  auto kernel = histogram_kernel<T>;
+  cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+  if (e != cudaSuccess) return e;
+  long long slots = (long long)(p.scratch_bytes / (size_t)a.slot_bytes);
+  long long grid = std::min<long long>(a.tiles, slots);
+  if (grid < 1) return cudaErrorInvalidValue;
+  kernel<<<(unsigned)grid, kHThreads, p.smem_bytes, s>>>(in, out, a, (unsigned char*)p.d_scratch);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool histogram_supported(const Plan& p) {
+  if (p.ndim > 2 || !p.footprint.empty()) return false;
+  const int k = p.r.kind;
+  if (k != kMedian && k != kMedianNetwork && k != kMedianHistogram && k != kRank &&
+      k != kRankHistogram && k != kMin && k != kMax && k != kPercentile)
+    return false;
+  HistChoice c = choose_tile(p.tile.g);
+  return c.TW > 0;
+}
+
+void histogram_configure(Plan& p) {
+  HistChoice c = choose_tile(p.tile.g);
+  p.hist_block_w = c.TW;
+  p.hist_block_h = c.TH;
+  HistArgs a = make_args(p);
+  p.hist_blocks_x = a.tiles_x;
+  p.hist_blocks_y = a.tiles / a.tiles_x;
+}
+
+size_t histogram_smem(const Plan& p) { return smem_for(make_args(p)); }
+
+// Scratch slots: one per resident block (occupancy x SMs), capped by the
+// number of tiles.
+cudaError_t histogram_allocate(Plan& p) {
+  HistArgs a = make_args(p);
+  int per_sm = 1;
+  cudaError_t e;
+  if (p.dtype == 0) {
+    cudaFuncSetAttribute(histogram_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)p.smem_bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, histogram_kernel<float>, kHThreads,
+                                                      p.smem_bytes);
+  } else {
+    cudaFuncSetAttribute(histogram_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)p.smem_bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, histogram_kernel<double>, kHThreads,
+                                                      p.smem_bytes);
+  }
+  if (e != cudaSuccess) return e;
+  long long slots = std::min<long long>(a.tiles, (long long)std::max(per_sm, 1) * p.sm_count);
+  p.scratch_bytes = (size_t)slots * (size_t)a.slot_bytes;
+  return cudaMalloc(&p.d_scratch, p.scratch_bytes);
+}
+
+cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  if (p.dtype == 0) return launch_t<float>(p, (const float*)in, (float*)out, s);
+  return launch_t<double>(p, (const double*)in, (double*)out, s);
 }
 
 }  // namespace ndf

@@ -123,6 +123,7 @@ size_t tile_moments_smem(const Plan& p, const Tile& t);
 size_t histogram_smem(const Plan& p);
 bool histogram_supported(const Plan& p);
 void histogram_configure(Plan& p);
+cudaError_t histogram_allocate(Plan& p);
 int network_width_for(int dtype, int count);
 
 }  // namespace ndf

@@ -39,6 +39,8 @@ def _gpu(kind, array, size, footprint, origin, mode, cval, omit, ignore_inf, min
          moments=None):
     from ndfiltrs_gb300 import _core
 
+    if footprint is not None:
+        size = list(np.asarray(footprint).shape)
     if kind == "percentile":
         return _core.robust_filter(array, size, footprint, origin, mode, cval, "percentile", q, omit,
                                    ignore_inf if omit else False, min_count if omit else 1,
