@@ -1,0 +1,138 @@
+// Box-window pair kernel (see tile_box_kernel): 3x3, 5x5 and 7x7 windows in
+// 2-D arrays, two vertically adjacent outputs per thread sharing the sort of
+// their common rows.
+#include "network.cuh"
+
+namespace ndf {
+namespace {
+using namespace net;
+
+// ---------------------------------------------------------------------------
+// Box windows (KH x KW, compile-time) in 2-D: each thread computes vertically
+// adjacent output pairs. The two windows share KH - 1 rows: those keys are
+// sorted once, each private row is sorted separately, and each output merges
+// the shared sorted run with its private run (the last Batcher level). With a
+// fixed tile width every tap offset is a compile-time shared-memory
+// immediate.
+constexpr int kBoxTW = 32;
+constexpr int kBoxPairs = 2;  // pairs per thread: tile height 16 * kBoxPairs
+
+template <typename T, int KH, int KW, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    tile_box_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a) {
+  using K = typename KeyOf<T>::K;
+  constexpr K kSent = KeyOf<T>::kSentinel;
+  constexpr int SW = kBoxTW + KW - 1;
+  constexpr int SHARED = (KH - 1) * KW;
+  constexpr int P = pow2_at_least(SHARED > KW ? SHARED : KW);
+  constexpr int V = KH * KW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
+  long long z, y0, x0;
+  tile_coords(a, z, y0, x0);
+  build_maps(maps, g, t, z, y0, x0);
+  __syncthreads();
+  const bool drop_inf = a.r.drop_inf;
+  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  __syncthreads();
+
+  const int tx = threadIdx.x % kBoxTW;
+  const int tr = threadIdx.x / kBoxTW;
+  const long long x = x0 + tx;
+  if (x >= g.W) return;
+#pragma unroll 1
+  for (int pair = 0; pair < kBoxPairs; ++pair) {
+    const int row0 = 2 * (tr + (kThreads / kBoxTW) * pair);
+    const long long y = y0 + row0;
+    if (y >= g.H) break;
+    const K* base = s + row0 * SW + tx;
+    K sh[P], pa[P], pb[P];
+    int n_sh = 0, n_a = 0, n_b = 0;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      sh[i] = i < SHARED ? base[(1 + i / KW) * SW + i % KW] : kSent;
+      pa[i] = i < KW ? base[i] : kSent;
+      pb[i] = i < KW ? base[KH * SW + i] : kSent;
+      n_sh += (i < SHARED && sh[i] != kSent) ? 1 : 0;
+      n_a += (i < KW && pa[i] != kSent) ? 1 : 0;
+      n_b += (i < KW && pb[i] != kSent) ? 1 : 0;
+    }
+    batcher_sort<P>(sh);
+    batcher_sort<P>(pa);
+    batcher_sort<P>(pb);
+    {
+      K m[2 * P];
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        m[i] = sh[i];
+        m[P + i] = pa[i];
+      }
+      batcher_merge<2 * P>(m);
+      out[(z * g.H + y) * g.W + x] = canonical(network_finish<T, 2 * P, V, MODE>(m, n_sh + n_a, a.r));
+    }
+    if (y + 1 < g.H) {
+      K m[2 * P];
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        m[i] = sh[i];
+        m[P + i] = pb[i];
+      }
+      batcher_merge<2 * P>(m);
+      out[(z * g.H + y + 1) * g.W + x] = canonical(network_finish<T, 2 * P, V, MODE>(m, n_sh + n_b, a.r));
+    }
+  }
+}
+
+template <typename T, int KH, int KW>
+cudaError_t launch_box(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork;
+  auto kernel = median ? tile_box_kernel<T, KH, KW, 1> : tile_box_kernel<T, KH, KW, 0>;
+  cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+  if (e != cudaSuccess) return e;
+  kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool box_supported(int dtype, int kh, int kw) {
+  if (kh == 3 && kw == 3) return true;
+  if (kh == 5 && kw == 5) return true;
+  return dtype == 0 && kh == 7 && kw == 7;
+}
+
+Tile box_tile(const Geom3& g) {
+  Tile t{};
+  t.TW = kBoxTW;
+  t.TH = 16 * kBoxPairs;
+  t.SW = t.TW + g.kw - 1;
+  t.SH = t.TH + g.kh - 1;
+  t.tiles_x = (g.W + t.TW - 1) / t.TW;
+  t.tiles_y = (g.H + t.TH - 1) / t.TH;
+  t.tiles = t.tiles_x * t.tiles_y * g.D;
+  return t;
+}
+
+cudaError_t launch_tile_box(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  const int kh = p.tile.g.kh, kw = p.tile.g.kw;
+  if (p.dtype == 0) {
+    const float* i = (const float*)in;
+    float* o = (float*)out;
+    if (kh == 3 && kw == 3) return launch_box<float, 3, 3>(p, i, o, s);
+    if (kh == 5 && kw == 5) return launch_box<float, 5, 5>(p, i, o, s);
+    if (kh == 7 && kw == 7) return launch_box<float, 7, 7>(p, i, o, s);
+  } else {
+    const double* i = (const double*)in;
+    double* o = (double*)out;
+    if (kh == 3 && kw == 3) return launch_box<double, 3, 3>(p, i, o, s);
+    if (kh == 5 && kw == 5) return launch_box<double, 5, 5>(p, i, o, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ndf

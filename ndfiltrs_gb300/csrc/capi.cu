@@ -39,6 +39,8 @@ const char* algo_name(Algo a) {
       return "empty";
     case Algo::kTileNetwork:
       return "tile_network";
+    case Algo::kTileBox:
+      return "tile_box";
     case Algo::kTileRadix:
       return "tile_radix";
     case Algo::kGenericSelect:
@@ -311,6 +313,7 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
   r.min_count = r.omit ? (long long)d->min_count : 1;
   r.param = (long long)std::min<uint64_t>(d->parameter, (uint64_t)std::numeric_limits<long long>::max());
   r.q = d->percentile;
+  r.q_fraction = d->percentile / 100.0;
   r.cval = d->dtype == NDF_FLOAT32 ? (double)(float)d->cval : d->cval;
   r.moments = d->moments == NDF_MOMENTS_FP64 ? 1 : 0;
   if (kind == kPercentile) {
@@ -383,6 +386,18 @@ int choose_algorithm(Plan& p, int smem_limit) {
         return NDF_OK;
       }
     }
+    // Box windows with a compiled pair kernel (2-D, 3x3 / 5x5 / 7x7).
+    if (p.footprint.empty() && p.tile.g.kd == 1 && p.tile.g.H > 1 && !hist_kind &&
+        box_supported(p.dtype, p.tile.g.kh, p.tile.g.kw)) {
+      Tile bt = box_tile(p.tile.g);
+      size_t smem = tile_select_smem(p, bt);
+      if (smem <= (size_t)smem_limit) {
+        p.tile.t = bt;
+        p.smem_bytes = smem;
+        p.algo = Algo::kTileBox;
+        return NDF_OK;
+      }
+    }
     size_t smem = tile_select_smem(p, p.tile.t);
     if (smem <= (size_t)smem_limit) {
       int width = network_width_for(p.dtype, p.r.count);
@@ -406,6 +421,7 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
     case Algo::kEmpty:
       return NDF_OK;
     case Algo::kTileNetwork:
+    case Algo::kTileBox:
     case Algo::kTileRadix:
       e = launch_tile_select(p, in, out, s);
       break;

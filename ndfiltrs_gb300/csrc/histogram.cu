@@ -249,7 +249,7 @@ __device__ __forceinline__ T hist_finish(const WarpHist& h, const HistArgs& a,
       return value_at(h.count - 1);
     case kPercentile: {
       if (r.q == 100.0) return value_at(h.count - 1);
-      PercentileRank pr = percentile_rank(r.q, h.count);
+      PercentileRank pr = percentile_rank(r.q_fraction, h.count);
       double lo = (double)value_at((int)pr.lower);
       double hi = pr.upper == pr.lower ? lo : (double)value_at((int)pr.upper);
       return from_f64<T>(interpolate(lo, hi, pr.fraction));

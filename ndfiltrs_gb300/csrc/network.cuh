@@ -1,0 +1,164 @@
+// Register sorting networks and their epilogues, shared by the tile
+// selection kernels (select.cu, box.cu).
+#pragma once
+
+#include <utility>
+
+#include "common.cuh"
+#include "plan.h"
+#include "staging.cuh"
+
+namespace ndf {
+namespace net {
+
+constexpr int kThreads = 256;
+
+template <int N>
+struct TapTable {
+  int32_t off[N];
+};
+
+template <typename K>
+__device__ __forceinline__ void cmpx(K& a, K& b) {
+  K lo = a < b ? a : b;
+  K hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
+// Batcher odd-even merge sort over N (a power of two) wires, generated at
+// compile time as a comparator table and applied by a fold expression, so
+// every wire index is a constant expression and the keys stay in registers.
+template <int N, int PSTART = 1>
+struct Batcher {
+  static constexpr bool same_block(int lo, int hi, int p) { return lo / (2 * p) == hi / (2 * p); }
+  static constexpr int count() {
+    int c = 0;
+    for (int p = PSTART; p < N; p <<= 1)
+      for (int k = p; k >= 1; k >>= 1)
+        for (int j = k % p; j + k < N; j += 2 * k)
+          for (int i = 0; i < k && i + j + k < N; ++i)
+            if (same_block(i + j, i + j + k, p)) ++c;
+    return c;
+  }
+  static constexpr int kCount = count();
+  struct Table {
+    short lo[kCount];
+    short hi[kCount];
+  };
+  static constexpr Table table() {
+    Table t{};
+    int c = 0;
+    for (int p = PSTART; p < N; p <<= 1)
+      for (int k = p; k >= 1; k >>= 1)
+        for (int j = k % p; j + k < N; j += 2 * k)
+          for (int i = 0; i < k && i + j + k < N; ++i)
+            if (same_block(i + j, i + j + k, p)) {
+              t.lo[c] = (short)(i + j);
+              t.hi[c] = (short)(i + j + k);
+              ++c;
+            }
+    return t;
+  }
+  static constexpr Table kTable = table();
+};
+
+template <int N, int PSTART, int I, typename K>
+__device__ __forceinline__ void cmpx_at(K (&a)[N]) {
+  constexpr int lo = Batcher<N, PSTART>::kTable.lo[I];
+  constexpr int hi = Batcher<N, PSTART>::kTable.hi[I];
+  cmpx(a[lo], a[hi]);
+}
+
+template <int N, int PSTART, typename K, int... Is>
+__device__ __forceinline__ void apply_network(K (&a)[N], std::integer_sequence<int, Is...>) {
+  (cmpx_at<N, PSTART, Is>(a), ...);
+}
+
+template <int N, typename K>
+__device__ __forceinline__ void batcher_sort(K (&a)[N]) {
+  apply_network<N, 1>(a, std::make_integer_sequence<int, Batcher<N, 1>::kCount>{});
+}
+
+// Merge of two sorted halves a[0, N/2) and a[N/2, N): the last level of the
+// Batcher network.
+template <int N, typename K>
+__device__ __forceinline__ void batcher_merge(K (&a)[N]) {
+  apply_network<N, N / 2>(a, std::make_integer_sequence<int, Batcher<N, N / 2>::kCount>{});
+}
+
+constexpr int pow2_at_least(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+// Register pick a[idx] for a runtime idx < BOUND.
+template <int BOUND, int N, typename K>
+__device__ __forceinline__ K pick(const K (&a)[N], int idx) {
+  K v = a[0];
+#pragma unroll
+  for (int i = 1; i < BOUND; ++i) v = (i == idx) ? a[i] : v;
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T median_of_two(T lower, T upper) {
+  return from_f64<T>(midpoint((double)lower, (double)upper));
+}
+
+// Epilogue of the register network: the statistic from sorted keys.
+// MODE 0: any selection kind, runtime policy. MODE 1: median kinds only.
+template <typename T, int N, int VFIX, int MODE, typename K>
+__device__ __forceinline__ T network_finish(const K (&k)[N], int nv, const Reduce& r) {
+  using KO = KeyOf<T>;
+  const int V = VFIX > 0 ? VFIX : r.count;
+  const bool missing = r.omit ? (nv < r.min_count) : (nv != V);
+  if (missing || nv == 0) return nan_of(T());
+  if (MODE == 1) {
+    if (VFIX > 0 && !r.omit) {
+      // Propagate with a fixed tap count: compile-time ranks.
+      if (VFIX & 1) return KO::value(k[VFIX / 2]);
+      return median_of_two(KO::value(k[VFIX / 2 - 1]), KO::value(k[VFIX / 2]));
+    }
+    constexpr int B = (VFIX > 0 ? VFIX : N) / 2 + 1;
+    if (nv & 1) return KO::value(pick<B>(k, nv / 2));
+    return median_of_two(KO::value(pick<B>(k, nv / 2 - 1)), KO::value(pick<B>(k, nv / 2)));
+  }
+  constexpr int A = (VFIX > 0 && VFIX < N) ? VFIX : N;
+  switch (r.kind) {
+    case kMin:
+      return KO::value(k[0]);
+    case kMax:
+      return KO::value(pick<A>(k, nv - 1));
+    case kRank:
+    case kRankHistogram:
+      if (r.param >= nv) return nan_of(T());
+      return KO::value(pick<A>(k, (int)r.param));
+    case kPercentile: {
+      if (r.q == 100.0) return KO::value(pick<A>(k, nv - 1));
+      PercentileRank pr = percentile_rank(r.q_fraction, nv);
+      double lo = (double)KO::value(pick<A>(k, (int)pr.lower));
+      double hi = (double)KO::value(pick<A>(k, (int)pr.upper));
+      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+    }
+    default:
+      if (nv & 1) return KO::value(pick<A>(k, nv / 2));
+      return median_of_two(KO::value(pick<A>(k, nv / 2 - 1)), KO::value(pick<A>(k, nv / 2)));
+  }
+}
+
+__device__ __forceinline__ void tile_coords(const TileArgs& a, long long& z, long long& y0,
+                                            long long& x0) {
+  long long tile = blockIdx.x;
+  long long tx = tile % a.t.tiles_x;
+  long long rest = tile / a.t.tiles_x;
+  long long ty = rest % a.t.tiles_y;
+  z = rest / a.t.tiles_y;
+  y0 = ty * a.t.TH;
+  x0 = tx * a.t.TW;
+}
+
+
+}  // namespace net
+}  // namespace ndf

@@ -31,6 +31,7 @@ struct Reduce {
   long long min_count; // Omit { min_count }
   long long param;     // rank or ddof
   double q;            // percentile
+  double q_fraction;   // q / 100.0 (src/robust.rs:348 computes it the same way)
   double cval;         // constant boundary value, already cast to the dtype
   int moments;         // NDF_MOMENTS_* for mean/var/std
 };
@@ -62,6 +63,7 @@ struct GenericArgs {
 enum class Algo {
   kEmpty,
   kTileNetwork,
+  kTileBox,
   kTileRadix,
   kGenericSelect,
   kHistogram,
@@ -112,6 +114,7 @@ const char* algo_name(Algo a);
 
 // Launchers (one per translation unit). Return a cudaError_t.
 cudaError_t launch_tile_select(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_tile_box(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_generic_select(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_tile_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_generic_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
@@ -125,5 +128,7 @@ bool histogram_supported(const Plan& p);
 void histogram_configure(Plan& p);
 cudaError_t histogram_allocate(Plan& p);
 int network_width_for(int dtype, int count);
+bool box_supported(int dtype, int kh, int kw);
+Tile box_tile(const Geom3& g);
 
 }  // namespace ndf

@@ -214,3 +214,27 @@ def test_large_window_medians(gpu, oracle) -> None:
             args = (kind, image.astype(dtype), (65, 65), None, (0, 0), ("nearest", "nearest"), 0.0,
                     True, False, 1)
             _assert_bits(_gpu(*args), _oracle(oracle, "median", *args[1:]), (kind, dtype))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("box", [3, 5, 7])
+def test_box_pair_kernel(gpu, oracle, dtype, box) -> None:
+    """3x3 / 5x5 / 7x7 windows (the vertical-pair box kernel) over partial
+    tiles, every mode, shifted origins, all policies and selection kinds."""
+    from ndfiltrs_gb300 import _core
+
+    values = _special_values((45, 70), dtype, seed=box)
+    volume = box * box
+    for mode in MODES:
+        for origin in ((0, 0), (box // 2, -(box // 2)), (-1, 1)):
+            for omit, ignore_inf, min_count in ((False, False, 1), (True, False, 1), (True, True, volume // 2)):
+                for kind, parameter, q in (("median", 0, 50.0), ("median_network", 0, 50.0),
+                                           ("rank", 2, 50.0), ("rank", volume - 1, 50.0),
+                                           ("min", 0, 50.0), ("max", 0, 50.0), ("percentile", 0, 84.0)):
+                    args = (kind, values, (box, box), None, origin, (mode, mode), 0.25, omit, ignore_inf,
+                            min_count, parameter, q)
+                    _assert_bits(_gpu(*args), _oracle(oracle, *args), (box, mode, origin, omit, kind))
+    plan = _core.Plan(values.shape, dtype, "median", (box, box), omit_nan=True)
+    if dtype == np.float32 or box < 7:
+        assert plan.algorithm == "tile_box"
+    plan.close()
