@@ -175,6 +175,26 @@ __device__ __forceinline__ double midpoint(double lower, double upper) {
   return __dmul_rn(__dadd_rn(lower, upper), 0.5);
 }
 
+// The same midpoint for two float32 values, cast once to float32. When
+// both values are zero or normal with biased exponents in [30, 253] and
+// their exponents differ by at most 28, the float64 computation above is
+// exact ((a + b) / 2 needs at most 53 significant bits), so the result is
+// the float32 rounding of (a + b) / 2. In that range RN32(a + b) * 0.5 is
+// that rounding too: halving a normal float is exact and commutes with
+// rounding. Everything else takes the float64 path.
+__device__ __forceinline__ float midpoint_f32(float lower, float upper) {
+  const unsigned int bl = __float_as_uint(lower), bu = __float_as_uint(upper);
+  const int el = (int)((bl >> 23) & 0xFF), eu = (int)((bu >> 23) & 0xFF);
+  const bool zl = (bl << 1) == 0u, zu = (bu << 1) == 0u;
+  const bool nl = el >= 30 && el <= 253, nu = eu >= 30 && eu <= 253;
+  const int diff = el > eu ? el - eu : eu - el;
+  if ((zl || nl) && (zu || nu) && (zl || zu || diff <= 28)) {
+    if (bl == bu) return lower;
+    return __fmul_rn(__fadd_rn(lower, upper), 0.5f);
+  }
+  return __double2float_rn(midpoint((double)lower, (double)upper));
+}
+
 // Neumaier float64 sum, src/mean.rs:7-26.
 struct Sum64 {
   double value = 0.0, correction = 0.0;

@@ -52,14 +52,13 @@ struct Slot {
   K* keys_b;
   uint32_t* pay_a;
   uint32_t* pay_b;
-  uint16_t* codes;
 };
 
 __host__ __device__ inline long long align16(long long v) { return (v + 15) & ~15ll; }
 
 template <typename K>
 __host__ __device__ inline long long slot_bytes_for(int S) {
-  return 2 * align16((long long)S * sizeof(K)) + 2 * align16((long long)S * 4) + align16((long long)S * 2);
+  return 2 * align16((long long)S * sizeof(K)) + 2 * align16((long long)S * 4);
 }
 
 template <typename K>
@@ -73,14 +72,16 @@ __device__ inline Slot<K> slot_at(unsigned char* base, int S) {
   s.pay_a = reinterpret_cast<uint32_t*>(base + off);
   off += align16((long long)S * 4);
   s.pay_b = reinterpret_cast<uint32_t*>(base + off);
-  off += align16((long long)S * 4);
-  s.codes = reinterpret_cast<uint16_t*>(base + off);
   return s;
 }
 
 // One stable counting pass over 8-bit digits. `table` holds kHWarps x 256
 // counters, `totals` 256. Each warp owns a contiguous segment and ranks its
 // 32-key chunks in order with match_any, so equal digits keep their order.
+// Loads are batched (kBatch keys per lane in registers) so a pass costs one
+// memory round trip per batch rather than one per chunk.
+constexpr int kBatch = 16;
+
 template <typename K, typename Digit>
 __device__ void radix_pass(const K* src_k, const uint32_t* src_p, K* dst_k, uint32_t* dst_p, int S,
                            unsigned int* table, unsigned int* totals, Digit digit) {
@@ -91,7 +92,17 @@ __device__ void radix_pass(const K* src_k, const uint32_t* src_p, K* dst_k, uint
   const int begin = warp * chunk;
   const int end = min(S, begin + chunk);
   unsigned int* wt = table + warp * 256;
-  for (int i = begin + lane; i < end; i += 32) atomicAdd(&wt[digit(src_k[i])], 1u);
+  for (int b = begin; b < end; b += 32 * kBatch) {
+    K keys[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int i = b + j * 32 + lane;
+      keys[j] = i < end ? src_k[i] : K(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j)
+      if (b + j * 32 + lane < end) atomicAdd(&wt[digit(keys[j])], 1u);
+  }
   __syncthreads();
   if (threadIdx.x < 256) {
     unsigned int sum = 0;
@@ -125,22 +136,30 @@ __device__ void radix_pass(const K* src_k, const uint32_t* src_p, K* dst_k, uint
     }
   }
   __syncthreads();
-  for (int i0 = begin; i0 < end; i0 += 32) {
-    const int i = i0 + lane;
-    const bool valid = i < end;
-    K key = valid ? src_k[i] : K(0);
-    uint32_t pay = valid ? src_p[i] : 0u;
-    const int d = valid ? (int)digit(key) : 256 + lane;
-    const unsigned int peers = __match_any_sync(0xffffffffu, d);
-    const int before = __popc(peers & ((1u << lane) - 1u));
-    unsigned int pos = 0;
-    if (valid) pos = wt[d] + before;
-    __syncwarp();
-    if (valid && lane == 31 - __clz(peers)) wt[d] += __popc(peers);
-    __syncwarp();
-    if (valid) {
-      dst_k[pos] = key;
-      dst_p[pos] = pay;
+  for (int b = begin; b < end; b += 32 * kBatch) {
+    K keys[kBatch];
+    uint32_t pays[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int i = b + j * 32 + lane;
+      keys[j] = i < end ? src_k[i] : K(0);
+      pays[j] = i < end ? src_p[i] : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const bool valid = b + j * 32 + lane < end;
+      const int d = valid ? (int)digit(keys[j]) : 256 + lane;
+      const unsigned int peers = __match_any_sync(0xffffffffu, d);
+      const int before = __popc(peers & ((1u << lane) - 1u));
+      unsigned int pos = 0;
+      if (valid) pos = wt[d] + before;
+      __syncwarp();
+      if (valid && lane == 31 - __clz(peers)) wt[d] += __popc(peers);
+      __syncwarp();
+      if (valid) {
+        dst_k[pos] = keys[j];
+        dst_p[pos] = pays[j];
+      }
     }
   }
   __syncthreads();
@@ -205,27 +224,52 @@ struct WarpHist {
   int nan;    // propagated NaN samples in the window
 };
 
-// Add (sign = +1) or remove (-1) n codes starting at `start` with `stride`.
-// The codes were written earlier in this kernel, so they are read through
-// the coherent path (no const __restrict__ / __ldg).
-__device__ __forceinline__ void face(const uint16_t* codes, int start, int n, int stride,
-                                     int sign, WarpHist& h) {
+// Apply one step: remove the codes of one face and add those of another
+// (n codes each, `stride` apart, in shared memory). All loads are issued
+// before the atomics.
+__device__ __forceinline__ void update(const uint16_t* codes, unsigned int* words, unsigned int* groups,
+                                       int c, int sign, int& kept, int& nans) {
+  if (c < kPropagated) {
+    atomicXor(&words[c >> 5], 1u << (c & 31));
+    atomicAdd(&groups[c >> 10], (unsigned int)sign);
+    kept += sign;
+  } else if (c == kPropagated) {
+    nans += sign;
+  }
+}
+
+__device__ __forceinline__ void step(const uint16_t* codes, int remove_start, int add_start, int n,
+                                     int stride, WarpHist& h) {
   const int lane = threadIdx.x & 31;
   int kept = 0, nans = 0;
-  for (int i = lane; i < n; i += 32) {
-    const unsigned int c = codes[start + i * stride];
-    if (c < kPropagated) {
-      atomicXor(&h.words[c >> 5], 1u << (c & 31));
-      atomicAdd(&h.groups[c >> 10], (unsigned int)sign);
-      ++kept;
-    } else if (c == kPropagated) {
-      ++nans;
+  for (int i0 = 0; i0 < n; i0 += 128) {
+    int rc[4], ac[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = i0 + j * 32 + lane;
+      rc[j] = i < n ? (int)codes[remove_start + i * stride] : (int)kOmitted;
+      ac[j] = i < n ? (int)codes[add_start + i * stride] : (int)kOmitted;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      update(codes, h.words, h.groups, rc[j], -1, kept, nans);
+      update(codes, h.words, h.groups, ac[j], +1, kept, nans);
     }
   }
-  kept = __reduce_add_sync(0xffffffffu, kept);
-  nans = __reduce_add_sync(0xffffffffu, nans);
-  h.count += sign * kept;
-  h.nan += sign * nans;
+  h.count += __reduce_add_sync(0xffffffffu, kept);
+  h.nan += __reduce_add_sync(0xffffffffu, nans);
+  __syncwarp();
+}
+
+// Add every code of a kh x kw box (the first window of a warp's walk).
+__device__ __forceinline__ void add_box(const uint16_t* codes, int start, int kh, int kw, int SW,
+                                       WarpHist& h) {
+  const int lane = threadIdx.x & 31;
+  int kept = 0, nans = 0;
+  for (int ky = 0; ky < kh; ++ky)
+    for (int i = lane; i < kw; i += 32) update(codes, h.words, h.groups, codes[start + ky * SW + i], +1, kept, nans);
+  h.count += __reduce_add_sync(0xffffffffu, kept);
+  h.nan += __reduce_add_sync(0xffffffffu, nans);
   __syncwarp();
 }
 
@@ -258,12 +302,16 @@ __device__ __forceinline__ T hist_finish(const WarpHist& h, const HistArgs& a,
       break;
   }
   if (h.count & 1) return value_at(h.count / 2);
-  double lower = (double)value_at(h.count / 2 - 1);
-  double upper = (double)value_at(h.count / 2);
-  return from_f64<T>(midpoint(lower, upper));
+  const int lo = hist_select(h.words, h.groups, a.words, a.groups, h.count / 2 - 1);
+  const int hi = hist_select(h.words, h.groups, a.words, a.groups, h.count / 2);
+  if constexpr (sizeof(T) == 4) {
+    return midpoint_f32(KO::value(sorted[lo]), KO::value(sorted[hi]));
+  } else {
+    return midpoint(KO::value(sorted[lo]), KO::value(sorted[hi]));
+  }
 }
 
-template <typename T>
+template <typename T, bool SDEC>
 __global__ void __launch_bounds__(kHThreads)
     histogram_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ HistArgs a,
                      unsigned char* scratch) {
@@ -275,7 +323,12 @@ __global__ void __launch_bounds__(kHThreads)
   __shared__ int red_sent[kHWarps];
   const Geom3& g = a.g;
   const int S = a.S;
-  unsigned int* work = reinterpret_cast<unsigned int*>(smem);
+  // Shared memory: rank codes [S] u16 | decode table [S] keys (SDEC) |
+  // work (radix tables during the sort, warp histograms while sliding).
+  uint16_t* codes_s = reinterpret_cast<uint16_t*>(smem);
+  K* decode_s = reinterpret_cast<K*>(smem + align16((long long)a.S * 2));
+  unsigned int* work = reinterpret_cast<unsigned int*>(
+      smem + align16((long long)a.S * 2) + (SDEC ? align16((long long)a.S * sizeof(K)) : 0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Slot<K> slot = slot_at<K>(scratch + (long long)blockIdx.x * a.slot_bytes, S);
   const bool drop_inf = a.r.drop_inf;
@@ -357,9 +410,11 @@ __global__ void __launch_bounds__(kHThreads)
     const uint16_t dropped = a.r.omit ? kOmitted : kPropagated;
     for (int pos = threadIdx.x; pos < S; pos += blockDim.x) {
       const K key = src_k[pos];
-      slot.codes[src_p[pos]] = key == kSent ? dropped : (uint16_t)pos;
+      codes_s[src_p[pos]] = key == kSent ? dropped : (uint16_t)pos;
+      if (SDEC) decode_s[pos] = key;
     }
     __syncthreads();
+    const K* sorted = SDEC ? decode_s : src_k;
 
     // Slide: each warp walks its columns in boustrophedon order.
     const int th_eff = (int)min((long long)a.TH, g.H - y0);
@@ -373,32 +428,27 @@ __global__ void __launch_bounds__(kHThreads)
     h.nan = 0;
     for (int i = lane; i < a.words + a.groups; i += 32) h.words[i] = 0u;
     __syncwarp();
-    const uint16_t* codes = slot.codes;
+    const uint16_t* codes = codes_s;
     const int kh = g.kh, kw = g.kw, SW = a.SW;
     if (c_begin < c_end) {
-      for (int ky = 0; ky < kh; ++ky) face(codes, ky * SW + c_begin, kw, 1, +1, h);
+      add_box(codes, c_begin, kh, kw, SW, h);
       int row = 0;
       int dir = 1;
       for (int c = c_begin; c < c_end; ++c) {
-        for (int step = 0; step < th_eff; ++step) {
-          T result = hist_finish<T>(h, a, src_k);
+        for (int i = 0; i < th_eff; ++i) {
+          T result = hist_finish<T>(h, a, sorted);
           if (lane == 0) out[(y0 + row) * g.W + x0 + c] = canonical(result);
-          if (step + 1 < th_eff) {
+          if (i + 1 < th_eff) {
             if (dir > 0) {
-              face(codes, row * SW + c, kw, 1, -1, h);
-              face(codes, (row + kh) * SW + c, kw, 1, +1, h);
+              step(codes, row * SW + c, (row + kh) * SW + c, kw, 1, h);
               ++row;
             } else {
-              face(codes, (row + kh - 1) * SW + c, kw, 1, -1, h);
-              face(codes, (row - 1) * SW + c, kw, 1, +1, h);
+              step(codes, (row + kh - 1) * SW + c, (row - 1) * SW + c, kw, 1, h);
               --row;
             }
           }
         }
-        if (c + 1 < c_end) {
-          face(codes, row * SW + c, kh, SW, -1, h);
-          face(codes, row * SW + c + kw, kh, SW, +1, h);
-        }
+        if (c + 1 < c_end) step(codes, row * SW + c, row * SW + c + kw, kh, SW, h);
         dir = -dir;
       }
     }
@@ -408,42 +458,63 @@ __global__ void __launch_bounds__(kHThreads)
 
 struct HistChoice {
   int TW = 0, TH = 0;
+  bool sdec = false;
+  size_t smem = 0;
 };
 
-HistChoice choose_tile(const Geom3& g) {
-  HistChoice c;
-  if (g.kd != 1 || g.D != 1) return c;
-  if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport) return c;
-  if (g.H == 1 && g.kh == 1) {
-    for (int tw : {4096, 2048, 1024, 512, 256, 128, 64, 32, 16}) {
-      if (tw + g.kw - 1 <= kMaxSupport && (tw <= 16 || tw / 2 < g.W)) {
-        c.TW = tw;
-        c.TH = 1;
-        return c;
+constexpr size_t kSmemBudget = 225 * 1024;
+
+size_t smem_bytes_for(int S, bool sdec, size_t key_bytes) {
+  size_t codes = (size_t)align16((long long)S * 2);
+  size_t decode = sdec ? (size_t)align16((long long)S * (long long)key_bytes) : 0;
+  size_t sort = (size_t)kHWarps * 256 * 4;
+  size_t hist = (size_t)kHWarps * ((S + 31) / 32 + (S + 1023) / 1024) * 4;
+  return codes + decode + std::max(sort, hist);
+}
+
+// Pick the output tile by a cost model in units of one histogram update per
+// output: vertical steps (2 kw), the first window of each warp's walk, the
+// column moves, the block sort (about 8 units per support sample) and a
+// global decode when the sorted keys do not fit in shared memory.
+HistChoice choose_tile(const Geom3& g, size_t key_bytes) {
+  HistChoice best;
+  if (g.kd != 1 || g.D != 1) return best;
+  if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport) return best;
+  double best_cost = 1e300;
+  auto consider = [&](int tw, int th) {
+    long long S = (long long)(tw + g.kw - 1) * (th + g.kh - 1);
+    if (S > kMaxSupport) return;
+    for (int sdec = 1; sdec >= 0; --sdec) {
+      size_t smem = smem_bytes_for((int)S, sdec != 0, key_bytes);
+      if (smem > kSmemBudget) continue;
+      const double cpw = (tw + kHWarps - 1) / kHWarps;
+      const double outputs = (double)tw * th;
+      double cost = 2.0 * g.kw + (double)g.kh * g.kw / (cpw * th) + 2.0 * g.kh / th +
+                    8.0 * (double)S / outputs + (sdec ? 0.0 : 12.0);
+      if (smem * 2 <= kSmemBudget) cost *= 0.9;  // two resident blocks per SM
+      if (cost < best_cost) {
+        best_cost = cost;
+        best.TW = tw;
+        best.TH = th;
+        best.sdec = sdec != 0;
+        best.smem = smem;
       }
+      return;
     }
-    return c;
+  };
+  if (g.H == 1 && g.kh == 1) {
+    for (int tw : {8192, 4096, 2048, 1024, 512, 256, 128, 64, 32, 16})
+      if (tw <= 16 || tw / 2 < g.W) consider(tw, 1);
+    return best;
   }
-  int tw = g.W >= 64 ? 64 : (int)(((g.W + 15) / 16) * 16);
-  for (int th : {256, 128, 64, 32, 16, 8, 4, 2, 1}) {
-    if (th > 1 && th / 2 >= g.H) continue;
-    long long s = (long long)(tw + g.kw - 1) * (th + g.kh - 1);
-    if (s <= kMaxSupport) {
-      c.TW = tw;
-      c.TH = th;
-      return c;
-    }
-  }
-  for (int w : {32, 16}) {
-    if (w >= tw) continue;
-    long long s = (long long)(w + g.kw - 1) * g.kh;
-    if (s <= kMaxSupport) {
-      c.TW = w;
-      c.TH = 1;
-      return c;
+  for (int tw : {64, 32, 16}) {
+    if (tw > 16 && tw / 2 >= g.W) continue;
+    for (int th : {256, 192, 128, 96, 64, 48, 32, 16, 8, 4, 2, 1}) {
+      if (th > 1 && th / 2 >= g.H) continue;
+      consider(tw, th);
     }
   }
-  return c;
+  return best;
 }
 
 HistArgs make_args(const Plan& p) {
@@ -464,23 +535,23 @@ HistArgs make_args(const Plan& p) {
   return a;
 }
 
-size_t smem_for(const HistArgs& a) {
-  size_t sort = (size_t)kHWarps * 256 * 4;
-  size_t hist = (size_t)kHWarps * (a.words + a.groups) * 4;
-  return std::max(sort, hist);
+template <typename T>
+void* kernel_for(bool sdec) {
+  return sdec ? (void*)histogram_kernel<T, true> : (void*)histogram_kernel<T, false>;
 }
 
 template <typename T>
 cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   HistArgs a = make_args(p);
-  auto kernel = histogram_kernel<T>;
-  cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
-  if (e != cudaSuccess) return e;
   long long slots = (long long)(p.scratch_bytes / (size_t)a.slot_bytes);
   long long grid = std::min<long long>(a.tiles, slots);
   if (grid < 1) return cudaErrorInvalidValue;
-  kernel<<<(unsigned)grid, kHThreads, p.smem_bytes, s>>>(in, out, a, (unsigned char*)p.d_scratch);
+  if (p.hist_sdec)
+    histogram_kernel<T, true><<<(unsigned)grid, kHThreads, p.smem_bytes, s>>>(in, out, a,
+                                                                             (unsigned char*)p.d_scratch);
+  else
+    histogram_kernel<T, false><<<(unsigned)grid, kHThreads, p.smem_bytes, s>>>(in, out, a,
+                                                                              (unsigned char*)p.d_scratch);
   return cudaGetLastError();
 }
 
@@ -492,38 +563,34 @@ bool histogram_supported(const Plan& p) {
   if (k != kMedian && k != kMedianNetwork && k != kMedianHistogram && k != kRank &&
       k != kRankHistogram && k != kMin && k != kMax && k != kPercentile)
     return false;
-  HistChoice c = choose_tile(p.tile.g);
+  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8);
   return c.TW > 0;
 }
 
 void histogram_configure(Plan& p) {
-  HistChoice c = choose_tile(p.tile.g);
+  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8);
   p.hist_block_w = c.TW;
   p.hist_block_h = c.TH;
+  p.hist_sdec = c.sdec;
   HistArgs a = make_args(p);
   p.hist_blocks_x = a.tiles_x;
   p.hist_blocks_y = a.tiles / a.tiles_x;
 }
 
-size_t histogram_smem(const Plan& p) { return smem_for(make_args(p)); }
+size_t histogram_smem(const Plan& p) {
+  HistArgs a = make_args(p);
+  return smem_bytes_for(a.S, p.hist_sdec, p.dtype == 0 ? 4 : 8);
+}
 
-// Scratch slots: one per resident block (occupancy x SMs), capped by the
-// number of tiles.
+// Scratch slots for the block sort: one per resident block (occupancy x
+// SMs), capped by the number of tiles.
 cudaError_t histogram_allocate(Plan& p) {
   HistArgs a = make_args(p);
+  void* kernel = p.dtype == 0 ? kernel_for<float>(p.hist_sdec) : kernel_for<double>(p.hist_sdec);
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+  if (e != cudaSuccess) return e;
   int per_sm = 1;
-  cudaError_t e;
-  if (p.dtype == 0) {
-    cudaFuncSetAttribute(histogram_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)p.smem_bytes);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, histogram_kernel<float>, kHThreads,
-                                                      p.smem_bytes);
-  } else {
-    cudaFuncSetAttribute(histogram_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)p.smem_bytes);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, histogram_kernel<double>, kHThreads,
-                                                      p.smem_bytes);
-  }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kHThreads, p.smem_bytes);
   if (e != cudaSuccess) return e;
   long long slots = std::min<long long>(a.tiles, (long long)std::max(per_sm, 1) * p.sm_count);
   p.scratch_bytes = (size_t)slots * (size_t)a.slot_bytes;

@@ -104,7 +104,11 @@ __device__ __forceinline__ K pick(const K (&a)[N], int idx) {
 
 template <typename T>
 __device__ __forceinline__ T median_of_two(T lower, T upper) {
-  return from_f64<T>(midpoint((double)lower, (double)upper));
+  if constexpr (sizeof(T) == 4) {
+    return midpoint_f32(lower, upper);
+  } else {
+    return midpoint(lower, upper);
+  }
 }
 
 // Epilogue of the register network: the statistic from sorted keys.
@@ -122,6 +126,22 @@ __device__ __forceinline__ T network_finish(const K (&k)[N], int nv, const Reduc
       return median_of_two(KO::value(k[VFIX / 2 - 1]), KO::value(k[VFIX / 2]));
     }
     constexpr int B = (VFIX > 0 ? VFIX : N) / 2 + 1;
+    if constexpr (VFIX >= 9 && VFIX % 2 == 1) {
+      // With at most 4 dropped samples (odd VFIX) the middle ranks lie in
+      // [VFIX/2 - 2, VFIX/2]: a 3-way pick instead of a B-way one.
+      constexpr int L = VFIX / 2 - 2;
+      if (nv >= VFIX - 4) {
+        const int hi = nv / 2 - L;
+        K a_hi = k[L];
+#pragma unroll
+        for (int i = 1; i < 3; ++i) a_hi = (i == hi) ? k[L + i] : a_hi;
+        if (nv & 1) return KO::value(a_hi);
+        K a_lo = k[L];
+#pragma unroll
+        for (int i = 1; i < 3; ++i) a_lo = (i == hi - 1) ? k[L + i] : a_lo;
+        return median_of_two(KO::value(a_lo), KO::value(a_hi));
+      }
+    }
     if (nv & 1) return KO::value(pick<B>(k, nv / 2));
     return median_of_two(KO::value(pick<B>(k, nv / 2 - 1)), KO::value(pick<B>(k, nv / 2)));
   }

@@ -107,6 +107,7 @@ struct Plan {
 
   // Histogram kernel geometry (rectangular 1-D/2-D windows).
   int hist_block_w = 0, hist_block_h = 0;
+  bool hist_sdec = false;  // sorted keys staged in shared memory
   long long hist_blocks_x = 0, hist_blocks_y = 0;
 };
 

@@ -238,3 +238,29 @@ def test_box_pair_kernel(gpu, oracle, dtype, box) -> None:
     if dtype == np.float32 or box < 7:
         assert plan.algorithm == "tile_box"
     plan.close()
+
+
+def test_float32_midpoint_fast_path_matches_float64_rule(gpu, oracle) -> None:
+    """Even-count medians over value pairs that straddle every branch of the
+    float32 midpoint fast path (exponent gaps around 28, tiny and huge
+    magnitudes, signed zeros, opposite signs) stay bit-identical."""
+    rng = np.random.default_rng(99)
+    specials = np.array([0.0, -0.0, 1.0, -1.0, 3.4e38, -3.4e38, 1e-30, -1e-30, 1e-38, 2.0 ** -97,
+                         2.0 ** -98, 2.0 ** 126, 2.0 ** 127, 1.0 + 2.0 ** -23, 2.0 ** 28, 2.0 ** 29,
+                         1.5e-45, np.inf, -np.inf], dtype=np.float32)
+    mags = (2.0 ** rng.integers(-140, 128, size=4000)).astype(np.float32)
+    values = np.concatenate([specials, mags * rng.choice([-1, 1], size=mags.size),
+                             rng.normal(size=4000).astype(np.float32) * 1000])
+    rng.shuffle(values)
+    pairs = values[: (values.size // 2) * 2].reshape(-1, 2)
+    # Each 2-sample window (size 2, wrap over a 2-long axis) is one midpoint.
+    array = np.ascontiguousarray(pairs, dtype=np.float32)
+    for kind in ("median", "median_network"):
+        args = (kind, array, (1, 2), None, (0, 0), ("wrap", "wrap"), 0.0, True, False, 1)
+        _assert_bits(_gpu(*args), _oracle(oracle, "median", *args[1:]), kind)
+    # The same pairs inside 3x3 windows with one NaN (8 retained samples).
+    grid = np.resize(values, (40, 60)).astype(np.float32)
+    grid[::3, ::3] = np.nan
+    for kind in ("median", "median_network"):
+        args = (kind, grid, (3, 3), None, (0, 0), ("reflect", "reflect"), 0.0, True, False, 1)
+        _assert_bits(_gpu(*args), _oracle(oracle, "median", *args[1:]), kind)
