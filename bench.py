@@ -218,6 +218,47 @@ def cpu_baseline(image: np.ndarray, spec, budget_s: float = 3.0, threads: int | 
 
 
 # ---------------------------------------------------------------------------
+# Precision study: nanstd against an exact (double-double) oracle.
+
+def precision_study(rows: int = 192, width: int = 4096) -> dict:
+    """Max relative error (and float32 ulp error) of nanstd on a strip of the
+    1e4 + N(0, 1) image with 1% NaN, ddof=1, min_count=5, ignore_inf=True."""
+    import ndfiltrs_gb300 as nf
+    from oracle import oracle
+
+    report = {"sample": f"{rows}x{width} strip of the seed-4 precision image (1e4 + N(0,1), 1% NaN)",
+              "reference": "exact double-double window moments rounded once to float64"}
+    for dtype in (np.float32, np.float64):
+        image = np.ascontiguousarray(precision_image(width, dtype=dtype)[:rows])
+        for size in ((31, 31), (7, 51)):
+            opts = dict(omit_nan=True, ignore_inf=True, min_count=5)
+            exact = oracle.exact_moments(image, "std", size, mode="reflect", ddof=1, **opts)
+            finite = np.isfinite(exact) & (exact > 0)
+            results = {}
+            for name in ("fp32c", "fp64"):
+                plan = nf.Plan(image.shape, dtype, "std", size, mode=["reflect"] * 2, parameter=1,
+                               moments=name, **opts)
+                results[f"gpu_{name}"] = plan.run_host(image)
+                plan.close()
+            results["cpu_reference_restatement"] = oracle.window_filter(
+                image, "std", size, mode="reflect", parameter=1, **opts)
+            entry = {}
+            for name, value in results.items():
+                nan_match = bool(np.array_equal(np.isnan(value), np.isnan(exact)))
+                a = value[finite].astype(np.float64)
+                e = exact[finite]
+                rel = float(np.max(np.abs(a - e) / np.abs(e))) if a.size else 0.0
+                item = {"max_rel_err": rel, "nan_pattern_matches": nan_match}
+                if dtype == np.float32:
+                    rounded = e.astype(np.float32)
+                    ulp = np.spacing(np.abs(rounded)).astype(np.float64)
+                    item["max_ulp_err"] = float(np.max(np.abs(a - rounded.astype(np.float64)) / ulp))
+                entry[name] = item
+            report[f"{np.dtype(dtype).name}_{size[0]}x{size[1]}"] = entry
+    return report
+
+
+# ---------------------------------------------------------------------------
 
 def run_reference(args, spec, workload: str) -> None:
     image = spec[0]()
@@ -268,6 +309,8 @@ def main() -> None:
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     parser.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--precision", action=argparse.BooleanOptionalAction, default=True,
+                        help="add the nanstd precision study to the line")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
     spec = WORKLOADS[args.workload]
@@ -372,8 +415,11 @@ def main() -> None:
     bytes_per_launch = pixels * image.itemsize * 2
     achieved = bytes_per_launch / (ms_per_step / 1e3) / 1e9
     base = None
+    precision = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(image, spec)
+    if rank == 0 and world == 1 and args.precision:
+        precision = precision_study()
 
     if rank == 0:
         line = {
@@ -421,6 +467,7 @@ def main() -> None:
             "cpu_baseline": base,
             "clocks": clocks.summary(),
             "gpu_launches": args.steps,
+            "nanstd_precision": precision,
             "parity_check_rows64": check,
         }
         print(json.dumps(line))

@@ -92,7 +92,7 @@ cudaError_t launch_box(const Plan& p, const T* in, T* out, cudaStream_t s) {
   const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork;
   auto kernel = median ? tile_box_kernel<T, KH, KW, 1> : tile_box_kernel<T, KH, KW, 0>;
   cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+      allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
   kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile);
   return cudaGetLastError();

@@ -55,6 +55,25 @@ const char* algo_name(Algo a) {
   return "unknown";
 }
 
+cudaError_t allow_max_smem(const void* kernel) {
+  static std::mutex lock;
+  static std::vector<const void*> done;
+  std::lock_guard<std::mutex> guard(lock);
+  for (const void* k : done)
+    if (k == kernel) return cudaSuccess;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes attr;
+  e = cudaFuncGetAttributes(&attr, kernel);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)attr.sharedSizeBytes);
+  if (e == cudaSuccess) done.push_back(kernel);
+  return e;
+}
+
 namespace {
 
 struct DeviceState {

@@ -587,7 +587,7 @@ size_t histogram_smem(const Plan& p) {
 cudaError_t histogram_allocate(Plan& p) {
   HistArgs a = make_args(p);
   void* kernel = p.dtype == 0 ? kernel_for<float>(p.hist_sdec) : kernel_for<double>(p.hist_sdec);
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+  cudaError_t e = allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
   int per_sm = 1;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kHThreads, p.smem_bytes);

@@ -428,7 +428,7 @@ template <typename T, int PREC>
 cudaError_t launch_tile_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   auto kernel = tile_moments_kernel<T, PREC>;
   cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+      allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
   kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile, p.d_tile_taps);
   return cudaGetLastError();

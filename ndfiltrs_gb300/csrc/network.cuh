@@ -131,14 +131,11 @@ __device__ __forceinline__ T network_finish(const K (&k)[N], int nv, const Reduc
       // [VFIX/2 - 2, VFIX/2]: a 3-way pick instead of a B-way one.
       constexpr int L = VFIX / 2 - 2;
       if (nv >= VFIX - 4) {
-        const int hi = nv / 2 - L;
-        K a_hi = k[L];
-#pragma unroll
-        for (int i = 1; i < 3; ++i) a_hi = (i == hi) ? k[L + i] : a_hi;
+        const int hi = nv / 2 - L;  // 0, 1 or 2
+        const K c0 = k[L], c1 = k[L + 1], c2 = k[L + 2];
+        const K a_hi = hi == 0 ? c0 : (hi == 1 ? c1 : c2);
         if (nv & 1) return KO::value(a_hi);
-        K a_lo = k[L];
-#pragma unroll
-        for (int i = 1; i < 3; ++i) a_lo = (i == hi - 1) ? k[L + i] : a_lo;
+        const K a_lo = hi == 1 ? c0 : c1;  // even nv: hi is 1 or 2
         return median_of_two(KO::value(a_lo), KO::value(a_hi));
       }
     }

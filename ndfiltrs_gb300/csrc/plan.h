@@ -113,6 +113,11 @@ struct Plan {
 
 const char* algo_name(Algo a);
 
+// Raise a kernel's dynamic shared-memory limit to the device maximum, once.
+// The attribute belongs to the function, not to a plan, so it is never
+// lowered after one plan set it.
+cudaError_t allow_max_smem(const void* kernel);
+
 // Launchers (one per translation unit). Return a cudaError_t.
 cudaError_t launch_tile_select(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_tile_box(const Plan& p, const void* in, void* out, cudaStream_t s);

@@ -214,7 +214,7 @@ cudaError_t launch_network(const Plan& p, const T* in, T* out, cudaStream_t s) {
   }
   auto kernel = tile_network_kernel<T, N, VFIX, MODE>;
   cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+      allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
   kernel<<<(unsigned)a.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, a, taps);
   return cudaGetLastError();
@@ -256,7 +256,7 @@ cudaError_t launch_tile_select_t(const Plan& p, const T* in, T* out, cudaStream_
   }
   auto kernel = tile_radix_kernel<T>;
   cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem_bytes);
+      allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
   kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile, p.d_tile_taps);
   return cudaGetLastError();
