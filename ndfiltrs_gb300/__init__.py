@@ -25,10 +25,11 @@ from ._api import (
     std_filter,
     var_filter,
 )
-from ._core import Plan, device_info
+from ._core import Batch, Plan, device_info
 from ._robust import nanpercentile_filter, percentile_filter
 
 __all__ = [
+    "Batch",
     "Plan",
     "device_info",
     "get_num_threads",

@@ -315,6 +315,74 @@ class Plan:
         self.close()
 
 
+class Batch:
+    """Batched persistent path over many float32 images (``ndf_batch_*``).
+
+    ``specs`` is a list of dicts with the Plan keyword arguments (``shape``,
+    ``kind``, ``size``, ``footprint``, ``origin``, ``mode``, ``cval``,
+    ``omit_nan``, ``ignore_inf``, ``min_count``, ``parameter``,
+    ``percentile``, ``moments``). ``run_device`` takes device pointers of
+    every image and enqueues the captured CUDA graph on ``stream``.
+    """
+
+    def __init__(self, specs: list[dict]) -> None:
+        lib, _ = _load()
+        self._keep = []
+        descs = (FilterDesc * len(specs))()
+        for i, spec in enumerate(specs):
+            shape = tuple(int(v) for v in spec["shape"])
+            ndim = len(shape)
+            footprint = spec.get("footprint")
+            size = list(np.asarray(footprint).shape) if footprint is not None else list(spec["size"])
+            origin = list(spec.get("origin") or [0] * ndim)
+            mode = spec.get("mode") or ["reflect"] * ndim
+            if isinstance(mode, str):
+                mode = [mode] * ndim
+            fp_ptr = None
+            if footprint is not None:
+                mask = np.ascontiguousarray(np.asarray(footprint, dtype=bool).ravel(), dtype=np.uint8)
+                self._keep.append(mask)
+                fp_ptr = mask.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+            arrays = (_u64(shape), _u64(size), _i64(origin), _i32([MODES[m] for m in mode]))
+            self._keep.append(arrays)
+            descs[i] = FilterDesc(
+                0, ndim, arrays[0], arrays[1], fp_ptr, arrays[2], arrays[3],
+                float(np.float32(spec.get("cval", 0.0))), KINDS[spec["kind"]],
+                int(bool(spec.get("omit_nan", False))), int(bool(spec.get("ignore_inf", False))),
+                int(spec.get("min_count", 1)), int(spec.get("parameter", 0)),
+                float(spec.get("percentile", 50.0)), MOMENTS[spec.get("moments", "fp32c")],
+            )
+        handle = ctypes.c_void_p()
+        _check(lib.ndf_batch_create(descs, len(specs), ctypes.byref(handle)), lib)
+        self._handle = handle
+        self.count = len(specs)
+
+    @property
+    def launches(self) -> int:
+        lib, _ = _load()
+        return int(lib.ndf_batch_launches(self._handle))
+
+    def run_device(self, d_in: list[int], d_out: list[int], stream: int = 0) -> None:
+        lib, _ = _load()
+        if len(d_in) != self.count or len(d_out) != self.count:
+            raise ValueError("one input and one output pointer per image")
+        ins = (ctypes.c_void_p * self.count)(*d_in)
+        outs = (ctypes.c_void_p * self.count)(*d_out)
+        _check(lib.ndf_batch_run(self._handle, ins, outs, stream), lib)
+
+    def close(self) -> None:
+        if getattr(self, "_handle", None) is not None and self._handle.value:
+            lib, _ = _load()
+            lib.ndf_batch_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _typed_array(array: object) -> np.ndarray:
     if not isinstance(array, np.ndarray) or array.dtype not in (np.float32, np.float64):
         raise TypeError("argument 'array': expected a float32 or float64 numpy.ndarray")

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kThreads)
   long long* maps = reinterpret_cast<long long*>(smem_raw);
   K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
   long long z, y0, x0;
-  tile_coords(a, z, y0, x0);
+  tile_coords(a, blockIdx.x, z, y0, x0);
   build_maps(maps, g, t, z, y0, x0);
   __syncthreads();
   const bool drop_inf = a.r.drop_inf;

@@ -527,6 +527,22 @@ int one_shot(const ndf_filter_desc& d, const void* h_in, void* h_out) {
 }
 
 }  // namespace
+
+// Plan construction for the batched path (batch.cu).
+int batch_build_plan(const ndf_filter_desc* d, Plan& p, int* smem_limit) {
+  int rc = build_plan(d, p);
+  if (rc != NDF_OK) return rc;
+  if (p.n_out == 0) {
+    p.algo = Algo::kEmpty;
+    return NDF_OK;
+  }
+  rc = ensure_device(&p.device, &p.sm_count, smem_limit);
+  if (rc != NDF_OK) return rc;
+  return choose_algorithm(p, *smem_limit);
+}
+
+void batch_release_plan(Plan& p) { release(p); }
+
 }  // namespace ndf
 
 using namespace ndf;

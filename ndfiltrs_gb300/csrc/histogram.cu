@@ -19,9 +19,9 @@
 //  * sliding: each warp owns a strip of output columns and walks it in
 //    boustrophedon order; a vertical step removes one support row segment
 //    (kw codes) and adds another, spread over the 32 lanes with shared-memory
-//    atomics on the warp's private bitset and per-1024-rank group counts; a
-//    selection is two warp scans (groups, then words) and a 5-step select in
-//    the final word.
+//    atomics on the warp's private bitset; a selection scans 1024 ranks per
+//    warp step from a tracked pivot (the previous window's median) and ends
+//    with a 5-step select in the final word.
 #include <algorithm>
 
 #include "common.cuh"
@@ -41,7 +41,7 @@ struct HistArgs {
   int TW, TH, SW, SH, S;
   long long tiles_x, tiles;
   int cols_per_warp;
-  int words, groups;        // per-warp bit histogram: 32-bit words, 1024-rank groups
+  int words;                // per-warp bit histogram: 32-bit words
   long long slot_bytes;     // scratch bytes per block slot
   Reduce r;
 };
@@ -179,69 +179,103 @@ __device__ __forceinline__ int select_in_word32(unsigned int word, int k) {
   return position;
 }
 
-// Rank (0-based position in the block's sorted keys) of the k-th set bit.
-__device__ __forceinline__ int hist_select(const unsigned int* words, const unsigned int* groups,
-                                           int nwords, int ngroups, int k) {
-  const int lane = threadIdx.x & 31;
-  unsigned int g0 = lane < ngroups ? groups[lane] : 0u;
-  unsigned int g1 = lane + 32 < ngroups ? groups[lane + 32] : 0u;
-  unsigned int tot0 = __reduce_add_sync(0xffffffffu, g0);
-  unsigned int v = g0;
-  int base = 0;
-  if ((unsigned int)k >= tot0) {
-    k -= (int)tot0;
-    v = g1;
-    base = 32;
-  }
-  unsigned int s = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned int t = __shfl_up_sync(0xffffffffu, s, o);
-    if (lane >= o) s += t;
-  }
-  int L = max(__ffs(__ballot_sync(0xffffffffu, s > (unsigned int)k)) - 1, 0);
-  k -= (int)__shfl_sync(0xffffffffu, s - v, L);
-  const int g = base + L;
-  const int wi = g * 32 + lane;
-  unsigned int w = wi < nwords ? words[wi] : 0u;
-  unsigned int pc = __popc(w);
-  unsigned int s2 = pc;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned int t = __shfl_up_sync(0xffffffffu, s2, o);
-    if (lane >= o) s2 += t;
-  }
-  int L2 = max(__ffs(__ballot_sync(0xffffffffu, s2 > (unsigned int)k)) - 1, 0);
-  k -= (int)__shfl_sync(0xffffffffu, s2 - pc, L2);
-  unsigned int word = __shfl_sync(0xffffffffu, w, L2);
-  return (g * 32 + L2) * 32 + select_in_word32(word, k);
-}
-
+// Bit histogram of one warp. `pivot` is a word-aligned rank and `below`
+// the number of window samples whose rank is below it; both are uniform
+// across the warp. A selection scans 32 words (1024 ranks) at a time from
+// the pivot and leaves the pivot at the word it found, so the next window's
+// median (a few ranks away) is usually found in one scan.
 struct WarpHist {
   unsigned int* words;
-  unsigned int* groups;
+  int nwords;
+  int pivot;  // multiple of 32
+  int below;
   int count;  // retained samples in the window
   int nan;    // propagated NaN samples in the window
 };
 
-// Apply one step: remove the codes of one face and add those of another
-// (n codes each, `stride` apart, in shared memory). All loads are issued
-// before the atomics.
-__device__ __forceinline__ void update(const uint16_t* codes, unsigned int* words, unsigned int* groups,
-                                       int c, int sign, int& kept, int& nans) {
-  if (c < kPropagated) {
-    atomicXor(&words[c >> 5], 1u << (c & 31));
-    atomicAdd(&groups[c >> 10], (unsigned int)sign);
-    kept += sign;
-  } else if (c == kPropagated) {
-    nans += sign;
+__device__ __forceinline__ unsigned int warp_inclusive_scan(unsigned int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
   }
+  return v;
 }
 
+// Rank of the k-th (0-based) set bit; k < h.count.
+__device__ __forceinline__ int hist_select(WarpHist& h, int k) {
+  const int lane = threadIdx.x & 31;
+  int w0 = h.pivot >> 5;
+  if (k >= h.below) {
+    int base = h.below;  // set bits below word w0
+    for (int guard = 0; guard < 4096; ++guard) {
+      const int wi = w0 + lane;
+      const unsigned int word = wi < h.nwords ? h.words[wi] : 0u;
+      const unsigned int pc = __popc(word);
+      const unsigned int incl = warp_inclusive_scan(pc);
+      const int total = (int)__shfl_sync(0xffffffffu, incl, 31);
+      if (base + total > k || w0 + 32 >= h.nwords) {
+        const unsigned int ball = __ballot_sync(0xffffffffu, base + (int)incl > k);
+        const int L = ball ? __ffs(ball) - 1 : 31;
+        const int before = base + (int)__shfl_sync(0xffffffffu, incl - pc, L);
+        const unsigned int w = __shfl_sync(0xffffffffu, word, L);
+        h.pivot = (w0 + L) * 32;
+        h.below = before;
+        return h.pivot + select_in_word32(w, k - before);
+      }
+      base += total;
+      w0 += 32;
+    }
+    return 0;
+  }
+  int top = h.below;  // set bits below word w0
+  for (int guard = 0; guard < 4096; ++guard) {
+    const int lo = w0 - 32;
+    const int wi = lo + lane;
+    const unsigned int word = wi >= 0 ? h.words[wi] : 0u;
+    const unsigned int pc = __popc(word);
+    const unsigned int incl = warp_inclusive_scan(pc);
+    const int total = (int)__shfl_sync(0xffffffffu, incl, 31);
+    const int start = top - total;  // set bits below word lo
+    if (start <= k || lo <= 0) {
+      const unsigned int ball = __ballot_sync(0xffffffffu, start + (int)incl > k);
+      const int L = ball ? __ffs(ball) - 1 : 31;
+      const int before = start + (int)__shfl_sync(0xffffffffu, incl - pc, L);
+      const unsigned int w = __shfl_sync(0xffffffffu, word, L);
+      h.pivot = (lo + L) * 32;
+      h.below = before;
+      return h.pivot + select_in_word32(w, k - before);
+    }
+    top = start;
+    w0 = lo;
+  }
+  return 0;
+}
+
+// One add (+1) or remove (-1) of a code.
+__device__ __forceinline__ void update(const WarpHist& h, int c, int sign, int& kept, int& below,
+                                       int& nans) {
+  const bool valid = c < (int)kPropagated;
+  if (valid) atomicXor(&h.words[c >> 5], 1u << (c & 31));
+  kept += valid ? sign : 0;
+  below += (valid && c < h.pivot) ? sign : 0;
+  nans += c == (int)kPropagated ? sign : 0;
+}
+
+__device__ __forceinline__ void finish_update(WarpHist& h, int kept, int below, int nans) {
+  h.count += __reduce_add_sync(0xffffffffu, kept);
+  h.below += __reduce_add_sync(0xffffffffu, below);
+  h.nan += __reduce_add_sync(0xffffffffu, nans);
+  __syncwarp();
+}
+
+// Remove the codes of one face and add those of another (n codes each,
+// `stride` apart, in shared memory). All loads are issued before the atomics.
 __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, int add_start, int n,
                                      int stride, WarpHist& h) {
   const int lane = threadIdx.x & 31;
-  int kept = 0, nans = 0;
+  int kept = 0, below = 0, nans = 0;
   for (int i0 = 0; i0 < n; i0 += 128) {
     int rc[4], ac[4];
 #pragma unroll
@@ -252,36 +286,30 @@ __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, in
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      update(codes, h.words, h.groups, rc[j], -1, kept, nans);
-      update(codes, h.words, h.groups, ac[j], +1, kept, nans);
+      update(h, rc[j], -1, kept, below, nans);
+      update(h, ac[j], +1, kept, below, nans);
     }
   }
-  h.count += __reduce_add_sync(0xffffffffu, kept);
-  h.nan += __reduce_add_sync(0xffffffffu, nans);
-  __syncwarp();
+  finish_update(h, kept, below, nans);
 }
 
 // Add every code of a kh x kw box (the first window of a warp's walk).
 __device__ __forceinline__ void add_box(const uint16_t* codes, int start, int kh, int kw, int SW,
                                        WarpHist& h) {
   const int lane = threadIdx.x & 31;
-  int kept = 0, nans = 0;
+  int kept = 0, below = 0, nans = 0;
   for (int ky = 0; ky < kh; ++ky)
-    for (int i = lane; i < kw; i += 32) update(codes, h.words, h.groups, codes[start + ky * SW + i], +1, kept, nans);
-  h.count += __reduce_add_sync(0xffffffffu, kept);
-  h.nan += __reduce_add_sync(0xffffffffu, nans);
-  __syncwarp();
+    for (int i = lane; i < kw; i += 32) update(h, codes[start + ky * SW + i], +1, kept, below, nans);
+  finish_update(h, kept, below, nans);
 }
 
 template <typename T>
-__device__ __forceinline__ T hist_finish(const WarpHist& h, const HistArgs& a,
+__device__ __forceinline__ T hist_finish(WarpHist& h, const HistArgs& a,
                                          const typename KeyOf<T>::K* sorted) {
   using KO = KeyOf<T>;
   const Reduce& r = a.r;
   if ((!r.omit && h.nan > 0) || (r.omit && h.count < r.min_count) || h.count == 0) return nan_of(T());
-  auto value_at = [&](int k) {
-    return KO::value(sorted[hist_select(h.words, h.groups, a.words, a.groups, k)]);
-  };
+  auto value_at = [&](int k) { return KO::value(sorted[hist_select(h, k)]); };
   switch (r.kind) {
     case kRank:
     case kRankHistogram:
@@ -302,8 +330,8 @@ __device__ __forceinline__ T hist_finish(const WarpHist& h, const HistArgs& a,
       break;
   }
   if (h.count & 1) return value_at(h.count / 2);
-  const int lo = hist_select(h.words, h.groups, a.words, a.groups, h.count / 2 - 1);
-  const int hi = hist_select(h.words, h.groups, a.words, a.groups, h.count / 2);
+  const int lo = hist_select(h, h.count / 2 - 1);
+  const int hi = hist_select(h, h.count / 2);
   if constexpr (sizeof(T) == 4) {
     return midpoint_f32(KO::value(sorted[lo]), KO::value(sorted[hi]));
   } else {
@@ -312,7 +340,7 @@ __device__ __forceinline__ T hist_finish(const WarpHist& h, const HistArgs& a,
 }
 
 template <typename T, bool SDEC>
-__global__ void __launch_bounds__(kHThreads)
+__global__ void __launch_bounds__(kHThreads, 1)
     histogram_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ HistArgs a,
                      unsigned char* scratch) {
   using K = typename KeyOf<T>::K;
@@ -422,11 +450,13 @@ __global__ void __launch_bounds__(kHThreads)
     const int c_begin = warp * a.cols_per_warp;
     const int c_end = min(tw_eff, c_begin + a.cols_per_warp);
     WarpHist h;
-    h.words = work + warp * (a.words + a.groups);
-    h.groups = h.words + a.words;
+    h.words = work + warp * a.words;
+    h.nwords = a.words;
+    h.pivot = 0;
+    h.below = 0;
     h.count = 0;
     h.nan = 0;
-    for (int i = lane; i < a.words + a.groups; i += 32) h.words[i] = 0u;
+    for (int i = lane; i < a.words; i += 32) h.words[i] = 0u;
     __syncwarp();
     const uint16_t* codes = codes_s;
     const int kh = g.kh, kw = g.kw, SW = a.SW;
@@ -468,7 +498,7 @@ size_t smem_bytes_for(int S, bool sdec, size_t key_bytes) {
   size_t codes = (size_t)align16((long long)S * 2);
   size_t decode = sdec ? (size_t)align16((long long)S * (long long)key_bytes) : 0;
   size_t sort = (size_t)kHWarps * 256 * 4;
-  size_t hist = (size_t)kHWarps * ((S + 31) / 32 + (S + 1023) / 1024) * 4;
+  size_t hist = (size_t)kHWarps * ((S + 31) / 32) * 4;
   return codes + decode + std::max(sort, hist);
 }
 
@@ -529,7 +559,6 @@ HistArgs make_args(const Plan& p) {
   a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
   a.cols_per_warp = (a.TW + kHWarps - 1) / kHWarps;
   a.words = (a.S + 31) / 32;
-  a.groups = (a.S + 1023) / 1024;
   a.slot_bytes = p.dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
   a.r = p.r;
   return a;

@@ -165,9 +165,8 @@ __device__ __forceinline__ T network_finish(const K (&k)[N], int nv, const Reduc
   }
 }
 
-__device__ __forceinline__ void tile_coords(const TileArgs& a, long long& z, long long& y0,
-                                            long long& x0) {
-  long long tile = blockIdx.x;
+__device__ __forceinline__ void tile_coords(const TileArgs& a, long long tile, long long& z,
+                                            long long& y0, long long& x0) {
   long long tx = tile % a.t.tiles_x;
   long long rest = tile / a.t.tiles_x;
   long long ty = rest % a.t.tiles_y;
@@ -176,6 +175,142 @@ __device__ __forceinline__ void tile_coords(const TileArgs& a, long long& z, lon
   x0 = tx * a.t.TW;
 }
 
+// One output tile of the register-network kernel. `tap(i)` returns the
+// shared-memory offset of tap i relative to a thread's output.
+template <typename T, int N, int VFIX, int MODE, typename Tap>
+__device__ __forceinline__ void tile_network_body(const T* __restrict__ in, T* __restrict__ out,
+                                                  const TileArgs& a, long long tile,
+                                                  unsigned char* smem_raw, Tap tap) {
+  using K = typename KeyOf<T>::K;
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
+  long long z, y0, x0;
+  tile_coords(a, tile, z, y0, x0);
+  build_maps(maps, g, t, z, y0, x0);
+  __syncthreads();
+  const bool drop_inf = a.r.drop_inf;
+  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  __syncthreads();
+
+  const int tx = threadIdx.x % t.TW;
+  const int ty = threadIdx.x / t.TW;
+  const long long y = y0 + ty, x = x0 + tx;
+  if (ty >= t.TH || y >= g.H || x >= g.W) return;
+  const K* base = s + ty * t.SW + tx;
+  const int V = VFIX > 0 ? VFIX : a.r.count;
+  K k[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) k[i] = i < V ? base[tap(i)] : KeyOf<T>::kSentinel;
+  int nv = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) nv += (i < V && k[i] != KeyOf<T>::kSentinel) ? 1 : 0;
+  batcher_sort<N>(k);
+  T result = network_finish<T, N, VFIX, MODE>(k, nv, a.r);
+  out[(z * g.H + y) * g.W + x] = canonical(result);
+}
+
+// ---------------------------------------------------------------------------
+// Bit-serial radix select: the k-th smallest retained key (k < nv). Bits
+// shared by every retained key (from their AND and OR) are skipped.
+template <typename K, typename Fetch>
+__device__ __forceinline__ K radix_select(Fetch&& fetch, int V, long long k, K and_v, K or_v) {
+  K diff = and_v ^ or_v;
+  if (diff == 0) return and_v;
+  const int bits = sizeof(K) * 8;
+  int top = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)diff) : __clz((int)diff));
+  K mask = top + 1 >= bits ? K(0) : ~((K(1) << (top + 1)) - 1);
+  K prefix = and_v & mask;
+  for (int b = top; b >= 0; --b) {
+    K bit = K(1) << b;
+    K m = mask | bit;
+    long long c = 0;
+    for (int i = 0; i < V; ++i) c += ((fetch(i) & m) == prefix) ? 1 : 0;
+    if (k >= c) {
+      k -= c;
+      prefix |= bit;
+    }
+    mask = m;
+  }
+  return prefix;
+}
+
+struct KeyStats {
+  int nv;
+};
+
+template <typename T, typename K, typename Fetch>
+__device__ __forceinline__ T radix_finish(Fetch&& fetch, const Reduce& r) {
+  using KO = KeyOf<T>;
+  const K sent = KO::kSentinel;
+  const int V = r.count;
+  int nv = 0;
+  K and_v = sent, or_v = 0, kmin = sent, kmax = 0;
+  for (int i = 0; i < V; ++i) {
+    K key = fetch(i);
+    if (key != sent) {
+      nv += 1;
+      and_v &= key;
+      or_v |= key;
+      kmin = key < kmin ? key : kmin;
+      kmax = key > kmax ? key : kmax;
+    }
+  }
+  const bool missing = r.omit ? (nv < r.min_count) : (nv != V);
+  if (missing || nv == 0) return nan_of(T());
+  auto sel = [&](long long kk) { return radix_select<K>(fetch, V, kk, and_v, or_v); };
+  switch (r.kind) {
+    case kMin:
+      return KO::value(kmin);
+    case kMax:
+      return KO::value(kmax);
+    case kRank:
+    case kRankHistogram:
+      if (r.param >= nv) return nan_of(T());
+      return KO::value(sel(r.param));
+    case kPercentile: {
+      if (r.q == 100.0) return KO::value(kmax);
+      PercentileRank pr = percentile_rank(r.q_fraction, nv);
+      double lo = (double)KO::value(sel(pr.lower));
+      double hi = pr.upper == pr.lower ? lo : (double)KO::value(sel(pr.upper));
+      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+    }
+    default:
+      if (nv & 1) return KO::value(sel(nv / 2));
+      return median_of_two(KO::value(sel(nv / 2 - 1)), KO::value(sel(nv / 2)));
+  }
+}
+
+// One output tile of the radix-select kernel; `taps` are shared-memory
+// offsets relative to a thread's output.
+template <typename T>
+__device__ __forceinline__ void tile_radix_body(const T* __restrict__ in, T* __restrict__ out,
+                                                const TileArgs& a, long long tile,
+                                                unsigned char* smem_raw, const int32_t* taps) {
+  using K = typename KeyOf<T>::K;
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
+  long long z, y0, x0;
+  tile_coords(a, tile, z, y0, x0);
+  build_maps(maps, g, t, z, y0, x0);
+  __syncthreads();
+  const bool drop_inf = a.r.drop_inf;
+  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  __syncthreads();
+  const int tx = threadIdx.x % t.TW;
+  const int ty = threadIdx.x / t.TW;
+  const long long y = y0 + ty, x = x0 + tx;
+  if (ty >= t.TH || y >= g.H || x >= g.W) return;
+  const K* base = s + ty * t.SW + tx;
+  auto fetch = [&](int i) -> K { return base[taps[i]]; };
+  T result = radix_finish<T, K>(fetch, a.r);
+  out[(z * g.H + y) * g.W + x] = canonical(result);
+}
 
 }  // namespace net
 }  // namespace ndf

@@ -27,135 +27,17 @@ template <typename T, int N, int VFIX, int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     tile_network_kernel(const T* __restrict__ in, T* __restrict__ out,
                         const __grid_constant__ TileArgs a, const __grid_constant__ TapTable<N> taps) {
-  using K = typename KeyOf<T>::K;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Geom3& g = a.g;
-  const Tile& t = a.t;
-  long long* maps = reinterpret_cast<long long*>(smem_raw);
-  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
-  long long z, y0, x0;
-  tile_coords(a, z, y0, x0);
-  build_maps(maps, g, t, z, y0, x0);
-  __syncthreads();
-  const bool drop_inf = a.r.drop_inf;
-  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
-  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
-  __syncthreads();
-
-  const int tx = threadIdx.x % t.TW;
-  const int ty = threadIdx.x / t.TW;
-  const long long y = y0 + ty, x = x0 + tx;
-  if (ty >= t.TH || y >= g.H || x >= g.W) return;
-  const K* base = s + ty * t.SW + tx;
-  const int V = VFIX > 0 ? VFIX : a.r.count;
-  K k[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) k[i] = i < V ? base[taps.off[i]] : KeyOf<T>::kSentinel;
-  int nv = 0;
-#pragma unroll
-  for (int i = 0; i < N; ++i) nv += (i < V && k[i] != KeyOf<T>::kSentinel) ? 1 : 0;
-  batcher_sort<N>(k);
-  T result = network_finish<T, N, VFIX, MODE>(k, nv, a.r);
-  out[(z * g.H + y) * g.W + x] = canonical(result);
-}
-
-// ---------------------------------------------------------------------------
-// Bit-serial radix select: the k-th smallest retained key (k < nv). Bits
-// shared by every retained key (from their AND and OR) are skipped.
-template <typename K, typename Fetch>
-__device__ __forceinline__ K radix_select(Fetch&& fetch, int V, long long k, K and_v, K or_v) {
-  K diff = and_v ^ or_v;
-  if (diff == 0) return and_v;
-  const int bits = sizeof(K) * 8;
-  int top = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)diff) : __clz((int)diff));
-  K mask = top + 1 >= bits ? K(0) : ~((K(1) << (top + 1)) - 1);
-  K prefix = and_v & mask;
-  for (int b = top; b >= 0; --b) {
-    K bit = K(1) << b;
-    K m = mask | bit;
-    long long c = 0;
-    for (int i = 0; i < V; ++i) c += ((fetch(i) & m) == prefix) ? 1 : 0;
-    if (k >= c) {
-      k -= c;
-      prefix |= bit;
-    }
-    mask = m;
-  }
-  return prefix;
-}
-
-struct KeyStats {
-  int nv;
-};
-
-template <typename T, typename K, typename Fetch>
-__device__ __forceinline__ T radix_finish(Fetch&& fetch, const Reduce& r) {
-  using KO = KeyOf<T>;
-  const K sent = KO::kSentinel;
-  const int V = r.count;
-  int nv = 0;
-  K and_v = sent, or_v = 0, kmin = sent, kmax = 0;
-  for (int i = 0; i < V; ++i) {
-    K key = fetch(i);
-    if (key != sent) {
-      nv += 1;
-      and_v &= key;
-      or_v |= key;
-      kmin = key < kmin ? key : kmin;
-      kmax = key > kmax ? key : kmax;
-    }
-  }
-  const bool missing = r.omit ? (nv < r.min_count) : (nv != V);
-  if (missing || nv == 0) return nan_of(T());
-  auto sel = [&](long long kk) { return radix_select<K>(fetch, V, kk, and_v, or_v); };
-  switch (r.kind) {
-    case kMin:
-      return KO::value(kmin);
-    case kMax:
-      return KO::value(kmax);
-    case kRank:
-    case kRankHistogram:
-      if (r.param >= nv) return nan_of(T());
-      return KO::value(sel(r.param));
-    case kPercentile: {
-      if (r.q == 100.0) return KO::value(kmax);
-      PercentileRank pr = percentile_rank(r.q_fraction, nv);
-      double lo = (double)KO::value(sel(pr.lower));
-      double hi = pr.upper == pr.lower ? lo : (double)KO::value(sel(pr.upper));
-      return from_f64<T>(interpolate(lo, hi, pr.fraction));
-    }
-    default:
-      if (nv & 1) return KO::value(sel(nv / 2));
-      return median_of_two(KO::value(sel(nv / 2 - 1)), KO::value(sel(nv / 2)));
-  }
+  tile_network_body<T, N, VFIX, MODE>(in, out, a, blockIdx.x, smem_raw,
+                                      [&](int i) { return taps.off[i]; });
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     tile_radix_kernel(const T* __restrict__ in, T* __restrict__ out,
                       const __grid_constant__ TileArgs a, const int32_t* __restrict__ taps) {
-  using K = typename KeyOf<T>::K;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Geom3& g = a.g;
-  const Tile& t = a.t;
-  long long* maps = reinterpret_cast<long long*>(smem_raw);
-  K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
-  long long z, y0, x0;
-  tile_coords(a, z, y0, x0);
-  build_maps(maps, g, t, z, y0, x0);
-  __syncthreads();
-  const bool drop_inf = a.r.drop_inf;
-  const K outside = sample_key<T>((T)a.r.cval, drop_inf);
-  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
-  __syncthreads();
-  const int tx = threadIdx.x % t.TW;
-  const int ty = threadIdx.x / t.TW;
-  const long long y = y0 + ty, x = x0 + tx;
-  if (ty >= t.TH || y >= g.H || x >= g.W) return;
-  const K* base = s + ty * t.SW + tx;
-  auto fetch = [&](int i) -> K { return base[__ldg(taps + i)]; };
-  T result = radix_finish<T, K>(fetch, a.r);
-  out[(z * g.H + y) * g.W + x] = canonical(result);
+  tile_radix_body<T>(in, out, a, blockIdx.x, smem_raw, taps);
 }
 
 // ---------------------------------------------------------------------------
