@@ -58,8 +58,10 @@ def test_batch_matches_per_image_plans_and_oracle(gpu, oracle) -> None:
     for spec, image, out in zip(specs, images, d_out):
         got = out.cpu().numpy()
         kw = {k: spec[k] for k in ("size", "footprint", "omit_nan", "ignore_inf", "min_count",
-                                    "parameter", "percentile", "mode")}
-        plan = _core.Plan(image.shape, np.float32, spec["kind"], **kw)
+                                    "parameter", "percentile")}
+        if spec["footprint"] is not None:
+            kw["size"] = spec["footprint"].shape
+        plan = _core.Plan(image.shape, np.float32, spec["kind"], mode=[spec["mode"]] * 2, **kw)
         want = plan.run_host(image)
         plan.close()
         np.testing.assert_array_equal(bits(got), bits(want), err_msg=str(spec["kind"]))
