@@ -218,6 +218,121 @@ def cpu_baseline(image: np.ndarray, spec, budget_s: float = 3.0, threads: int | 
 
 
 # ---------------------------------------------------------------------------
+# Batched mixed workload: many float32 images of uneven sizes.
+
+def mixed_batch(count: int = 512, seed: int = 5, lo: int = 256, hi: int = 4096):
+    """Per image: sides log-uniform in [lo, hi] per axis, 1% NaN, 0.2%
+    outliers; window in {3, 5, ..., 15}; footprint box / tophat / ring(r, r+2);
+    filter nanmedian / nanpercentile 84 / nanstd."""
+    from ndfiltrs_gb300 import kernels
+
+    rng = np.random.default_rng(seed)
+    specs, images = [], []
+    for i in range(count):
+        h = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        w = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        image = rng.standard_normal((h, w), dtype=np.float32) * np.float32(10) + np.float32(1000)
+        image[rng.random((h, w), dtype=np.float32) < 0.01] = np.nan
+        outliers = rng.random((h, w), dtype=np.float32) < 0.002
+        image[outliers] = rng.uniform(2000.0, 60000.0, size=int(outliers.sum())).astype(np.float32)
+        window = int(rng.choice(np.arange(3, 16, 2)))
+        footprint_kind = rng.choice(["box", "tophat", "ring"])
+        footprint = None
+        if footprint_kind == "tophat":
+            footprint = kernels.tophat(window // 2, 2) != 0
+        elif footprint_kind == "ring":
+            outer = max(window // 2, 2)
+            footprint = kernels.ring(outer - 2, outer, 2) != 0
+        filt = rng.choice(["nanmedian", "percentile", "nanstd"])
+        kind = {"nanmedian": "median", "percentile": "percentile", "nanstd": "std"}[str(filt)]
+        specs.append(dict(shape=(h, w), kind=kind, size=(window, window), footprint=footprint,
+                          omit_nan=True, ignore_inf=kind == "std", min_count=1,
+                          parameter=1 if kind == "std" else 0, percentile=84.0, mode="reflect"))
+        images.append(image)
+    return specs, images
+
+
+def run_batch(args) -> None:
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import ndfiltrs_gb300 as nf
+
+    specs, images = mixed_batch(args.batch_images)
+    pixels = int(sum(im.size for im in images))
+    device = torch.device("cuda", 0)
+    d_in = [torch.from_numpy(im).to(device) for im in images]
+    d_plain = [torch.empty_like(t) for t in d_in]
+    d_batch = [torch.empty_like(t) for t in d_in]
+    stream = torch.cuda.Stream(device)
+    handle = stream.cuda_stream
+    plans = []
+    for spec in specs:
+        kw = dict(footprint=spec["footprint"], omit_nan=True, ignore_inf=spec["ignore_inf"],
+                  min_count=1, parameter=spec["parameter"], percentile=84.0, mode=["reflect"] * 2)
+        size = spec["footprint"].shape if spec["footprint"] is not None else spec["size"]
+        plans.append(nf.Plan(spec["shape"], np.float32, spec["kind"], size, **kw))
+    batch = nf.Batch(specs)
+    in_ptrs = [t.data_ptr() for t in d_in]
+    out_ptrs = [t.data_ptr() for t in d_batch]
+
+    def plain_step() -> None:
+        for plan, src, dst in zip(plans, d_in, d_plain):
+            plan.run_device(src.data_ptr(), dst.data_ptr(), handle)
+
+    def batch_step() -> None:
+        batch.run_device(in_ptrs, out_ptrs, handle)
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        start.record(stream)
+        for _ in range(steps):
+            fn()
+        end.record(stream)
+        torch.cuda.synchronize()
+        return start.elapsed_time(end) / steps, (time.perf_counter() - t0) / steps * 1e3
+
+    steps = max(3, min(args.steps, 20))
+    with ClockSampler(0) as clocks:
+        plain_ms, plain_wall = timed(plain_step, steps)
+        batch_ms, batch_wall = timed(batch_step, steps)
+    identical = all(torch.equal(a.view(torch.int32), b.view(torch.int32)) for a, b in zip(d_plain, d_batch))
+    line = {
+        "metric": METRIC,
+        "value": round(pixels / (batch_ms / 1e3) / 1e6, 3),
+        "unit": "Mpix/s",
+        "n_gpus": 1,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(batch_ms, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "batch_mixed", "images": len(images), "pixels": pixels,
+                   "families_launches": batch.launches},
+        "plain_per_call": {"value": round(pixels / (plain_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
+                           "ms_per_step": round(plain_ms, 3), "host_ms_per_step": round(plain_wall, 3),
+                           "launches": len(plans)},
+        "batched": {"value": round(pixels / (batch_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
+                    "ms_per_step": round(batch_ms, 3), "host_ms_per_step": round(batch_wall, 3),
+                    "images_per_s": round(len(images) / (batch_ms / 1e3), 1)},
+        "speedup_batched_vs_plain": round(plain_ms / batch_ms, 3),
+        "outputs_identical": bool(identical),
+        "clocks": clocks.summary(),
+        "gpu_launches": batch.launches,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # Precision study: nanstd against an exact (double-double) oracle.
 
 def precision_study(rows: int = 192, width: int = 4096) -> dict:
@@ -307,12 +422,16 @@ def main() -> None:
     parser.add_argument("--steps", type=int, default=200)
     parser.add_argument("--warmup", type=int, default=5)
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    parser.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    parser.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + ["batch_mixed"])
+    parser.add_argument("--batch-images", type=int, default=512)
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--precision", action=argparse.BooleanOptionalAction, default=True,
                         help="add the nanstd precision study to the line")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.workload == "batch_mixed":
+        run_batch(args)
+        return
     spec = WORKLOADS[args.workload]
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

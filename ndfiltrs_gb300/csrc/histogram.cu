@@ -253,54 +253,89 @@ __device__ __forceinline__ int hist_select(WarpHist& h, int k) {
   return 0;
 }
 
-// One add (+1) or remove (-1) of a code.
-__device__ __forceinline__ void update(const WarpHist& h, int c, int sign, int& kept, int& below,
-                                       int& nans) {
-  const bool valid = c < (int)kPropagated;
-  if (valid) atomicXor(&h.words[c >> 5], 1u << (c & 31));
-  kept += valid ? sign : 0;
-  below += (valid && c < h.pivot) ? sign : 0;
-  nans += c == (int)kPropagated ? sign : 0;
+// Rank of the first set bit above `rank` (the next retained sample in
+// order); the caller guarantees one exists. Scans 1024 ranks per warp step.
+__device__ __forceinline__ int next_set_bit(const WarpHist& h, int rank) {
+  const int lane = threadIdx.x & 31;
+  const int w_first = rank >> 5;
+  unsigned int first = h.words[w_first] & ~((2u << (rank & 31)) - 1u);
+  if (rank % 32 == 31) first = 0u;
+  if (first) return (w_first << 5) + __ffs(first) - 1;
+  for (int w0 = w_first + 1; w0 < h.nwords; w0 += 32) {
+    const int wi = w0 + lane;
+    const unsigned int word = wi < h.nwords ? h.words[wi] : 0u;
+    const unsigned int ball = __ballot_sync(0xffffffffu, word != 0u);
+    if (ball) {
+      const int L = __ffs(ball) - 1;
+      const unsigned int w = __shfl_sync(0xffffffffu, word, L);
+      return ((w0 + L) << 5) + __ffs(w) - 1;
+    }
+  }
+  return rank;
 }
 
-__device__ __forceinline__ void finish_update(WarpHist& h, int kept, int below, int nans) {
-  h.count += __reduce_add_sync(0xffffffffu, kept);
-  h.below += __reduce_add_sync(0xffffffffu, below);
-  h.nan += __reduce_add_sync(0xffffffffu, nans);
+// Per-step bookkeeping of a lane: retained, below-pivot and propagated-NaN
+// deltas.
+struct StepDelta {
+  int kept = 0, below = 0, nans = 0;
+};
+
+template <bool PROPAGATE>
+__device__ __forceinline__ void update(const WarpHist& h, int c, int sign, StepDelta& d) {
+  const bool valid = c < (int)kPropagated;
+  if (valid) atomicXor(&h.words[c >> 5], 1u << (c & 31));
+  const int inc = valid ? sign : 0;
+  d.kept += inc;
+  d.below += c < h.pivot ? inc : 0;
+  if (PROPAGATE) d.nans += c == (int)kPropagated ? sign : 0;
+}
+
+// Apply a step's deltas with warp reductions. Under the omit policy the
+// retained and below-pivot deltas share one reduction in two 16-bit halves
+// biased by 1024 per lane, valid while a lane handles fewer than 512 codes
+// (`narrow`); wider faces use one reduction per counter.
+template <bool PROPAGATE>
+__device__ __forceinline__ void finish_update(WarpHist& h, const StepDelta& d, bool narrow) {
+  if (PROPAGATE || !narrow) {
+    h.count += __reduce_add_sync(0xffffffffu, d.kept);
+    h.below += __reduce_add_sync(0xffffffffu, d.below);
+    if (PROPAGATE) h.nan += __reduce_add_sync(0xffffffffu, d.nans);
+  } else {
+    const unsigned int packed =
+        (unsigned int)(d.kept + 1024) | ((unsigned int)(d.below + 1024) << 16);
+    const unsigned int sum = __reduce_add_sync(0xffffffffu, packed);
+    h.count += (int)(sum & 0xFFFFu) - 32 * 1024;
+    h.below += (int)(sum >> 16) - 32 * 1024;
+  }
   __syncwarp();
 }
 
 // Remove the codes of one face and add those of another (n codes each,
-// `stride` apart, in shared memory). All loads are issued before the atomics.
+// `stride` apart, in shared memory).
+template <bool PROPAGATE>
 __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, int add_start, int n,
                                      int stride, WarpHist& h) {
   const int lane = threadIdx.x & 31;
-  int kept = 0, below = 0, nans = 0;
-  for (int i0 = 0; i0 < n; i0 += 128) {
-    int rc[4], ac[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int i = i0 + j * 32 + lane;
-      rc[j] = i < n ? (int)codes[remove_start + i * stride] : (int)kOmitted;
-      ac[j] = i < n ? (int)codes[add_start + i * stride] : (int)kOmitted;
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      update(h, rc[j], -1, kept, below, nans);
-      update(h, ac[j], +1, kept, below, nans);
-    }
+  StepDelta d;
+  for (int i = lane; i < n; i += 32) {
+    const int rc = codes[remove_start + i * stride];
+    const int ac = codes[add_start + i * stride];
+    update<PROPAGATE>(h, rc, -1, d);
+    update<PROPAGATE>(h, ac, +1, d);
   }
-  finish_update(h, kept, below, nans);
+  finish_update<PROPAGATE>(h, d, n <= 16 * 1024);
 }
 
 // Add every code of a kh x kw box (the first window of a warp's walk).
+template <bool PROPAGATE>
 __device__ __forceinline__ void add_box(const uint16_t* codes, int start, int kh, int kw, int SW,
                                        WarpHist& h) {
   const int lane = threadIdx.x & 31;
-  int kept = 0, below = 0, nans = 0;
-  for (int ky = 0; ky < kh; ++ky)
-    for (int i = lane; i < kw; i += 32) update(h, codes[start + ky * SW + i], +1, kept, below, nans);
-  finish_update(h, kept, below, nans);
+  for (int ky = 0; ky < kh; ++ky) {
+    StepDelta d;
+    for (int i = lane; i < kw; i += 32) update<PROPAGATE>(h, codes[start + ky * SW + i], +1, d);
+    finish_update<PROPAGATE>(h, d, kw <= 16 * 1024);
+  }
 }
 
 template <typename T>
@@ -331,11 +366,40 @@ __device__ __forceinline__ T hist_finish(WarpHist& h, const HistArgs& a,
   }
   if (h.count & 1) return value_at(h.count / 2);
   const int lo = hist_select(h, h.count / 2 - 1);
-  const int hi = hist_select(h, h.count / 2);
+  const int hi = next_set_bit(h, lo);
   if constexpr (sizeof(T) == 4) {
     return midpoint_f32(KO::value(sorted[lo]), KO::value(sorted[hi]));
   } else {
     return midpoint(KO::value(sorted[lo]), KO::value(sorted[hi]));
+  }
+}
+
+// A warp's boustrophedon walk over columns [c_begin, c_end) of its tile.
+template <typename T, bool PROPAGATE>
+__device__ __forceinline__ void walk(const uint16_t* codes, int c_begin, int c_end, int th_eff, int kh,
+                                     int kw, int SW, long long y0, long long x0, const Geom3& g,
+                                     const HistArgs& a, const typename KeyOf<T>::K* sorted,
+                                     T* __restrict__ out, WarpHist& h) {
+  const int lane = threadIdx.x & 31;
+  add_box<PROPAGATE>(codes, c_begin, kh, kw, SW, h);
+  int row = 0;
+  int dir = 1;
+  for (int c = c_begin; c < c_end; ++c) {
+    for (int i = 0; i < th_eff; ++i) {
+      T result = hist_finish<T>(h, a, sorted);
+      if (lane == 0) out[(y0 + row) * g.W + x0 + c] = canonical(result);
+      if (i + 1 < th_eff) {
+        if (dir > 0) {
+          step<PROPAGATE>(codes, row * SW + c, (row + kh) * SW + c, kw, 1, h);
+          ++row;
+        } else {
+          step<PROPAGATE>(codes, (row + kh - 1) * SW + c, (row - 1) * SW + c, kw, 1, h);
+          --row;
+        }
+      }
+    }
+    if (c + 1 < c_end) step<PROPAGATE>(codes, row * SW + c, row * SW + c + kw, kh, SW, h);
+    dir = -dir;
   }
 }
 
@@ -460,27 +524,10 @@ __global__ void __launch_bounds__(kHThreads, 1)
     __syncwarp();
     const uint16_t* codes = codes_s;
     const int kh = g.kh, kw = g.kw, SW = a.SW;
-    if (c_begin < c_end) {
-      add_box(codes, c_begin, kh, kw, SW, h);
-      int row = 0;
-      int dir = 1;
-      for (int c = c_begin; c < c_end; ++c) {
-        for (int i = 0; i < th_eff; ++i) {
-          T result = hist_finish<T>(h, a, sorted);
-          if (lane == 0) out[(y0 + row) * g.W + x0 + c] = canonical(result);
-          if (i + 1 < th_eff) {
-            if (dir > 0) {
-              step(codes, row * SW + c, (row + kh) * SW + c, kw, 1, h);
-              ++row;
-            } else {
-              step(codes, (row + kh - 1) * SW + c, (row - 1) * SW + c, kw, 1, h);
-              --row;
-            }
-          }
-        }
-        if (c + 1 < c_end) step(codes, row * SW + c, row * SW + c + kw, kh, SW, h);
-        dir = -dir;
-      }
+    if (c_begin < c_end && !a.r.omit) {
+      walk<T, true>(codes, c_begin, c_end, th_eff, kh, kw, SW, y0, x0, g, a, sorted, out, h);
+    } else if (c_begin < c_end) {
+      walk<T, false>(codes, c_begin, c_end, th_eff, kh, kw, SW, y0, x0, g, a, sorted, out, h);
     }
     __syncthreads();
   }
