@@ -172,6 +172,27 @@ int ndf_batch_run(ndf_batch* batch, const void* const* d_in, void* const* d_out,
 /* Number of persistent launches one ndf_batch_run enqueues. */
 int32_t ndf_batch_launches(const ndf_batch* batch);
 
+/* Allocation-free histogram filter over caller-owned device buffers. No
+ * counterpart in the reference. For callers that cannot let a library
+ * allocate device memory (code running during stream capture, frameworks
+ * that own all device memory, real-time pipelines that cannot absorb an
+ * allocation's implicit synchronization): the sliding rank-histogram kernel's
+ * sort scratch lives in a static 16 MiB device array of the library, so this
+ * call never runs cudaMalloc, cudaFree or any allocating routine. 1-D and 2-D
+ * rectangular windows; `kind` is an order statistic (median, rank, min, max,
+ * percentile; histogram or not); arguments mean what they mean in
+ * ndf_filter_desc. Enqueues on `stream` and returns. The array is shared by
+ * every call and keeps the last call's contents (the kernel overwrites what
+ * it reads, nothing needs clearing); calls that overlap on the GPU race on
+ * it. The first call on a device looks up the array's address with that
+ * device current: make it before any stream capture. A window whose sort slot
+ * does not fit in the array returns NDF_ERR_MEMORY. */
+int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32_t dtype, int32_t ndim,
+                                 const uint64_t* shape, const uint64_t* size, const int64_t* origin,
+                                 const int32_t* modes, double cval, int32_t kind, int32_t omit_nan,
+                                 int32_t ignore_inf, uint64_t min_count, uint64_t parameter,
+                                 double percentile, void* stream);
+
 /* Number of SMs, device name and compute capability of device 0. */
 int ndf_device_info(int32_t* sm_count, int32_t* major, int32_t* minor, char* name,
                     size_t name_capacity);

@@ -23,11 +23,19 @@
 //    warp step from a tracked pivot (the previous window's median) and ends
 //    with a 5-step select in the final word.
 #include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
 
+#include "../../include/ndfiltrs_gb300.h"
 #include "common.cuh"
 #include "plan.h"
 
 namespace ndf {
+
+int fail(int code, const std::string& message);
+int cuda_fail(cudaError_t e, const char* what);
+
 namespace {
 
 constexpr int kHThreads = 512;
@@ -594,6 +602,23 @@ HistChoice choose_tile(const Geom3& g, size_t key_bytes) {
   return best;
 }
 
+HistArgs make_args_core(const Geom3& g, int TW, int TH, int dtype, const Reduce& r) {
+  HistArgs a{};
+  a.g = g;
+  a.TW = TW;
+  a.TH = TH;
+  a.SW = a.TW + a.g.kw - 1;
+  a.SH = a.TH + a.g.kh - 1;
+  a.S = a.SW * a.SH;
+  a.tiles_x = (a.g.W + a.TW - 1) / a.TW;
+  a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
+  a.cols_per_warp = (a.TW + kHWarps - 1) / kHWarps;
+  a.words = (a.S + 31) / 32;
+  a.slot_bytes = dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
+  a.r = r;
+  return a;
+}
+
 HistArgs make_args(const Plan& p) {
   HistArgs a{};
   a.g = p.tile.g;
@@ -678,4 +703,184 @@ cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStrea
   return launch_t<double>(p, (const double*)in, (double*)out, s);
 }
 
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the histogram kernel.
+//
+// Some callers cannot let a library allocate device memory: code that runs
+// while a CUDA stream is being captured (cudaMalloc is not allowed there),
+// frameworks that own all device memory through their own pool, and real-time
+// pipelines where an allocation's implicit device synchronization is not
+// acceptable. For them, ndf_histogram_filter_noalloc takes the caller's
+// device input and output and keeps its only scratch (the per-block sort
+// slots) in the file-scope array below, so it never calls cudaMalloc,
+// cudaFree or any allocating routine.
+//
+// Limits and sharing:
+//  * the array holds kNoAllocScratchBytes (16 MiB) on every GPU that loads
+//    the library, until the process exits;
+//  * the number of concurrently working thread blocks is the number of sort
+//    slots that fit in it (a slot is 2 x S keys + 2 x S u32 payloads for a
+//    support of S samples), capped by the device's resident capacity; a
+//    support whose slot does not fit is rejected with NDF_ERR_MEMORY;
+//  * every call shares the array and it keeps the last call's contents; the
+//    kernel writes every slot word before reading it, so nothing needs
+//    clearing; calls that overlap on the GPU (other streams, other host
+//    threads) race on it and must be serialized by the caller;
+//  * the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress) with that device current; make that first call
+//    before any stream capture.
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+struct NoAllocDevices {
+  std::mutex lock;
+  void* address[kMaxDevices] = {};
+};
+
+NoAllocDevices& noalloc_devices() {
+  static NoAllocDevices d;
+  return d;
+}
+
+// Device address of g_noalloc_scratch on the current device (set-up once
+// per device, with that device current).
+cudaError_t noalloc_scratch(int device, void** out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  NoAllocDevices& d = noalloc_devices();
+  std::lock_guard<std::mutex> guard(d.lock);
+  if (!d.address[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    d.address[device] = ptr;
+  }
+  *out = d.address[device];
+  return cudaSuccess;
+}
+
+int noalloc_fail(int code, const char* message) {
+  return fail(code, message);
+}
+
+}  // namespace
 }  // namespace ndf
+
+extern "C" int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32_t dtype, int32_t ndim,
+                                            const uint64_t* shape, const uint64_t* size,
+                                            const int64_t* origin, const int32_t* modes, double cval,
+                                            int32_t kind, int32_t omit_nan, int32_t ignore_inf,
+                                            uint64_t min_count, uint64_t parameter, double percentile,
+                                            void* stream) {
+  using namespace ndf;
+  if (dtype != NDF_FLOAT32 && dtype != NDF_FLOAT64)
+    return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION, "array dtype must be float32 or float64");
+  if (ndim < 1 || ndim > 2)
+    return noalloc_fail(NDF_ERR_UNSUPPORTED, "the allocation-free histogram filter takes 1-D or 2-D arrays");
+  if (!shape || !size || !origin || !modes)
+    return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION, "missing shape, size, origin or mode");
+  if (kind != kMedian && kind != kMedianNetwork && kind != kMedianHistogram && kind != kRank &&
+      kind != kRankHistogram && kind != kMin && kind != kMax && kind != kPercentile)
+    return noalloc_fail(NDF_ERR_UNSUPPORTED, "the allocation-free histogram filter computes order statistics");
+  long long shp[2] = {1, 1}, sz[2] = {1, 1}, org[2] = {0, 0};
+  int md[2] = {kNearest, kNearest};
+  const int pad = 2 - ndim;
+  unsigned long long volume = 1, n_out = 1;
+  for (int a = 0; a < ndim; ++a) {
+    if (modes[a] < 0 || modes[a] > 4) return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported boundary mode");
+    if (size[a] == 0) return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION, "window sizes must be positive");
+    if (size[a] > 65534 || shape[a] > (1ull << 40))
+      return noalloc_fail(NDF_ERR_OVERFLOW, "shape or index arithmetic overflowed");
+    const long long length = (long long)size[a];
+    if (origin[a] < -(length / 2) || origin[a] > (length - 1) / 2)
+      return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION,
+                          "origin must satisfy -(size // 2) <= origin <= (size - 1) // 2");
+    shp[a + pad] = (long long)shape[a];
+    sz[a + pad] = length;
+    org[a + pad] = origin[a];
+    md[a + pad] = modes[a];
+    volume *= size[a];
+    n_out *= shape[a];
+  }
+  if (omit_nan && (min_count == 0 || min_count > volume))
+    return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION,
+                        "min_count must be between 1 and the number of window elements");
+  if (kind == kPercentile && (!std::isfinite(percentile) || percentile < 0.0 || percentile > 100.0))
+    return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION, "percentile must be finite and between zero and 100");
+  if (n_out == 0) return NDF_OK;
+  if (!d_in || !d_out) return noalloc_fail(NDF_ERR_LENGTH_MISMATCH, "missing input or output buffer");
+  Geom3 g{};
+  g.D = 1;
+  g.H = shp[0];
+  g.W = shp[1];
+  g.kd = 1;
+  g.kh = (int)sz[0];
+  g.kw = (int)sz[1];
+  g.az = 0;
+  g.ay = (int)(sz[0] / 2 + org[0]);
+  g.ax = (int)(sz[1] / 2 + org[1]);
+  g.mz = kNearest;
+  g.my = md[0];
+  g.mx = md[1];
+  Reduce r{};
+  r.kind = kind;
+  r.omit = omit_nan != 0;
+  r.drop_inf = r.omit && ignore_inf != 0;
+  r.count = (int)std::min<unsigned long long>(volume, 1ull << 30);
+  r.min_count = r.omit ? (long long)min_count : 1;
+  r.param = (long long)std::min<uint64_t>(parameter, (uint64_t)(1ull << 62));
+  r.q = percentile;
+  r.q_fraction = percentile / 100.0;
+  r.cval = dtype == NDF_FLOAT32 ? (double)(float)cval : cval;
+  HistChoice c = choose_tile(g, dtype == 0 ? 4 : 8);
+  if (c.TW == 0) return noalloc_fail(NDF_ERR_UNSUPPORTED, "window too large for the histogram kernel");
+  HistArgs a = make_args_core(g, c.TW, c.TH, dtype, r);
+  if ((size_t)a.slot_bytes > kNoAllocScratchBytes)
+    return noalloc_fail(NDF_ERR_MEMORY,
+                        "the window's sort slot exceeds the 16 MiB allocation-free scratch");
+  int device = 0, sm_count = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return noalloc_fail(NDF_ERR_NO_DEVICE, "no usable CUDA device");
+  }
+  const size_t smem = smem_bytes_for(a.S, c.sdec, dtype == 0 ? 4 : 8);
+  if (smem > (size_t)optin) return noalloc_fail(NDF_ERR_UNSUPPORTED, "window too large for shared memory");
+  void* scratch = nullptr;
+  e = noalloc_scratch(device, &scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  const void* kernel = dtype == 0 ? kernel_for<float>(c.sdec) : kernel_for<double>(c.sdec);
+  e = allow_max_smem(kernel);
+  int per_sm = 1;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kHThreads, smem);
+  if (e != cudaSuccess) return cuda_fail(e, "histogram (allocation-free) set-up");
+  long long slots = (long long)(kNoAllocScratchBytes / (size_t)a.slot_bytes);
+  long long grid = std::min<long long>(std::min<long long>(a.tiles, slots),
+                                       (long long)std::max(per_sm, 1) * sm_count);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == 0) {
+    if (c.sdec)
+      histogram_kernel<float, true><<<(unsigned)grid, kHThreads, smem, s>>>(
+          (const float*)d_in, (float*)d_out, a, (unsigned char*)scratch);
+    else
+      histogram_kernel<float, false><<<(unsigned)grid, kHThreads, smem, s>>>(
+          (const float*)d_in, (float*)d_out, a, (unsigned char*)scratch);
+  } else {
+    if (c.sdec)
+      histogram_kernel<double, true><<<(unsigned)grid, kHThreads, smem, s>>>(
+          (const double*)d_in, (double*)d_out, a, (unsigned char*)scratch);
+    else
+      histogram_kernel<double, false><<<(unsigned)grid, kHThreads, smem, s>>>(
+          (const double*)d_in, (double*)d_out, a, (unsigned char*)scratch);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "histogram (allocation-free)");
+  return NDF_OK;
+}
