@@ -258,7 +258,10 @@ __device__ __forceinline__ bool moments_fp32c_f64(FetchT&& fetch, const Reduce& 
   Triple p{0.0f, 0.0f, 0.0f};
   bool have_p = false;
   float maxdev = 0.0f;
-  SumFF s1, s2;
+  // Blocked float-float sums: 32 terms per inner sum, then an outer sum, so
+  // rounding errors accumulate over ~2 * sqrt-like chains instead of V.
+  SumFF s1, s2, b1, b2;
+  int block = 0;
   for (int i = 0; i < V; ++i) {
     Triple x = fetch(i);
     // NaN / infinity / out-of-range values are staged with x.m as a marker:
@@ -293,13 +296,22 @@ __device__ __forceinline__ bool moments_fp32c_f64(FetchT&& fetch, const Reduce& 
     float dh = __fadd_rn(sh, se);
     float dl = __fsub_rn(se, __fsub_rn(dh, sh));
     maxdev = fmaxf(maxdev, fabsf(dh));
-    s1.add(dh, dl);
+    b1.add(dh, dl);
     float sq = __fmul_rn(dh, dh);
     float sqe = fmaf(dh, dh, -sq);
     sqe = fmaf(__fmul_rn(2.0f, dh), dl, sqe);
     sqe = fmaf(dl, dl, sqe);
-    s2.add(sq, sqe);
+    b2.add(sq, sqe);
+    if (++block == 32) {
+      s1.add(b1.hi, b1.lo);
+      s2.add(b2.hi, b2.lo);
+      b1 = SumFF{};
+      b2 = SumFF{};
+      block = 0;
+    }
   }
+  s1.add(b1.hi, b1.lo);
+  s2.add(b2.hi, b2.lo);
   if (decide_special(r, n, nan, pinf, ninf, out)) return true;
   if (unsafe) return false;
   if (maxdev != 0.0f && (maxdev < kSafeLow || maxdev > kSafeHigh || !isfinite(maxdev))) return false;
