@@ -16,12 +16,14 @@
 //    digits, warp match_any ranking for stability, digits on which every
 //    retained key agrees are skipped) through a per-block scratch slot in
 //    global memory (L2-resident); rank codes are u16 (support <= 65534);
-//  * sliding: each warp owns a strip of output columns and walks it in
-//    boustrophedon order; a vertical step removes one support row segment
-//    (kw codes) and adds another, spread over the 32 lanes with shared-memory
-//    atomics on the warp's private bitset; a selection scans 1024 ranks per
-//    warp step from a tracked pivot (the previous window's median) and ends
-//    with a 5-step select in the final word.
+//  * sliding: each half-warp (16 lanes) owns a strip of output columns and
+//    walks it in boustrophedon order, so a warp advances two windows per
+//    step; a vertical step removes one support row segment (kw codes) and
+//    adds another, spread over the 16 lanes with shared-memory atomics on the
+//    half-warp's private bitset; a selection scans 512 ranks per step from a
+//    tracked pivot (the previous window's order statistic) and ends with a
+//    5-step select in the final word. Tile widths are multiples of 32 columns,
+//    so every half-warp's columns lie inside the tile's support.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -187,12 +189,19 @@ __device__ __forceinline__ int select_in_word32(unsigned int word, int k) {
   return position;
 }
 
-// Bit histogram of one warp. `pivot` is a word-aligned rank and `below`
-// the number of window samples whose rank is below it; both are uniform
-// across the warp. A selection scans 32 words (1024 ranks) at a time from
-// the pivot and leaves the pivot at the word it found, so the next window's
-// median (a few ranks away) is usually found in one scan.
-struct WarpHist {
+// Each half-warp (16 lanes, a "segment") owns one bit histogram, so a warp
+// advances two windows per step. `pivot` is a word-aligned rank and `below`
+// the number of window samples ranked below it; both are uniform within the
+// segment. A selection scans 16 words (512 ranks) per iteration from the
+// pivot and leaves the pivot at the word it found, so the next window's
+// order statistic (a few ranks away) is usually found in one iteration.
+// Every loop that contains warp-synchronous operations runs until both
+// segments are done, so the two halves stay converged.
+constexpr int kSeg = 16;
+constexpr int kSegs = kHThreads / kSeg;
+constexpr unsigned int kFull = 0xffffffffu;
+
+struct SegHist {
   unsigned int* words;
   int nwords;
   int pivot;  // multiple of 32
@@ -201,85 +210,101 @@ struct WarpHist {
   int nan;    // propagated NaN samples in the window
 };
 
-__device__ __forceinline__ unsigned int warp_inclusive_scan(unsigned int v) {
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ int seg_lane() { return threadIdx.x & (kSeg - 1); }
+
+__device__ __forceinline__ unsigned int seg_ballot(bool p) {
+  return (__ballot_sync(kFull, p) >> (threadIdx.x & kSeg)) & 0xFFFFu;
+}
+
+__device__ __forceinline__ int seg_sum(int v) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned int t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
+  for (int o = kSeg / 2; o >= 1; o >>= 1) v += __shfl_xor_sync(kFull, v, o, kSeg);
+  return v;
+}
+
+__device__ __forceinline__ unsigned int seg_scan(unsigned int v) {
+  const int hl = seg_lane();
+#pragma unroll
+  for (int o = 1; o < kSeg; o <<= 1) {
+    const unsigned int t = __shfl_up_sync(kFull, v, o, kSeg);
+    if (hl >= o) v += t;
   }
   return v;
 }
 
-// Rank of the k-th (0-based) set bit; k < h.count.
-__device__ __forceinline__ int hist_select(WarpHist& h, int k) {
-  const int lane = threadIdx.x & 31;
-  int w0 = h.pivot >> 5;
-  if (k >= h.below) {
-    int base = h.below;  // set bits below word w0
-    for (int guard = 0; guard < 4096; ++guard) {
-      const int wi = w0 + lane;
-      const unsigned int word = wi < h.nwords ? h.words[wi] : 0u;
-      const unsigned int pc = __popc(word);
-      const unsigned int incl = warp_inclusive_scan(pc);
-      const int total = (int)__shfl_sync(0xffffffffu, incl, 31);
-      if (base + total > k || w0 + 32 >= h.nwords) {
-        const unsigned int ball = __ballot_sync(0xffffffffu, base + (int)incl > k);
-        const int L = ball ? __ffs(ball) - 1 : 31;
-        const int before = base + (int)__shfl_sync(0xffffffffu, incl - pc, L);
-        const unsigned int w = __shfl_sync(0xffffffffu, word, L);
-        h.pivot = (w0 + L) * 32;
-        h.below = before;
-        return h.pivot + select_in_word32(w, k - before);
-      }
-      base += total;
-      w0 += 32;
-    }
-    return 0;
-  }
-  int top = h.below;  // set bits below word w0
-  for (int guard = 0; guard < 4096; ++guard) {
-    const int lo = w0 - 32;
-    const int wi = lo + lane;
-    const unsigned int word = wi >= 0 ? h.words[wi] : 0u;
-    const unsigned int pc = __popc(word);
-    const unsigned int incl = warp_inclusive_scan(pc);
-    const int total = (int)__shfl_sync(0xffffffffu, incl, 31);
-    const int start = top - total;  // set bits below word lo
-    if (start <= k || lo <= 0) {
-      const unsigned int ball = __ballot_sync(0xffffffffu, start + (int)incl > k);
-      const int L = ball ? __ffs(ball) - 1 : 31;
-      const int before = start + (int)__shfl_sync(0xffffffffu, incl - pc, L);
-      const unsigned int w = __shfl_sync(0xffffffffu, word, L);
-      h.pivot = (lo + L) * 32;
-      h.below = before;
-      return h.pivot + select_in_word32(w, k - before);
-    }
-    top = start;
-    w0 = lo;
-  }
-  return 0;
+template <typename V>
+__device__ __forceinline__ V seg_bcast(V v, int src) {
+  return __shfl_sync(kFull, v, src, kSeg);
 }
 
-// Rank of the first set bit above `rank` (the next retained sample in
-// order); the caller guarantees one exists. Scans 1024 ranks per warp step.
-__device__ __forceinline__ int next_set_bit(const WarpHist& h, int rank) {
-  const int lane = threadIdx.x & 31;
-  const int w_first = rank >> 5;
-  unsigned int first = h.words[w_first] & ~((2u << (rank & 31)) - 1u);
-  if (rank % 32 == 31) first = 0u;
-  if (first) return (w_first << 5) + __ffs(first) - 1;
-  for (int w0 = w_first + 1; w0 < h.nwords; w0 += 32) {
-    const int wi = w0 + lane;
+// Rank of the k-th (0-based) set bit of the segment's histogram; `active`
+// false runs the loop for convergence only and leaves the state untouched.
+__device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
+  const int hl = seg_lane();
+  const bool fwd = k >= h.below;
+  int w0 = h.pivot >> 5;
+  int base = h.below;  // set bits below word w0
+  bool found = !active;
+  int result = 0;
+  for (int guard = 0; guard < 8192; ++guard) {
+    const int lo = fwd ? w0 : w0 - kSeg;
+    const int wi = lo + hl;
+    const unsigned int word = (wi >= 0 && wi < h.nwords) ? h.words[wi] : 0u;
+    const unsigned int pc = __popc(word);
+    const unsigned int incl = seg_scan(pc);
+    const int total = (int)seg_bcast(incl, kSeg - 1);
+    const int start = fwd ? base : base - total;  // set bits below word lo
+    const bool edge = fwd ? (lo + kSeg >= h.nwords) : (lo <= 0);
+    const unsigned int ball = seg_ballot(start + (int)incl > k);
+    const int L = ball ? __ffs(ball) - 1 : kSeg - 1;
+    const int before = start + (int)seg_bcast(incl - pc, L);
+    const unsigned int w = seg_bcast(word, L);
+    if (!found) {
+      if ((fwd ? start + total > k : start <= k) || edge) {
+        h.pivot = max(lo + L, 0) * 32;
+        h.below = before;
+        result = h.pivot + select_in_word32(w, k - before);
+        found = true;
+      } else if (fwd) {
+        base += total;
+        w0 += kSeg;
+      } else {
+        base = start;
+        w0 = lo;
+      }
+    }
+    if (!__any_sync(kFull, !found)) break;
+  }
+  return result;
+}
+
+// Rank of the first set bit above `rank` (the next retained sample).
+__device__ __forceinline__ int seg_next(const SegHist& h, int rank, bool active) {
+  const int hl = seg_lane();
+  const int wf = rank >> 5;
+  unsigned int first = (rank & 31) == 31 ? 0u : (h.words[wf] & ~((2u << (rank & 31)) - 1u));
+  bool found = !active || first != 0u;
+  int result = first ? (wf << 5) + __ffs(first) - 1 : rank;
+  int w0 = wf + 1;
+  for (int guard = 0; guard < 8192; ++guard) {
+    if (!__any_sync(kFull, !found)) break;
+    const int wi = w0 + hl;
     const unsigned int word = wi < h.nwords ? h.words[wi] : 0u;
-    const unsigned int ball = __ballot_sync(0xffffffffu, word != 0u);
-    if (ball) {
-      const int L = __ffs(ball) - 1;
-      const unsigned int w = __shfl_sync(0xffffffffu, word, L);
-      return ((w0 + L) << 5) + __ffs(w) - 1;
+    const unsigned int ball = seg_ballot(word != 0u);
+    const int L = ball ? __ffs(ball) - 1 : 0;
+    const unsigned int w = seg_bcast(word, L);
+    if (!found) {
+      if (ball) {
+        result = ((w0 + L) << 5) + __ffs(w) - 1;
+        found = true;
+      } else if (w0 + kSeg >= h.nwords) {
+        found = true;
+      } else {
+        w0 += kSeg;
+      }
     }
   }
-  return rank;
+  return result;
 }
 
 // Per-step bookkeeping of a lane: retained, below-pivot and propagated-NaN
@@ -289,7 +314,7 @@ struct StepDelta {
 };
 
 template <bool PROPAGATE>
-__device__ __forceinline__ void update(const WarpHist& h, int c, int sign, StepDelta& d) {
+__device__ __forceinline__ void update(const SegHist& h, int c, int sign, StepDelta& d) {
   const bool valid = c < (int)kPropagated;
   if (valid) atomicXor(&h.words[c >> 5], 1u << (c & 31));
   const int inc = valid ? sign : 0;
@@ -298,22 +323,20 @@ __device__ __forceinline__ void update(const WarpHist& h, int c, int sign, StepD
   if (PROPAGATE) d.nans += c == (int)kPropagated ? sign : 0;
 }
 
-// Apply a step's deltas with warp reductions. Under the omit policy the
-// retained and below-pivot deltas share one reduction in two 16-bit halves
-// biased by 1024 per lane, valid while a lane handles fewer than 512 codes
-// (`narrow`); wider faces use one reduction per counter.
+// Apply a step's deltas. Under the omit policy the retained and below-pivot
+// deltas share one reduction in two 16-bit halves biased by 1024 per lane,
+// valid while a lane handles fewer than 512 codes (`narrow`).
 template <bool PROPAGATE>
-__device__ __forceinline__ void finish_update(WarpHist& h, const StepDelta& d, bool narrow) {
+__device__ __forceinline__ void finish_update(SegHist& h, const StepDelta& d, bool narrow) {
   if (PROPAGATE || !narrow) {
-    h.count += __reduce_add_sync(0xffffffffu, d.kept);
-    h.below += __reduce_add_sync(0xffffffffu, d.below);
-    if (PROPAGATE) h.nan += __reduce_add_sync(0xffffffffu, d.nans);
+    h.count += seg_sum(d.kept);
+    h.below += seg_sum(d.below);
+    if (PROPAGATE) h.nan += seg_sum(d.nans);
   } else {
-    const unsigned int packed =
-        (unsigned int)(d.kept + 1024) | ((unsigned int)(d.below + 1024) << 16);
-    const unsigned int sum = __reduce_add_sync(0xffffffffu, packed);
-    h.count += (int)(sum & 0xFFFFu) - 32 * 1024;
-    h.below += (int)(sum >> 16) - 32 * 1024;
+    const int packed = (d.kept + 1024) | ((d.below + 1024) << 16);
+    const unsigned int sum = (unsigned int)seg_sum(packed);
+    h.count += (int)(sum & 0xFFFFu) - kSeg * 1024;
+    h.below += (int)(sum >> 16) - kSeg * 1024;
   }
   __syncwarp();
 }
@@ -322,80 +345,101 @@ __device__ __forceinline__ void finish_update(WarpHist& h, const StepDelta& d, b
 // `stride` apart, in shared memory).
 template <bool PROPAGATE>
 __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, int add_start, int n,
-                                     int stride, WarpHist& h) {
-  const int lane = threadIdx.x & 31;
+                                     int stride, SegHist& h) {
+  const int hl = seg_lane();
   StepDelta d;
-  for (int i = lane; i < n; i += 32) {
+  for (int i = hl; i < n; i += kSeg) {
     const int rc = codes[remove_start + i * stride];
     const int ac = codes[add_start + i * stride];
     update<PROPAGATE>(h, rc, -1, d);
     update<PROPAGATE>(h, ac, +1, d);
   }
-  finish_update<PROPAGATE>(h, d, n <= 16 * 1024);
+  finish_update<PROPAGATE>(h, d, n <= 8 * 1024);
 }
 
-// Add every code of a kh x kw box (the first window of a warp's walk).
+// Add every code of a kh x kw box (the first window of a segment's walk).
 template <bool PROPAGATE>
 __device__ __forceinline__ void add_box(const uint16_t* codes, int start, int kh, int kw, int SW,
-                                       WarpHist& h) {
-  const int lane = threadIdx.x & 31;
+                                       SegHist& h) {
+  const int hl = seg_lane();
   for (int ky = 0; ky < kh; ++ky) {
     StepDelta d;
-    for (int i = lane; i < kw; i += 32) update<PROPAGATE>(h, codes[start + ky * SW + i], +1, d);
-    finish_update<PROPAGATE>(h, d, kw <= 16 * 1024);
+    for (int i = hl; i < kw; i += kSeg) update<PROPAGATE>(h, codes[start + ky * SW + i], +1, d);
+    finish_update<PROPAGATE>(h, d, kw <= 8 * 1024);
   }
 }
 
+// The statistic of the segment's window. Every branch on per-segment data
+// calls the same sequence of selections, so the warp stays converged.
 template <typename T>
-__device__ __forceinline__ T hist_finish(WarpHist& h, const HistArgs& a,
+__device__ __forceinline__ T hist_finish(SegHist& h, const HistArgs& a,
                                          const typename KeyOf<T>::K* sorted) {
   using KO = KeyOf<T>;
   const Reduce& r = a.r;
-  if ((!r.omit && h.nan > 0) || (r.omit && h.count < r.min_count) || h.count == 0) return nan_of(T());
-  auto value_at = [&](int k) { return KO::value(sorted[hist_select(h, k)]); };
+  const bool valid = !((!r.omit && h.nan > 0) || (r.omit && h.count < r.min_count) || h.count == 0);
+  const int last = max(h.count - 1, 0);
   switch (r.kind) {
     case kRank:
-    case kRankHistogram:
-      if (r.param >= h.count) return nan_of(T());
-      return value_at((int)r.param);
-    case kMin:
-      return value_at(0);
-    case kMax:
-      return value_at(h.count - 1);
-    case kPercentile: {
-      if (r.q == 100.0) return value_at(h.count - 1);
-      PercentileRank pr = percentile_rank(r.q_fraction, h.count);
-      double lo = (double)value_at((int)pr.lower);
-      double hi = pr.upper == pr.lower ? lo : (double)value_at((int)pr.upper);
-      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+    case kRankHistogram: {
+      const bool ok = valid && r.param < h.count;
+      const int rank = seg_select(h, ok ? (int)r.param : 0, ok);
+      return ok ? KO::value(sorted[rank]) : nan_of(T());
     }
-    default:
-      break;
-  }
-  if (h.count & 1) return value_at(h.count / 2);
-  const int lo = hist_select(h, h.count / 2 - 1);
-  const int hi = next_set_bit(h, lo);
-  if constexpr (sizeof(T) == 4) {
-    return midpoint_f32(KO::value(sorted[lo]), KO::value(sorted[hi]));
-  } else {
-    return midpoint(KO::value(sorted[lo]), KO::value(sorted[hi]));
+    case kMin: {
+      const int rank = seg_select(h, 0, valid);
+      return valid ? KO::value(sorted[rank]) : nan_of(T());
+    }
+    case kMax: {
+      const int rank = seg_select(h, last, valid);
+      return valid ? KO::value(sorted[rank]) : nan_of(T());
+    }
+    case kPercentile: {
+      if (r.q == 100.0) {
+        const int rank = seg_select(h, last, valid);
+        return valid ? KO::value(sorted[rank]) : nan_of(T());
+      }
+      PercentileRank pr = percentile_rank(r.q_fraction, max(h.count, 1));
+      const int lo = seg_select(h, valid ? (int)pr.lower : 0, valid);
+      const int hi = seg_next(h, lo, valid && pr.upper != pr.lower);
+      if (!valid) return nan_of(T());
+      const double vlo = (double)KO::value(sorted[lo]);
+      const double vhi = pr.upper == pr.lower ? vlo : (double)KO::value(sorted[hi]);
+      return from_f64<T>(interpolate(vlo, vhi, pr.fraction));
+    }
+    default: {
+      const bool even = (h.count & 1) == 0;
+      const int k = even ? h.count / 2 - 1 : h.count / 2;
+      const int lo = seg_select(h, valid ? k : 0, valid);
+      const int hi = seg_next(h, lo, valid && even);
+      if (!valid) return nan_of(T());
+      if (!even) return KO::value(sorted[lo]);
+      if constexpr (sizeof(T) == 4) {
+        return midpoint_f32(KO::value(sorted[lo]), KO::value(sorted[hi]));
+      } else {
+        return midpoint(KO::value(sorted[lo]), KO::value(sorted[hi]));
+      }
+    }
   }
 }
 
-// A warp's boustrophedon walk over columns [c_begin, c_end) of its tile.
+// A segment's boustrophedon walk over columns [c_begin, c_begin + ncols)
+// of its tile; columns at or beyond `tw_eff` are computed for convergence
+// but not stored.
 template <typename T, bool PROPAGATE>
-__device__ __forceinline__ void walk(const uint16_t* codes, int c_begin, int c_end, int th_eff, int kh,
-                                     int kw, int SW, long long y0, long long x0, const Geom3& g,
-                                     const HistArgs& a, const typename KeyOf<T>::K* sorted,
-                                     T* __restrict__ out, WarpHist& h) {
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void walk(const uint16_t* codes, int c_begin, int ncols, int tw_eff,
+                                     int th_eff, int kh, int kw, int SW, long long y0, long long x0,
+                                     const Geom3& g, const HistArgs& a,
+                                     const typename KeyOf<T>::K* sorted, T* __restrict__ out,
+                                     SegHist& h) {
+  const int hl = seg_lane();
   add_box<PROPAGATE>(codes, c_begin, kh, kw, SW, h);
   int row = 0;
   int dir = 1;
-  for (int c = c_begin; c < c_end; ++c) {
+  for (int j = 0; j < ncols; ++j) {
+    const int c = c_begin + j;
     for (int i = 0; i < th_eff; ++i) {
       T result = hist_finish<T>(h, a, sorted);
-      if (lane == 0) out[(y0 + row) * g.W + x0 + c] = canonical(result);
+      if (hl == 0 && c < tw_eff) out[(y0 + row) * g.W + x0 + c] = canonical(result);
       if (i + 1 < th_eff) {
         if (dir > 0) {
           step<PROPAGATE>(codes, row * SW + c, (row + kh) * SW + c, kw, 1, h);
@@ -406,7 +450,7 @@ __device__ __forceinline__ void walk(const uint16_t* codes, int c_begin, int c_e
         }
       }
     }
-    if (c + 1 < c_end) step<PROPAGATE>(codes, row * SW + c, row * SW + c + kw, kh, SW, h);
+    if (j + 1 < ncols) step<PROPAGATE>(codes, row * SW + c, row * SW + c + kw, kh, SW, h);
     dir = -dir;
   }
 }
@@ -516,26 +560,30 @@ __global__ void __launch_bounds__(kHThreads, 1)
     __syncthreads();
     const K* sorted = SDEC ? decode_s : src_k;
 
-    // Slide: each warp walks its columns in boustrophedon order.
+    // Slide: each half-warp walks its columns in boustrophedon order.
     const int th_eff = (int)min((long long)a.TH, g.H - y0);
     const int tw_eff = (int)min((long long)a.TW, g.W - x0);
-    const int c_begin = warp * a.cols_per_warp;
-    const int c_end = min(tw_eff, c_begin + a.cols_per_warp);
-    WarpHist h;
-    h.words = work + warp * a.words;
+    const int seg = threadIdx.x / kSeg;
+    SegHist h;
+    h.words = work + seg * a.words;
     h.nwords = a.words;
     h.pivot = 0;
     h.below = 0;
     h.count = 0;
     h.nan = 0;
-    for (int i = lane; i < a.words; i += 32) h.words[i] = 0u;
+    for (int i = seg_lane(); i < a.words; i += kSeg) h.words[i] = 0u;
     __syncwarp();
-    const uint16_t* codes = codes_s;
     const int kh = g.kh, kw = g.kw, SW = a.SW;
-    if (c_begin < c_end && !a.r.omit) {
-      walk<T, true>(codes, c_begin, c_end, th_eff, kh, kw, SW, y0, x0, g, a, sorted, out, h);
-    } else if (c_begin < c_end) {
-      walk<T, false>(codes, c_begin, c_end, th_eff, kh, kw, SW, y0, x0, g, a, sorted, out, h);
+    // Both halves of a warp have columns iff the warp's first column is in
+    // the tile's valid width; whole warps beyond it sit out.
+    const int warp_first = (threadIdx.x / 32) * 2 * a.cols_per_warp;
+    if (warp_first < tw_eff) {
+      if (!a.r.omit)
+        walk<T, true>(codes_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh, kw, SW, y0,
+                      x0, g, a, sorted, out, h);
+      else
+        walk<T, false>(codes_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh, kw, SW, y0,
+                       x0, g, a, sorted, out, h);
     }
     __syncthreads();
   }
@@ -553,7 +601,7 @@ size_t smem_bytes_for(int S, bool sdec, size_t key_bytes) {
   size_t codes = (size_t)align16((long long)S * 2);
   size_t decode = sdec ? (size_t)align16((long long)S * (long long)key_bytes) : 0;
   size_t sort = (size_t)kHWarps * 256 * 4;
-  size_t hist = (size_t)kHWarps * ((S + 31) / 32) * 4;
+  size_t hist = (size_t)kSegs * ((S + 31) / 32) * 4;
   return codes + decode + std::max(sort, hist);
 }
 
@@ -572,7 +620,7 @@ HistChoice choose_tile(const Geom3& g, size_t key_bytes) {
     for (int sdec = 1; sdec >= 0; --sdec) {
       size_t smem = smem_bytes_for((int)S, sdec != 0, key_bytes);
       if (smem > kSmemBudget) continue;
-      const double cpw = (tw + kHWarps - 1) / kHWarps;
+      const double cpw = (tw + kSegs - 1) / kSegs;
       const double outputs = (double)tw * th;
       double cost = 2.0 * g.kw + (double)g.kh * g.kw / (cpw * th) + 2.0 * g.kh / th +
                     8.0 * (double)S / outputs + (sdec ? 0.0 : 12.0);
@@ -588,12 +636,12 @@ HistChoice choose_tile(const Geom3& g, size_t key_bytes) {
     }
   };
   if (g.H == 1 && g.kh == 1) {
-    for (int tw : {8192, 4096, 2048, 1024, 512, 256, 128, 64, 32, 16})
-      if (tw <= 16 || tw / 2 < g.W) consider(tw, 1);
+    for (int tw : {8192, 4096, 2048, 1024, 512, 256, 128, 64, 32})
+      if (tw <= 32 || tw / 2 < g.W) consider(tw, 1);
     return best;
   }
-  for (int tw : {64, 32, 16}) {
-    if (tw > 16 && tw / 2 >= g.W) continue;
+  for (int tw : {128, 64, 32}) {
+    if (tw > 32 && tw / 2 >= g.W) continue;
     for (int th : {256, 192, 128, 96, 64, 48, 32, 16, 8, 4, 2, 1}) {
       if (th > 1 && th / 2 >= g.H) continue;
       consider(tw, th);
@@ -612,7 +660,7 @@ HistArgs make_args_core(const Geom3& g, int TW, int TH, int dtype, const Reduce&
   a.S = a.SW * a.SH;
   a.tiles_x = (a.g.W + a.TW - 1) / a.TW;
   a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
-  a.cols_per_warp = (a.TW + kHWarps - 1) / kHWarps;
+  a.cols_per_warp = (a.TW + kSegs - 1) / kSegs;  // columns per half-warp segment
   a.words = (a.S + 31) / 32;
   a.slot_bytes = dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
   a.r = r;
@@ -629,7 +677,7 @@ HistArgs make_args(const Plan& p) {
   a.S = a.SW * a.SH;
   a.tiles_x = (a.g.W + a.TW - 1) / a.TW;
   a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
-  a.cols_per_warp = (a.TW + kHWarps - 1) / kHWarps;
+  a.cols_per_warp = (a.TW + kSegs - 1) / kSegs;  // columns per half-warp segment
   a.words = (a.S + 31) / 32;
   a.slot_bytes = p.dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
   a.r = p.r;
