@@ -29,7 +29,7 @@ NVCC_FLAGS = [
     ARCH,
     "-lineinfo",
     "-Xcompiler",
-    "-fPIC",
+    "-fPIC,-ffp-contract=off",
     "--expt-relaxed-constexpr",
     "-extended-lambda",
 ]

@@ -256,6 +256,11 @@ void release(Plan& p) {
   if (p.d_out) cudaFree(p.d_out);
   if (p.d_scratch) cudaFree(p.d_scratch);
   if (p.d_status) cudaFree(p.d_status);
+  if (p.d_hist_lists) cudaFree(p.d_hist_lists);
+  if (p.d_pct) cudaFree(p.d_pct);
+  p.d_hist_lists = nullptr;
+  p.d_pct = nullptr;
+  p.r.pct = nullptr;
   p.d_tile_taps = nullptr;
   p.d_gen_taps = nullptr;
   p.d_in = p.d_out = p.d_scratch = nullptr;
@@ -333,6 +338,8 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
   r.param = (long long)std::min<uint64_t>(d->parameter, (uint64_t)std::numeric_limits<long long>::max());
   r.q = d->percentile;
   r.q_fraction = d->percentile / 100.0;
+  r.q_is_max = d->percentile == 100.0;
+  r.pct = nullptr;
   r.cval = d->dtype == NDF_FLOAT32 ? (double)(float)d->cval : d->cval;
   r.moments = d->moments == NDF_MOMENTS_FP64 ? 1 : 0;
   if (kind == kPercentile) {
@@ -367,10 +374,39 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
   return NDF_OK;
 }
 
+// The percentile rank split per retained count n = 0..count, in the float64
+// arithmetic of src/robust.rs:343-352 (the library's host code is compiled
+// without floating-point contraction, so each operation rounds once).
+int upload_percentile_table(Plan& p) {
+  std::vector<PctEntry> table((size_t)p.r.count + 1);
+  for (int n = 1; n <= p.r.count; ++n) {
+    const double rank = p.r.q_fraction * (double)(n - 1);
+    const double lower = std::floor(rank);
+    const double fraction = rank - lower;
+    PctEntry& e = table[(size_t)n];
+    e.fraction = fraction;
+    e.lower = (int)lower;
+    const bool low = fraction <= 0.5;
+    e.w = low ? fraction : 1.0 - fraction;
+    e.flags = (fraction == 0.0 ? kPctFracZero : 0) | (low ? kPctLowSide : 0) |
+              (fraction == 1.0 ? kPctFracOne : 0);
+  }
+  cudaError_t e = cudaMalloc(&p.d_pct, table.size() * sizeof(PctEntry));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(percentile table)");
+  e = cudaMemcpy(p.d_pct, table.data(), table.size() * sizeof(PctEntry), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(percentile table)");
+  p.r.pct = p.d_pct;
+  return NDF_OK;
+}
+
 int choose_algorithm(Plan& p, int smem_limit) {
   if (p.n_out == 0) {
     p.algo = Algo::kEmpty;
     return NDF_OK;
+  }
+  if (p.r.kind == kPercentile && !p.r.q_is_max) {
+    int rc = upload_percentile_table(p);
+    if (rc != NDF_OK) return rc;
   }
   const bool tileable = p.ndim <= 3 && p.r.count <= (1 << 24);
   if (tileable) setup_tile(p);
@@ -387,11 +423,11 @@ int choose_algorithm(Plan& p, int smem_limit) {
     return setup_generic(p);
   }
   if (tileable) {
-    // Rectangular 1-D/2-D windows: the sliding rank histogram for the
-    // histogram kinds, and for every order statistic whose window is too
-    // wide for a register network.
+    // 1-D/2-D windows: the sliding rank histogram for the histogram kinds
+    // (rectangular windows only), and for every order statistic whose window
+    // is too wide for a register network (footprints slide their run ends).
     const bool hist_kind = p.r.kind == kMedianHistogram || p.r.kind == kRankHistogram;
-    if (p.footprint.empty() && histogram_supported(p) &&
+    if (histogram_supported(p) &&
         (hist_kind || network_width_for(p.dtype, p.r.count) == 0)) {
       histogram_configure(p);
       p.smem_bytes = histogram_smem(p);

@@ -10,6 +10,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "plan.h"
+
 namespace ndf {
 
 enum Mode : int32_t { kReflect = 0, kConstant = 1, kNearest = 2, kMirror = 3, kWrap = 4 };
@@ -324,6 +326,88 @@ __device__ __forceinline__ PercentileRank percentile_rank(double q_fraction, lon
   long long lower = (long long)floor(rank);
   long long upper = lower + 1 < n - 1 ? lower + 1 : n - 1;
   return {lower, upper, __dsub_rn(rank, (double)lower)};
+}
+
+// The split for n >= 1 retained samples: from the plan's table when it has
+// one (an L1-resident load instead of six FP64-pipe operations, which run at
+// a small fraction of the FP32 rate on this GPU), else computed.
+struct PctSplit {
+  int lower, upper, flags;
+  double fraction, w;
+};
+
+__device__ __forceinline__ PctSplit pct_split(const Reduce& r, long long n) {
+  PctSplit s;
+  if (r.pct) {
+    const PctEntry* e = r.pct + n;
+    s.fraction = __ldg(&e->fraction);
+    s.w = __ldg(&e->w);
+    s.lower = __ldg(&e->lower);
+    s.flags = __ldg(&e->flags);
+  } else {
+    PercentileRank pr = percentile_rank(r.q_fraction, n);
+    s.lower = (int)pr.lower;
+    s.fraction = pr.fraction;
+    const bool low = pr.fraction <= 0.5;
+    s.w = low ? pr.fraction : __dsub_rn(1.0, pr.fraction);
+    s.flags = (pr.fraction == 0.0 ? kPctFracZero : 0) | (low ? kPctLowSide : 0) |
+              (pr.fraction == 1.0 ? kPctFracOne : 0);
+  }
+  s.upper = s.lower + 1 < n - 1 ? s.lower + 1 : (int)(n - 1);
+  return s;
+}
+
+// float -> float64 bits for a normal or zero float (exact; integer ops only).
+__device__ __forceinline__ double f32_to_f64_exact(unsigned int b) {
+  const unsigned int sign = b & 0x80000000u;
+  const unsigned int e = (b >> 23) & 0xFFu;
+  const unsigned int hi = e == 0 ? sign : sign | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+  const unsigned int lo = e == 0 ? 0u : (b & 7u) << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// Round a float64 to float (to nearest, ties to even) with integer ops when
+// the result is a normal float; other results take the hardware conversion.
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+  const int e32 = (int)((hi >> 20) & 0x7FFu) - 896;
+  if (e32 < 1 || e32 > 254) return __double2float_rn(x);
+  const unsigned int mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  const unsigned int rem = lo & 0x1FFFFFFFu;
+  const unsigned int bits = (hi & 0x80000000u) | ((unsigned int)e32 << 23) | mant;
+  const bool up = rem > 0x10000000u || (rem == 0x10000000u && (mant & 1u));
+  return __uint_as_float(bits + (up ? 1u : 0u));  // a carry rounds into the exponent
+}
+
+// T(interpolate(lower, upper, fraction)) for order statistics lower <= upper.
+template <typename T>
+__device__ __forceinline__ T pct_value(const PctSplit& s, T lower, T upper);
+
+template <>
+__device__ __forceinline__ double pct_value<double>(const PctSplit& s, double lower, double upper) {
+  return interpolate(lower, upper, s.fraction);
+}
+
+// float inputs: the common case (both normal or zero, same sign, distinct,
+// 0 < fraction < 1) needs three FP64 operations; rounding the float64 result
+// once to float and clamping in float equals clamping in float64 first,
+// because lower and upper are floats and rounding is monotonic.
+template <>
+__device__ __forceinline__ float pct_value<float>(const PctSplit& s, float lower, float upper) {
+  const unsigned int lb = __float_as_uint(lower), ub = __float_as_uint(upper);
+  const unsigned int el = (lb >> 23) & 0xFFu, eu = (ub >> 23) & 0xFFu;
+  const bool ok_l = (el - 1u) < 254u || (lb << 1) == 0u;
+  const bool ok_u = (eu - 1u) < 254u || (ub << 1) == 0u;
+  const bool fast = ok_l && ok_u && lb != ub && ((lb ^ ub) >> 31) == 0u &&
+                    (s.flags & (kPctFracZero | kPctFracOne)) == 0;
+  if (!fast) return __double2float_rn(interpolate((double)lower, (double)upper, s.fraction));
+  const double dl = f32_to_f64_exact(lb), du = f32_to_f64_exact(ub);
+  const double p = __dmul_rn(__dsub_rn(du, dl), s.w);
+  const double r = (s.flags & kPctLowSide) ? __dadd_rn(dl, p) : __dsub_rn(du, p);
+  const float x = f64_to_f32_rn(r);
+  if (x < lower) return lower;
+  if (x > upper) return upper;
+  return x;
 }
 
 }  // namespace ndf

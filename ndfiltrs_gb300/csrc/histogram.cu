@@ -54,6 +54,12 @@ struct HistArgs {
   int words;                // per-warp bit histogram: 32-bit words
   long long slot_bytes;     // scratch bytes per block slot
   Reduce r;
+  // Footprint windows: support-linear offsets (y * SW + x) of the taps
+  // (nf), of the top and bottom ends of every vertical run of taps (nv
+  // each) and of the left and right ends of every horizontal run (nh
+  // each), in that order. Unused (nullptr) for rectangular windows.
+  const uint16_t* lists;
+  int nf, nv, nh;
 };
 
 template <typename K>
@@ -369,6 +375,32 @@ __device__ __forceinline__ void add_box(const uint16_t* codes, int start, int kh
   }
 }
 
+// Footprint windows: remove the codes at rbase + rlist[i] and add those at
+// abase + alist[i] (n each).
+template <bool PROPAGATE>
+__device__ __forceinline__ void step_lists(const uint16_t* codes, int rbase, const uint16_t* rlist,
+                                           int abase, const uint16_t* alist, int n, SegHist& h) {
+  const int hl = seg_lane();
+  StepDelta d;
+  for (int i = hl; i < n; i += kSeg) {
+    const int rc = codes[rbase + rlist[i]];
+    const int ac = codes[abase + alist[i]];
+    update<PROPAGATE>(h, rc, -1, d);
+    update<PROPAGATE>(h, ac, +1, d);
+  }
+  finish_update<PROPAGATE>(h, d, n <= 8 * 1024);
+}
+
+// Footprint windows: add every tap of the window whose origin is `base`.
+template <bool PROPAGATE>
+__device__ __forceinline__ void add_taps(const uint16_t* codes, int base, const uint16_t* taps, int n,
+                                        SegHist& h) {
+  const int hl = seg_lane();
+  StepDelta d;
+  for (int i = hl; i < n; i += kSeg) update<PROPAGATE>(h, codes[base + taps[i]], +1, d);
+  finish_update<PROPAGATE>(h, d, false);
+}
+
 // The statistic of the segment's window. Every branch on per-segment data
 // calls the same sequence of selections, so the warp stays converged.
 template <typename T>
@@ -394,17 +426,17 @@ __device__ __forceinline__ T hist_finish(SegHist& h, const HistArgs& a,
       return valid ? KO::value(sorted[rank]) : nan_of(T());
     }
     case kPercentile: {
-      if (r.q == 100.0) {
+      if (r.q_is_max) {
         const int rank = seg_select(h, last, valid);
         return valid ? KO::value(sorted[rank]) : nan_of(T());
       }
-      PercentileRank pr = percentile_rank(r.q_fraction, max(h.count, 1));
-      const int lo = seg_select(h, valid ? (int)pr.lower : 0, valid);
-      const int hi = seg_next(h, lo, valid && pr.upper != pr.lower);
+      const PctSplit ps = pct_split(r, max(h.count, 1));
+      const int lo = seg_select(h, valid ? ps.lower : 0, valid);
+      const int hi = seg_next(h, lo, valid && ps.upper != ps.lower);
       if (!valid) return nan_of(T());
-      const double vlo = (double)KO::value(sorted[lo]);
-      const double vhi = pr.upper == pr.lower ? vlo : (double)KO::value(sorted[hi]);
-      return from_f64<T>(interpolate(vlo, vhi, pr.fraction));
+      const T vlo = KO::value(sorted[lo]);
+      const T vhi = ps.upper == ps.lower ? vlo : KO::value(sorted[hi]);
+      return pct_value<T>(ps, vlo, vhi);
     }
     default: {
       const bool even = (h.count & 1) == 0;
@@ -424,15 +456,27 @@ __device__ __forceinline__ T hist_finish(SegHist& h, const HistArgs& a,
 
 // A segment's boustrophedon walk over columns [c_begin, c_begin + ncols)
 // of its tile; columns at or beyond `tw_eff` are computed for convergence
-// but not stored.
-template <typename T, bool PROPAGATE>
-__device__ __forceinline__ void walk(const uint16_t* codes, int c_begin, int ncols, int tw_eff,
-                                     int th_eff, int kh, int kw, int SW, long long y0, long long x0,
-                                     const Geom3& g, const HistArgs& a,
+// but not stored. A window's origin is its top-left support position
+// o = row * SW + c. Rectangular windows (FP false) move whole support row or
+// column segments; footprint windows (FP true) move the run ends in `lists`:
+// down removes o + top[i] and adds o + SW + bottom[i], up removes
+// o + bottom[i] and adds o - SW + top[i], right removes o + left[i] and adds
+// o + 1 + right[i].
+template <typename T, bool PROPAGATE, bool FP>
+__device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* lists, int c_begin,
+                                     int ncols, int tw_eff, int th_eff, int kh, int kw, int SW,
+                                     long long y0, long long x0, const Geom3& g, const HistArgs& a,
                                      const typename KeyOf<T>::K* sorted, T* __restrict__ out,
                                      SegHist& h) {
   const int hl = seg_lane();
-  add_box<PROPAGATE>(codes, c_begin, kh, kw, SW, h);
+  const uint16_t* top = lists + a.nf;
+  const uint16_t* bottom = top + a.nv;
+  const uint16_t* left = bottom + a.nv;
+  const uint16_t* right = left + a.nh;
+  if (FP)
+    add_taps<PROPAGATE>(codes, c_begin, lists, a.nf, h);
+  else
+    add_box<PROPAGATE>(codes, c_begin, kh, kw, SW, h);
   int row = 0;
   int dir = 1;
   for (int j = 0; j < ncols; ++j) {
@@ -441,21 +485,34 @@ __device__ __forceinline__ void walk(const uint16_t* codes, int c_begin, int nco
       T result = hist_finish<T>(h, a, sorted);
       if (hl == 0 && c < tw_eff) out[(y0 + row) * g.W + x0 + c] = canonical(result);
       if (i + 1 < th_eff) {
+        const int o = row * SW + c;
         if (dir > 0) {
-          step<PROPAGATE>(codes, row * SW + c, (row + kh) * SW + c, kw, 1, h);
+          if (FP)
+            step_lists<PROPAGATE>(codes, o, top, o + SW, bottom, a.nv, h);
+          else
+            step<PROPAGATE>(codes, o, o + kh * SW, kw, 1, h);
           ++row;
         } else {
-          step<PROPAGATE>(codes, (row + kh - 1) * SW + c, (row - 1) * SW + c, kw, 1, h);
+          if (FP)
+            step_lists<PROPAGATE>(codes, o, bottom, o - SW, top, a.nv, h);
+          else
+            step<PROPAGATE>(codes, o + (kh - 1) * SW, o - SW, kw, 1, h);
           --row;
         }
       }
     }
-    if (j + 1 < ncols) step<PROPAGATE>(codes, row * SW + c, row * SW + c + kw, kh, SW, h);
+    if (j + 1 < ncols) {
+      const int o = row * SW + c;
+      if (FP)
+        step_lists<PROPAGATE>(codes, o, left, o + 1, right, a.nh, h);
+      else
+        step<PROPAGATE>(codes, o, o + kw, kh, SW, h);
+    }
     dir = -dir;
   }
 }
 
-template <typename T, bool SDEC>
+template <typename T, bool SDEC, bool FP>
 __global__ void __launch_bounds__(kHThreads, 1)
     histogram_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ HistArgs a,
                      unsigned char* scratch) {
@@ -467,13 +524,21 @@ __global__ void __launch_bounds__(kHThreads, 1)
   __shared__ int red_sent[kHWarps];
   const Geom3& g = a.g;
   const int S = a.S;
-  // Shared memory: rank codes [S] u16 | decode table [S] keys (SDEC) |
-  // work (radix tables during the sort, warp histograms while sliding).
+  // Shared memory: rank codes [S] u16 | footprint lists (FP) | decode table
+  // [S] keys (SDEC) | work (radix tables during the sort, half-warp
+  // histograms while sliding).
   uint16_t* codes_s = reinterpret_cast<uint16_t*>(smem);
-  K* decode_s = reinterpret_cast<K*>(smem + align16((long long)a.S * 2));
+  const long long list_bytes = FP ? align16((long long)(a.nf + 2 * a.nv + 2 * a.nh) * 2) : 0;
+  uint16_t* lists_s = reinterpret_cast<uint16_t*>(smem + align16((long long)a.S * 2));
+  K* decode_s = reinterpret_cast<K*>(smem + align16((long long)a.S * 2) + list_bytes);
   unsigned int* work = reinterpret_cast<unsigned int*>(
-      smem + align16((long long)a.S * 2) + (SDEC ? align16((long long)a.S * sizeof(K)) : 0));
+      smem + align16((long long)a.S * 2) + list_bytes + (SDEC ? align16((long long)a.S * sizeof(K)) : 0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (FP) {
+    // Made visible by the first barrier of the tile loop.
+    const int n = a.nf + 2 * a.nv + 2 * a.nh;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) lists_s[i] = a.lists[i];
+  }
   Slot<K> slot = slot_at<K>(scratch + (long long)blockIdx.x * a.slot_bytes, S);
   const bool drop_inf = a.r.drop_inf;
   const K outside = sample_key<T>((T)a.r.cval, drop_inf);
@@ -579,11 +644,11 @@ __global__ void __launch_bounds__(kHThreads, 1)
     const int warp_first = (threadIdx.x / 32) * 2 * a.cols_per_warp;
     if (warp_first < tw_eff) {
       if (!a.r.omit)
-        walk<T, true>(codes_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh, kw, SW, y0,
-                      x0, g, a, sorted, out, h);
+        walk<T, true, FP>(codes_s, lists_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh,
+                          kw, SW, y0, x0, g, a, sorted, out, h);
       else
-        walk<T, false>(codes_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh, kw, SW, y0,
-                       x0, g, a, sorted, out, h);
+        walk<T, false, FP>(codes_s, lists_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh,
+                           kw, SW, y0, x0, g, a, sorted, out, h);
     }
     __syncthreads();
   }
@@ -597,19 +662,42 @@ struct HistChoice {
 
 constexpr size_t kSmemBudget = 225 * 1024;
 
-size_t smem_bytes_for(int S, bool sdec, size_t key_bytes) {
+// Run-list entries of a footprint window (0 for a rectangular one).
+struct Runs {
+  int nf = 0, nv = 0, nh = 0;
+  bool footprint = false;
+  int entries() const { return footprint ? nf + 2 * nv + 2 * nh : 0; }
+};
+
+size_t smem_bytes_for(int S, bool sdec, size_t key_bytes, int list_entries) {
   size_t codes = (size_t)align16((long long)S * 2);
+  size_t lists = (size_t)align16((long long)list_entries * 2);
   size_t decode = sdec ? (size_t)align16((long long)S * (long long)key_bytes) : 0;
   size_t sort = (size_t)kHWarps * 256 * 4;
   size_t hist = (size_t)kSegs * ((S + 31) / 32) * 4;
-  return codes + decode + std::max(sort, hist);
+  return codes + lists + decode + std::max(sort, hist);
+}
+
+// Count the taps and the vertical and horizontal runs of a kh x kw
+// footprint mask (row-major).
+Runs count_runs(const std::vector<uint8_t>& mask, int kh, int kw) {
+  Runs r;
+  r.footprint = true;
+  for (int y = 0; y < kh; ++y)
+    for (int x = 0; x < kw; ++x) {
+      if (!mask[(size_t)y * kw + x]) continue;
+      ++r.nf;
+      if (y == 0 || !mask[(size_t)(y - 1) * kw + x]) ++r.nv;
+      if (x == 0 || !mask[(size_t)y * kw + x - 1]) ++r.nh;
+    }
+  return r;
 }
 
 // Pick the output tile by a cost model in units of one histogram update per
 // output: vertical steps (2 kw), the first window of each warp's walk, the
 // column moves, the block sort (about 8 units per support sample) and a
 // global decode when the sorted keys do not fit in shared memory.
-HistChoice choose_tile(const Geom3& g, size_t key_bytes) {
+HistChoice choose_tile(const Geom3& g, size_t key_bytes, const Runs& runs = Runs{}) {
   HistChoice best;
   if (g.kd != 1 || g.D != 1) return best;
   if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport) return best;
@@ -618,11 +706,14 @@ HistChoice choose_tile(const Geom3& g, size_t key_bytes) {
     long long S = (long long)(tw + g.kw - 1) * (th + g.kh - 1);
     if (S > kMaxSupport) return;
     for (int sdec = 1; sdec >= 0; --sdec) {
-      size_t smem = smem_bytes_for((int)S, sdec != 0, key_bytes);
+      size_t smem = smem_bytes_for((int)S, sdec != 0, key_bytes, runs.entries());
       if (smem > kSmemBudget) continue;
       const double cpw = (tw + kSegs - 1) / kSegs;
       const double outputs = (double)tw * th;
-      double cost = 2.0 * g.kw + (double)g.kh * g.kw / (cpw * th) + 2.0 * g.kh / th +
+      const double vertical = runs.footprint ? runs.nv : g.kw;
+      const double horizontal = runs.footprint ? runs.nh : g.kh;
+      const double taps = runs.footprint ? runs.nf : (double)g.kh * g.kw;
+      double cost = 2.0 * vertical + taps / (cpw * th) + 2.0 * horizontal / th +
                     8.0 * (double)S / outputs + (sdec ? 0.0 : 12.0);
       if (smem * 2 <= kSmemBudget) cost *= 0.9;  // two resident blocks per SM
       if (cost < best_cost) {
@@ -664,6 +755,10 @@ HistArgs make_args_core(const Geom3& g, int TW, int TH, int dtype, const Reduce&
   a.words = (a.S + 31) / 32;
   a.slot_bytes = dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
   a.r = r;
+  a.lists = nullptr;
+  a.nf = a.g.kh * a.g.kw;
+  a.nv = a.g.kw;
+  a.nh = a.g.kh;
   return a;
 }
 
@@ -681,12 +776,24 @@ HistArgs make_args(const Plan& p) {
   a.words = (a.S + 31) / 32;
   a.slot_bytes = p.dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
   a.r = p.r;
+  if (p.hist_footprint) {
+    a.lists = p.d_hist_lists;
+    a.nf = p.hist_nf;
+    a.nv = p.hist_nv;
+    a.nh = p.hist_nh;
+  } else {
+    a.lists = nullptr;
+    a.nf = a.g.kh * a.g.kw;
+    a.nv = a.g.kw;
+    a.nh = a.g.kh;
+  }
   return a;
 }
 
 template <typename T>
-void* kernel_for(bool sdec) {
-  return sdec ? (void*)histogram_kernel<T, true> : (void*)histogram_kernel<T, false>;
+void* kernel_for(bool sdec, bool fp = false) {
+  if (fp) return sdec ? (void*)histogram_kernel<T, true, true> : (void*)histogram_kernel<T, false, true>;
+  return sdec ? (void*)histogram_kernel<T, true, false> : (void*)histogram_kernel<T, false, false>;
 }
 
 template <typename T>
@@ -695,32 +802,93 @@ cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   long long slots = (long long)(p.scratch_bytes / (size_t)a.slot_bytes);
   long long grid = std::min<long long>(a.tiles, slots);
   if (grid < 1) return cudaErrorInvalidValue;
-  if (p.hist_sdec)
-    histogram_kernel<T, true><<<(unsigned)grid, kHThreads, p.smem_bytes, s>>>(in, out, a,
-                                                                             (unsigned char*)p.d_scratch);
-  else
-    histogram_kernel<T, false><<<(unsigned)grid, kHThreads, p.smem_bytes, s>>>(in, out, a,
-                                                                              (unsigned char*)p.d_scratch);
+  unsigned char* scratch = (unsigned char*)p.d_scratch;
+  const unsigned blocks = (unsigned)grid;
+  if (p.hist_footprint) {
+    if (p.hist_sdec)
+      histogram_kernel<T, true, true><<<blocks, kHThreads, p.smem_bytes, s>>>(in, out, a, scratch);
+    else
+      histogram_kernel<T, false, true><<<blocks, kHThreads, p.smem_bytes, s>>>(in, out, a, scratch);
+  } else {
+    if (p.hist_sdec)
+      histogram_kernel<T, true, false><<<blocks, kHThreads, p.smem_bytes, s>>>(in, out, a, scratch);
+    else
+      histogram_kernel<T, false, false><<<blocks, kHThreads, p.smem_bytes, s>>>(in, out, a, scratch);
+  }
   return cudaGetLastError();
 }
 
 }  // namespace
 
+namespace {
+
+// The footprint of a 1-D/2-D plan as a kh x kw mask in the tile's (y, x)
+// orientation, from the taps' box positions.
+std::vector<uint8_t> footprint_mask(const Plan& p) {
+  const Geom3& g = p.tile.g;
+  std::vector<uint8_t> mask((size_t)g.kh * g.kw, 0);
+  for (int i = 0; i < p.r.count; ++i) {
+    const int* bt = &p.box_taps[(size_t)i * 3];
+    mask[(size_t)bt[1] * g.kw + bt[2]] = 1;
+  }
+  return mask;
+}
+
+Runs runs_of(const Plan& p) {
+  if (p.footprint.empty()) return Runs{};
+  return count_runs(footprint_mask(p), p.tile.g.kh, p.tile.g.kw);
+}
+
+}  // namespace
+
 bool histogram_supported(const Plan& p) {
-  if (p.ndim > 2 || !p.footprint.empty()) return false;
+  if (p.ndim > 2 || p.r.count < 1) return false;
   const int k = p.r.kind;
   if (k != kMedian && k != kMedianNetwork && k != kMedianHistogram && k != kRank &&
       k != kRankHistogram && k != kMin && k != kMax && k != kPercentile)
     return false;
-  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8);
+  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8, runs_of(p));
   return c.TW > 0;
 }
 
 void histogram_configure(Plan& p) {
-  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8);
+  const Runs runs = runs_of(p);
+  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8, runs);
   p.hist_block_w = c.TW;
   p.hist_block_h = c.TH;
   p.hist_sdec = c.sdec;
+  p.hist_footprint = runs.footprint;
+  p.hist_nf = runs.nf;
+  p.hist_nv = runs.nv;
+  p.hist_nh = runs.nh;
+  p.hist_lists.clear();
+  if (runs.footprint) {
+    // Support-linear offsets (y * SW + x) of the taps and of the run ends.
+    const Geom3& g = p.tile.g;
+    const int SW = c.TW + g.kw - 1;
+    const std::vector<uint8_t> mask = footprint_mask(p);
+    auto at = [&](int y, int x) {
+      return y >= 0 && y < g.kh && x >= 0 && x < g.kw && mask[(size_t)y * g.kw + x] != 0;
+    };
+    std::vector<uint16_t> taps, top, bottom, left, right;
+    for (int y = 0; y < g.kh; ++y)
+      for (int x = 0; x < g.kw; ++x) {
+        if (!at(y, x)) continue;
+        const uint16_t off = (uint16_t)(y * SW + x);
+        taps.push_back(off);
+        if (!at(y - 1, x)) top.push_back(off);
+        if (!at(y + 1, x)) bottom.push_back(off);
+        if (!at(y, x - 1)) left.push_back(off);
+        if (!at(y, x + 1)) right.push_back(off);
+      }
+    // A step removes one list and adds the other; the pairing of entries
+    // does not matter, only that both lists of an axis have one entry per run.
+    p.hist_lists = taps;
+    p.hist_lists.insert(p.hist_lists.end(), top.begin(), top.end());
+    p.hist_lists.insert(p.hist_lists.end(), bottom.begin(), bottom.end());
+    p.hist_lists.insert(p.hist_lists.end(), left.begin(), left.end());
+    p.hist_lists.insert(p.hist_lists.end(), right.begin(), right.end());
+  }
   HistArgs a = make_args(p);
   p.hist_blocks_x = a.tiles_x;
   p.hist_blocks_y = a.tiles / a.tiles_x;
@@ -728,15 +896,23 @@ void histogram_configure(Plan& p) {
 
 size_t histogram_smem(const Plan& p) {
   HistArgs a = make_args(p);
-  return smem_bytes_for(a.S, p.hist_sdec, p.dtype == 0 ? 4 : 8);
+  return smem_bytes_for(a.S, p.hist_sdec, p.dtype == 0 ? 4 : 8, (int)p.hist_lists.size());
 }
 
 // Scratch slots for the block sort: one per resident block (occupancy x
 // SMs), capped by the number of tiles.
 cudaError_t histogram_allocate(Plan& p) {
   HistArgs a = make_args(p);
-  void* kernel = p.dtype == 0 ? kernel_for<float>(p.hist_sdec) : kernel_for<double>(p.hist_sdec);
+  void* kernel = p.dtype == 0 ? kernel_for<float>(p.hist_sdec, p.hist_footprint)
+                              : kernel_for<double>(p.hist_sdec, p.hist_footprint);
   cudaError_t e = allow_max_smem((const void*)kernel);
+  if (e != cudaSuccess) return e;
+  if (p.hist_footprint) {
+    e = cudaMalloc(&p.d_hist_lists, p.hist_lists.size() * sizeof(uint16_t));
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(p.d_hist_lists, p.hist_lists.data(), p.hist_lists.size() * sizeof(uint16_t),
+                   cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) return e;
   int per_sm = 1;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kHThreads, p.smem_bytes);
@@ -884,6 +1060,8 @@ extern "C" int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32
   r.param = (long long)std::min<uint64_t>(parameter, (uint64_t)(1ull << 62));
   r.q = percentile;
   r.q_fraction = percentile / 100.0;
+  r.q_is_max = percentile == 100.0;
+  r.pct = nullptr;
   r.cval = dtype == NDF_FLOAT32 ? (double)(float)cval : cval;
   HistChoice c = choose_tile(g, dtype == 0 ? 4 : 8);
   if (c.TW == 0) return noalloc_fail(NDF_ERR_UNSUPPORTED, "window too large for the histogram kernel");
@@ -899,7 +1077,7 @@ extern "C" int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32
     cudaGetLastError();
     return noalloc_fail(NDF_ERR_NO_DEVICE, "no usable CUDA device");
   }
-  const size_t smem = smem_bytes_for(a.S, c.sdec, dtype == 0 ? 4 : 8);
+  const size_t smem = smem_bytes_for(a.S, c.sdec, dtype == 0 ? 4 : 8, 0);
   if (smem > (size_t)optin) return noalloc_fail(NDF_ERR_UNSUPPORTED, "window too large for shared memory");
   void* scratch = nullptr;
   e = noalloc_scratch(device, &scratch);
@@ -915,17 +1093,17 @@ extern "C" int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == 0) {
     if (c.sdec)
-      histogram_kernel<float, true><<<(unsigned)grid, kHThreads, smem, s>>>(
+      histogram_kernel<float, true, false><<<(unsigned)grid, kHThreads, smem, s>>>(
           (const float*)d_in, (float*)d_out, a, (unsigned char*)scratch);
     else
-      histogram_kernel<float, false><<<(unsigned)grid, kHThreads, smem, s>>>(
+      histogram_kernel<float, false, false><<<(unsigned)grid, kHThreads, smem, s>>>(
           (const float*)d_in, (float*)d_out, a, (unsigned char*)scratch);
   } else {
     if (c.sdec)
-      histogram_kernel<double, true><<<(unsigned)grid, kHThreads, smem, s>>>(
+      histogram_kernel<double, true, false><<<(unsigned)grid, kHThreads, smem, s>>>(
           (const double*)d_in, (double*)d_out, a, (unsigned char*)scratch);
     else
-      histogram_kernel<double, false><<<(unsigned)grid, kHThreads, smem, s>>>(
+      histogram_kernel<double, false, false><<<(unsigned)grid, kHThreads, smem, s>>>(
           (const double*)d_in, (double*)d_out, a, (unsigned char*)scratch);
   }
   e = cudaGetLastError();

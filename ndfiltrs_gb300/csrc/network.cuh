@@ -153,11 +153,9 @@ __device__ __forceinline__ T network_finish(const K (&k)[N], int nv, const Reduc
       if (r.param >= nv) return nan_of(T());
       return KO::value(pick<A>(k, (int)r.param));
     case kPercentile: {
-      if (r.q == 100.0) return KO::value(pick<A>(k, nv - 1));
-      PercentileRank pr = percentile_rank(r.q_fraction, nv);
-      double lo = (double)KO::value(pick<A>(k, (int)pr.lower));
-      double hi = (double)KO::value(pick<A>(k, (int)pr.upper));
-      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+      if (r.q_is_max) return KO::value(pick<A>(k, nv - 1));
+      const PctSplit ps = pct_split(r, nv);
+      return pct_value<T>(ps, KO::value(pick<A>(k, ps.lower)), KO::value(pick<A>(k, ps.upper)));
     }
     default:
       if (nv & 1) return KO::value(pick<A>(k, nv / 2));
@@ -271,11 +269,11 @@ __device__ __forceinline__ T radix_finish(Fetch&& fetch, const Reduce& r) {
       if (r.param >= nv) return nan_of(T());
       return KO::value(sel(r.param));
     case kPercentile: {
-      if (r.q == 100.0) return KO::value(kmax);
-      PercentileRank pr = percentile_rank(r.q_fraction, nv);
-      double lo = (double)KO::value(sel(pr.lower));
-      double hi = pr.upper == pr.lower ? lo : (double)KO::value(sel(pr.upper));
-      return from_f64<T>(interpolate(lo, hi, pr.fraction));
+      if (r.q_is_max) return KO::value(kmax);
+      const PctSplit ps = pct_split(r, nv);
+      const T lo = KO::value(sel(ps.lower));
+      const T hi = ps.upper == ps.lower ? lo : KO::value(sel(ps.upper));
+      return pct_value<T>(ps, lo, hi);
     }
     default:
       if (nv & 1) return KO::value(sel(nv / 2));

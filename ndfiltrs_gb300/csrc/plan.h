@@ -23,6 +23,19 @@ struct Geom3 {
 };
 
 // Reduction parameters every kernel reads.
+// Percentile rank split for a window of n retained samples (src/robust.rs:
+// 343-352), tabulated per n on the host: rank = (q / 100) * (n - 1),
+// lower = floor(rank), fraction f = rank - lower, w = f (f <= 0.5) or 1 - f.
+struct PctEntry {
+  double fraction;
+  double w;
+  int lower;
+  int flags;  // kPctFracZero | kPctLowSide | kPctFracOne
+};
+constexpr int kPctFracZero = 1;
+constexpr int kPctLowSide = 2;
+constexpr int kPctFracOne = 4;
+
 struct Reduce {
   int kind;            // NDF_KIND_*
   int omit;            // InvalidPolicy::Omit
@@ -34,6 +47,8 @@ struct Reduce {
   double q_fraction;   // q / 100.0 (src/robust.rs:348 computes it the same way)
   double cval;         // constant boundary value, already cast to the dtype
   int moments;         // NDF_MOMENTS_* for mean/var/std
+  int q_is_max;        // q == 100 (the maximum)
+  const PctEntry* pct; // device table indexed by n (count + 1 entries), or nullptr
 };
 
 // Halo tile of one thread block: TW x TH outputs of one z slice. The block
@@ -105,10 +120,17 @@ struct Plan {
   size_t scratch_bytes = 0;
   unsigned int* d_status = nullptr; // device error flags
 
-  // Histogram kernel geometry (rectangular 1-D/2-D windows).
+  // Histogram kernel geometry (1-D/2-D windows).
   int hist_block_w = 0, hist_block_h = 0;
   bool hist_sdec = false;  // sorted keys staged in shared memory
   long long hist_blocks_x = 0, hist_blocks_y = 0;
+  // Footprint windows: tap and run-end offsets in the tile's support
+  // (taps | top | bottom | left | right ends) and their counts.
+  bool hist_footprint = false;
+  int hist_nf = 0, hist_nv = 0, hist_nh = 0;
+  std::vector<uint16_t> hist_lists;
+  uint16_t* d_hist_lists = nullptr;
+  PctEntry* d_pct = nullptr;  // percentile rank table (kPercentile, q < 100)
 };
 
 const char* algo_name(Algo a);

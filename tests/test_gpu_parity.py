@@ -264,3 +264,74 @@ def test_float32_midpoint_fast_path_matches_float64_rule(gpu, oracle) -> None:
     for kind in ("median", "median_network"):
         args = (kind, grid, (3, 3), None, (0, 0), ("reflect", "reflect"), 0.0, True, False, 1)
         _assert_bits(_gpu(*args), _oracle(oracle, "median", *args[1:]), kind)
+
+
+def _disk(radius):
+    y, x = np.mgrid[-radius:radius + 1, -radius:radius + 1]
+    return (x * x + y * y) <= radius * radius
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_footprint_histogram(gpu, oracle, dtype) -> None:
+    """Footprints beyond the register networks (> 128 taps) slide the rank
+    histogram by the ends of the footprint's runs: disks, rings, masks with
+    holes and empty border rows/columns, over multi-tile images with partial
+    tiles, every mode and shifted origins."""
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(21)
+    holes = _disk(8)
+    holes[rng.random(holes.shape) < 0.3] = False
+    ring = _disk(9) & ~np.pad(_disk(6), 3)
+    bordered = np.zeros((15, 17), dtype=bool)
+    bordered[2:13, 1:15] = _disk(7)[2:13, 0:14] | (rng.random((11, 14)) < 0.2)
+    footprints = {"disk7": _disk(7), "ring9": ring, "holes": holes, "bordered": bordered}
+    values = _special_values((83, 150), dtype, seed=5, fraction=0.05)
+    for name, footprint in footprints.items():
+        assert footprint.sum() > 128, name
+        with _core.Plan(values.shape, dtype, "median", footprint.shape, footprint=footprint,
+                        omit_nan=True) as plan:
+            assert plan.algorithm == "histogram", name
+        for mode in MODES:
+            origin = (0, 0) if mode in ("reflect", "wrap") else (1, -2)
+            for omit, ignore_inf, min_count in ((False, False, 1), (True, True, 40)):
+                for kind, parameter, q in (("median", 0, 50.0), ("rank", 7, 50.0), ("min", 0, 50.0),
+                                           ("max", 0, 50.0), ("percentile", 0, 84.0)):
+                    args = (kind, values, None, footprint, origin, (mode, mode), -0.75, omit, ignore_inf,
+                            min_count, parameter, q)
+                    _assert_bits(_gpu(*args), _oracle(oracle, *args), (name, mode, omit, kind))
+
+
+def test_footprint_histogram_1d_and_small_arrays(gpu, oracle) -> None:
+    rng = np.random.default_rng(8)
+    mask = rng.random(301) < 0.6
+    mask[0] = mask[-1] = True
+    line = _special_values((1000,), np.float32, seed=1, fraction=0.05)
+    for mode in MODES:
+        for kind in ("median", "percentile", "rank"):
+            args = (kind, line, None, mask, (3,), (mode,), 2.0, True, False, 1, 11, 16.0)
+            _assert_bits(_gpu(*args), _oracle(oracle, *args), (mode, kind))
+    # An image smaller than the footprint (every sample is boundary-mapped).
+    small = _special_values((6, 9), np.float64, seed=4, fraction=0.1)
+    for mode in MODES:
+        args = ("median", small, None, _disk(7), (0, 0), (mode, mode), 1.0, True, False, 1)
+        _assert_bits(_gpu(*args), _oracle(oracle, *args), mode)
+
+
+def test_float32_percentile_fast_path_matches_float64_rule(gpu, oracle) -> None:
+    """Percentile interpolation of float32 samples (three float64 operations
+    and an integer float64 -> float32 rounding in the common case) stays
+    bit-identical to the reference's float64 rule for many q, over values of
+    every magnitude, subnormals, signed zeros and mixed signs, in the box,
+    register-network and histogram kernels."""
+    rng = np.random.default_rng(1234)
+    mags = (2.0 ** rng.uniform(-149, 127, size=(61, 67))).astype(np.float32)
+    wide = mags * rng.choice(np.array([-1, 1], dtype=np.float32), size=mags.shape)
+    near = (1000 + rng.normal(size=(61, 67)) * 1e-3).astype(np.float32)
+    for values in (wide, near, _special_values((61, 67), np.float32, seed=31)):
+        for q in (0.0, 0.1, 12.5, 33.3, 50.0, 66.7, 84.0, 99.9, 100.0):
+            for size, footprint in (((5, 5), None), ((7, 7), None), (None, _disk(3)),
+                                    ((15, 15), None), (None, _disk(7))):
+                args = ("percentile", values, size, footprint, (0, 0), ("reflect", "mirror"), 0.0, True,
+                        False, 1, 0, q)
+                _assert_bits(_gpu(*args), _oracle(oracle, *args), (q, size))
