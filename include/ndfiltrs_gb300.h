@@ -159,7 +159,9 @@ const char* ndf_plan_algorithm(const ndf_plan* plan);
 
 /* ---- Batched persistent path. Many images of uneven sizes, each with its
  * own window, footprint and reduction, run as one persistent launch per
- * kernel family; the launches are captured once into a CUDA graph and
+ * kernel family (register networks, radix select, moments) plus one launch
+ * per image for the specialized kernels (box pair, sliding histogram); the
+ * launches are captured once into a CUDA graph as concurrent branches and
  * replayed. No counterpart in the reference (its Python callers loop). */
 
 typedef struct ndf_batch ndf_batch;
@@ -169,7 +171,16 @@ typedef struct ndf_batch ndf_batch;
 int ndf_batch_create(const ndf_filter_desc* descs, int32_t count, ndf_batch** batch);
 int ndf_batch_destroy(ndf_batch* batch);
 int ndf_batch_run(ndf_batch* batch, const void* const* d_in, void* const* d_out, void* stream);
-/* Number of persistent launches one ndf_batch_run enqueues. */
+/* Host-buffer run of a batch: `h_in[i]` / `h_out[i]` are host buffers
+ * (pageable or pinned) of image i. Copies every image to batch-owned device
+ * buffers, filters, copies the results back and returns after synchronizing.
+ * Images are processed in groups so that host copies, uploads, kernels and
+ * downloads of different groups overlap; the first call allocates the device
+ * buffers and two pinned staging slots per direction. Starts after the work
+ * already enqueued on `stream`; runs of one batch must not overlap. */
+int ndf_batch_run_host(ndf_batch* batch, const void* const* h_in, void* const* h_out, void* stream);
+/* Number of launches (persistent family launches plus per-image launches)
+ * one ndf_batch_run replays; valid after the first run. */
 int32_t ndf_batch_launches(const ndf_batch* batch);
 
 /* Allocation-free histogram filter over caller-owned device buffers. No

@@ -145,6 +145,8 @@ def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
                 handle.ndf_batch_destroy.restype = ctypes.c_int
                 handle.ndf_batch_run.argtypes = [plan_p, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
                 handle.ndf_batch_run.restype = ctypes.c_int
+                handle.ndf_batch_run_host.argtypes = [plan_p, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
+                handle.ndf_batch_run_host.restype = ctypes.c_int
                 handle.ndf_batch_launches.argtypes = [plan_p]
                 handle.ndf_batch_launches.restype = ctypes.c_int32
             _lib, _pylib = lib, pylib
@@ -356,6 +358,7 @@ class Batch:
         _check(lib.ndf_batch_create(descs, len(specs), ctypes.byref(handle)), lib)
         self._handle = handle
         self.count = len(specs)
+        self._shapes = [tuple(int(v) for v in spec["shape"]) for spec in specs]
 
     @property
     def launches(self) -> int:
@@ -369,6 +372,30 @@ class Batch:
         ins = (ctypes.c_void_p * self.count)(*d_in)
         outs = (ctypes.c_void_p * self.count)(*d_out)
         _check(lib.ndf_batch_run(self._handle, ins, outs, stream), lib)
+
+    def run_host(self, images: list, outputs: list | None = None) -> list:
+        """Filter host arrays (float32, C-contiguous, one per spec) through
+        the batch's host pipeline and return the results (new arrays unless
+        ``outputs`` is given)."""
+        lib, _ = _load()
+        if len(images) != self.count:
+            raise ValueError("one input array per image")
+        arrays = []
+        for image, shape in zip(images, self._shapes):
+            array = np.asarray(image)
+            if array.dtype != np.float32 or array.shape != shape:
+                raise ValueError("batched images must be float32 arrays of the planned shapes")
+            arrays.append(np.ascontiguousarray(array))
+        if outputs is None:
+            outputs = [np.empty(shape, dtype=np.float32) for shape in self._shapes]
+        elif len(outputs) != self.count or any(
+                o.dtype != np.float32 or o.shape != s or not o.flags.c_contiguous
+                for o, s in zip(outputs, self._shapes)):
+            raise ValueError("outputs must be C-contiguous float32 arrays of the planned shapes")
+        ins = (ctypes.c_void_p * self.count)(*[a.ctypes.data for a in arrays])
+        outs = (ctypes.c_void_p * self.count)(*[o.ctypes.data for o in outputs])
+        _check(lib.ndf_batch_run_host(self._handle, ins, outs, None), lib)
+        return outputs
 
     def close(self) -> None:
         if getattr(self, "_handle", None) is not None and self._handle.value:

@@ -70,3 +70,42 @@ def test_batch_matches_per_image_plans_and_oracle(gpu, oracle) -> None:
                                        mode=spec["mode"], omit_nan=True, q=84.0)
             np.testing.assert_array_equal(bits(got), bits(ref))
     batch.close()
+
+
+def test_batch_host_pipeline_matches_device_run(gpu) -> None:
+    """ndf_batch_run_host (pageable inputs, grouped uploads, kernels and
+    downloads overlapping) equals the device-buffer run, twice in a row,
+    with empty images, box / histogram images (own launches) and family
+    images mixed; the second call reuses the pipeline's buffers."""
+    import torch
+
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(11)
+    specs, images = _specs(rng, 27)
+    # Large windows (histogram kernel) and an empty image in the mix.
+    big = rng.normal(500, 5, size=(211, 190)).astype(np.float32)
+    specs.append(dict(shape=big.shape, kind="median", size=(31, 31), footprint=None, omit_nan=True,
+                      ignore_inf=False, min_count=1, parameter=0, percentile=50.0, mode="nearest"))
+    images.append(big)
+    specs.insert(5, dict(shape=(0, 7), kind="median", size=(3, 3), footprint=None, omit_nan=True,
+                         ignore_inf=False, min_count=1, parameter=0, percentile=50.0, mode="reflect"))
+    images.insert(5, np.empty((0, 7), np.float32))
+    batch = _core.Batch(specs)
+    device = torch.device("cuda")
+    d_in = [torch.from_numpy(im).to(device) for im in images]
+    d_out = [torch.empty_like(t) for t in d_in]
+    stream = torch.cuda.current_stream().cuda_stream
+    batch.run_device([t.data_ptr() for t in d_in], [t.data_ptr() for t in d_out], stream)
+    torch.cuda.synchronize()
+    expected = [t.cpu().numpy() for t in d_out]
+    for _ in range(2):
+        got = batch.run_host(images)
+        for want, have, spec in zip(expected, got, specs):
+            assert have.shape == want.shape
+            np.testing.assert_array_equal(bits(have), bits(want), err_msg=str(spec["kind"]))
+    outputs = [np.full(im.shape, 3.0, np.float32) for im in images]
+    assert batch.run_host(images, outputs) is outputs
+    for want, have in zip(expected, outputs):
+        np.testing.assert_array_equal(bits(have), bits(want))
+    batch.close()
