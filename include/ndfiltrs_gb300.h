@@ -204,6 +204,22 @@ int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32_t dtype, i
                                  int32_t ignore_inf, uint64_t min_count, uint64_t parameter,
                                  double percentile, void* stream);
 
+/* ---- Autotuner. A plan whose window can run on several kernels (sliding
+ * histogram, box pair kernel, register network, radix select; output tile
+ * shapes) takes the choice measured for its (device, dtype, statistic,
+ * policy, window box, tap count, footprint class); every choice gives the
+ * same results. Modes: 0 = off (built-in preference order), 1 = plans use
+ * measured choices and batches measure the keys they miss (the default),
+ * 2 = every plan measures the keys it misses. Measured choices persist in a
+ * text file: `cache_path` NULL keeps the current file, "" keeps choices in
+ * memory only. The initial mode comes from the environment variable
+ * NDF_AUTOTUNE and the initial file from NDF_AUTOTUNE_CACHE (default
+ * $XDG_CACHE_HOME or ~/.cache, then ndfiltrs_gb300/autotune.txt). No
+ * counterpart in the reference. */
+int ndf_set_autotune(int32_t mode, const char* cache_path);
+/* Number of measured choices known (loading the file first). */
+int32_t ndf_autotune_entries(void);
+
 /* Number of SMs, device name and compute capability of device 0. */
 int ndf_device_info(int32_t* sm_count, int32_t* major, int32_t* minor, char* name,
                     size_t name_capacity);

@@ -25,12 +25,13 @@ from ._api import (
     std_filter,
     var_filter,
 )
-from ._core import Batch, Plan, device_info
+from ._core import Batch, Plan, autotune_entries, device_info, set_autotune
 from ._robust import nanpercentile_filter, percentile_filter
 
 __all__ = [
     "Batch",
     "Plan",
+    "autotune_entries",
     "device_info",
     "get_num_threads",
     "kernels",
@@ -47,6 +48,7 @@ __all__ = [
     "nanvar_filter",
     "percentile_filter",
     "rank_filter",
+    "set_autotune",
     "std_filter",
     "var_filter",
 ]

@@ -147,6 +147,9 @@ def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
                 handle.ndf_batch_run.restype = ctypes.c_int
                 handle.ndf_batch_run_host.argtypes = [plan_p, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
                 handle.ndf_batch_run_host.restype = ctypes.c_int
+                handle.ndf_set_autotune.argtypes = [ctypes.c_int32, ctypes.c_char_p]
+                handle.ndf_set_autotune.restype = ctypes.c_int
+                handle.ndf_autotune_entries.restype = ctypes.c_int32
                 handle.ndf_batch_launches.argtypes = [plan_p]
                 handle.ndf_batch_launches.restype = ctypes.c_int32
             _lib, _pylib = lib, pylib
@@ -537,3 +540,19 @@ def device_info() -> dict:
         "capability": (major.value, minor.value),
         "name": name.value.decode(),
     }
+
+
+def set_autotune(mode: int, cache_path: str | None = None) -> None:
+    """Kernel-choice autotuner: 0 off, 1 plans use measured choices and
+    batches measure what they miss (default), 2 every plan measures what it
+    misses. ``cache_path``: None keeps the current file, "" keeps choices in
+    memory only. Choices change speed only, never results."""
+    lib, _ = _load()
+    path = None if cache_path is None else str(cache_path).encode()
+    _check(lib.ndf_set_autotune(int(mode), path), lib)
+
+
+def autotune_entries() -> int:
+    """Number of measured kernel choices known to the autotuner."""
+    lib, _ = _load()
+    return int(lib.ndf_autotune_entries())

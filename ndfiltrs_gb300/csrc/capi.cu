@@ -399,6 +399,105 @@ int upload_percentile_table(Plan& p) {
   return NDF_OK;
 }
 
+// Output tile of the one-thread-per-output tile kernels.
+void set_tile(Plan& p, int tw, int th) {
+  const Geom3& g = p.tile.g;
+  Tile& t = p.tile.t;
+  t.TW = tw;
+  t.TH = th;
+  t.SW = t.TW + g.kw - 1;
+  t.SH = t.TH + g.kh - 1;
+  t.tiles_x = (g.W + t.TW - 1) / t.TW;
+  t.tiles_y = (g.H + t.TH - 1) / t.TH;
+  t.tiles = t.tiles_x * t.tiles_y * g.D;
+}
+
+// Kernel candidates of a tileable plan whose shared memory fits, in the
+// default preference order (the first is used unless the autotuner knows
+// better). Every candidate gives bit-identical order statistics; the
+// moments candidates differ only in the output tile.
+std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
+  std::vector<Candidate> out;
+  const Geom3& g = p.tile.g;
+  const bool line = g.H == 1;
+  const std::vector<std::pair<int, int>> tiles =
+      line ? std::vector<std::pair<int, int>>{{256, 1}}
+           : std::vector<std::pair<int, int>>{{32, 8}, {16, 16}, {64, 4}};
+  auto fits_tile = [&](int tw, int th, bool moments) {
+    Tile t = p.tile.t;
+    t.TW = tw;
+    t.TH = th;
+    t.SW = tw + g.kw - 1;
+    t.SH = th + g.kh - 1;
+    return (moments ? tile_moments_smem(p, t) : tile_select_smem(p, t)) <= (size_t)smem_limit;
+  };
+  if (is_moment(p.r.kind)) {
+    for (auto [tw, th] : tiles)
+      if (fits_tile(tw, th, true)) out.push_back({Algo::kMomentsTile, tw, th});
+    return out;
+  }
+  const bool hist_kind = p.r.kind == kMedianHistogram || p.r.kind == kRankHistogram;
+  const int width = network_width_for(p.dtype, p.r.count);
+  bool hist_ok = false;
+  if (histogram_supported(p)) {
+    Plan probe = p;  // configuration only, no device resources
+    histogram_configure(probe);
+    hist_ok = histogram_smem(probe) <= (size_t)smem_limit;
+  }
+  if (hist_ok && (hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
+  if (p.footprint.empty() && g.kd == 1 && !line && box_supported(p.dtype, g.kh, g.kw)) {
+    Tile bt = box_tile(g);
+    if (tile_select_smem(p, bt) <= (size_t)smem_limit) out.push_back({Algo::kTileBox, bt.TW, bt.TH});
+  }
+  for (auto [tw, th] : tiles) {
+    if (!fits_tile(tw, th, false)) continue;
+    if (width > 0)
+      out.push_back({Algo::kTileNetwork, tw, th});
+    else if (!hist_ok)
+      out.push_back({Algo::kTileRadix, tw, th});
+  }
+  if (hist_ok && !(hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
+  if (out.empty() && fits_tile(tiles[0].first, tiles[0].second, false))
+    out.push_back({Algo::kTileRadix, tiles[0].first, tiles[0].second});
+  return out;
+}
+
+int apply_candidate_impl(Plan& p, const Candidate& c, int smem_limit) {
+  p.algo = c.algo;
+  switch (c.algo) {
+    case Algo::kHistogram: {
+      histogram_configure(p);
+      p.smem_bytes = histogram_smem(p);
+      if (p.smem_bytes > (size_t)smem_limit) return fail(NDF_ERR_UNSUPPORTED, "window too large");
+      cudaError_t e = histogram_allocate(p);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+      }
+      return NDF_OK;
+    }
+    case Algo::kTileBox:
+      p.tile.t = box_tile(p.tile.g);
+      p.smem_bytes = tile_select_smem(p, p.tile.t);
+      return NDF_OK;
+    case Algo::kTileNetwork:
+      set_tile(p, c.tw, c.th);
+      p.smem_bytes = tile_select_smem(p, p.tile.t);
+      p.network = network_width_for(p.dtype, p.r.count);
+      return NDF_OK;
+    case Algo::kTileRadix:
+      set_tile(p, c.tw, c.th);
+      p.smem_bytes = tile_select_smem(p, p.tile.t);
+      return upload_tile_taps(p);
+    case Algo::kMomentsTile:
+      set_tile(p, c.tw, c.th);
+      p.smem_bytes = tile_moments_smem(p, p.tile.t);
+      return upload_tile_taps(p);
+    default:
+      return fail(NDF_ERR_UNSUPPORTED, "not a tile kernel");
+  }
+}
+
 int choose_algorithm(Plan& p, int smem_limit) {
   if (p.n_out == 0) {
     p.algo = Algo::kEmpty;
@@ -409,62 +508,18 @@ int choose_algorithm(Plan& p, int smem_limit) {
     if (rc != NDF_OK) return rc;
   }
   const bool tileable = p.ndim <= 3 && p.r.count <= (1 << 24);
-  if (tileable) setup_tile(p);
-  if (is_moment(p.r.kind)) {
-    if (tileable) {
-      size_t smem = tile_moments_smem(p, p.tile.t);
-      if (smem <= (size_t)smem_limit) {
-        p.algo = Algo::kMomentsTile;
-        p.smem_bytes = smem;
-        return upload_tile_taps(p);
-      }
+  if (tileable) {
+    setup_tile(p);
+    std::vector<Candidate> cands = plan_candidates_impl(p, smem_limit);
+    if (!cands.empty()) {
+      Candidate pick = cands[0];
+      if (cands.size() > 1) pick = autotune_pick(p, cands, smem_limit);
+      return apply_candidate_impl(p, pick, smem_limit);
     }
+  }
+  if (is_moment(p.r.kind)) {
     p.algo = Algo::kMomentsGeneric;
     return setup_generic(p);
-  }
-  if (tileable) {
-    // 1-D/2-D windows: the sliding rank histogram for the histogram kinds
-    // (rectangular windows only), and for every order statistic whose window
-    // is too wide for a register network (footprints slide their run ends).
-    const bool hist_kind = p.r.kind == kMedianHistogram || p.r.kind == kRankHistogram;
-    if (histogram_supported(p) &&
-        (hist_kind || network_width_for(p.dtype, p.r.count) == 0)) {
-      histogram_configure(p);
-      p.smem_bytes = histogram_smem(p);
-      if (p.smem_bytes <= (size_t)smem_limit) {
-        p.algo = Algo::kHistogram;
-        cudaError_t e = histogram_allocate(p);
-        if (e != cudaSuccess) {
-          cudaGetLastError();
-          return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
-        }
-        return NDF_OK;
-      }
-    }
-    // Box windows with a compiled pair kernel (2-D, 3x3 / 5x5 / 7x7).
-    if (p.footprint.empty() && p.tile.g.kd == 1 && p.tile.g.H > 1 && !hist_kind &&
-        box_supported(p.dtype, p.tile.g.kh, p.tile.g.kw)) {
-      Tile bt = box_tile(p.tile.g);
-      size_t smem = tile_select_smem(p, bt);
-      if (smem <= (size_t)smem_limit) {
-        p.tile.t = bt;
-        p.smem_bytes = smem;
-        p.algo = Algo::kTileBox;
-        return NDF_OK;
-      }
-    }
-    size_t smem = tile_select_smem(p, p.tile.t);
-    if (smem <= (size_t)smem_limit) {
-      int width = network_width_for(p.dtype, p.r.count);
-      p.smem_bytes = smem;
-      if (width > 0) {
-        p.algo = Algo::kTileNetwork;
-        p.network = width;
-        return NDF_OK;
-      }
-      p.algo = Algo::kTileRadix;
-      return upload_tile_taps(p);
-    }
   }
   p.algo = Algo::kGenericSelect;
   return setup_generic(p);
@@ -574,10 +629,17 @@ int batch_build_plan(const ndf_filter_desc* d, Plan& p, int* smem_limit) {
   }
   rc = ensure_device(&p.device, &p.sm_count, smem_limit);
   if (rc != NDF_OK) return rc;
+  p.may_tune = true;  // batches measure kernel choices they have not seen
   return choose_algorithm(p, *smem_limit);
 }
 
 void batch_release_plan(Plan& p) { release(p); }
+
+// Plan internals used by the autotuner (autotune.cu).
+void plan_setup_tile(Plan& p) { setup_tile(p); }
+void plan_release(Plan& p) { release(p); }
+int plan_run(const Plan& p, const void* in, void* out, cudaStream_t s) { return run_plan(p, in, out, s); }
+int plan_apply(Plan& p, const Candidate& c, int smem_limit) { return apply_candidate_impl(p, c, smem_limit); }
 
 }  // namespace ndf
 

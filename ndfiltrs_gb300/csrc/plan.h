@@ -131,9 +131,31 @@ struct Plan {
   std::vector<uint16_t> hist_lists;
   uint16_t* d_hist_lists = nullptr;
   PctEntry* d_pct = nullptr;  // percentile rank table (kPercentile, q < 100)
+
+  // Kernel choice: measure candidates not in the autotune cache (batches).
+  bool may_tune = false;
 };
 
 const char* algo_name(Algo a);
+
+// A kernel choice for a tileable plan: the algorithm and, for the tile
+// kernels, the output tile (tw x th outputs, one thread per output; 0 for
+// the histogram, whose block comes from its cost model).
+struct Candidate {
+  Algo algo = Algo::kEmpty;
+  int tw = 0, th = 0;
+};
+
+// Plan internals (capi.cu) used by the autotuner.
+void plan_setup_tile(Plan& p);
+void plan_release(Plan& p);
+int plan_run(const Plan& p, const void* in, void* out, cudaStream_t s);
+int plan_apply(Plan& p, const Candidate& c, int smem_limit);
+
+// The autotuner (autotune.cu): picks one of `cands` (two or more) by the
+// cached or, when the plan may tune, freshly measured timings of the plan's
+// (device, dtype, statistic, window, footprint class) key.
+Candidate autotune_pick(const Plan& p, const std::vector<Candidate>& cands, int smem_limit);
 
 // Raise a kernel's dynamic shared-memory limit to the device maximum, once.
 // The attribute belongs to the function, not to a plan, so it is never

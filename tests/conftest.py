@@ -10,6 +10,7 @@ exports every declared symbol, without touching a GPU.
 from __future__ import annotations
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -21,6 +22,12 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
+
+# Kernel choices stay on the built-in preference order unless a test turns
+# the autotuner on, so that assertions on a plan's algorithm do not depend on
+# a choice cache left by an earlier process.
+os.environ.setdefault("NDF_AUTOTUNE", "0")
+os.environ.setdefault("NDF_AUTOTUNE_CACHE", "")
 
 
 def pytest_configure(config: pytest.Config) -> None:

@@ -93,3 +93,48 @@ def test_validation_errors_before_device_work(gpu) -> None:
 
 def test_get_num_threads_is_device_parallelism(gpu) -> None:
     assert gpu.get_num_threads() == gpu.device_info()["sm_count"]
+
+
+def test_autotuner_changes_speed_not_results(gpu, oracle) -> None:
+    """With the autotuner measuring every plan (mode 2, in-memory cache), the
+    chosen kernels give the same bits as the built-in choice and the oracle,
+    and each key is measured once."""
+    import ndfiltrs_gb300 as nf
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(3)
+    image = rng.normal(1000, 10, size=(150, 170)).astype(np.float32)
+    image[rng.random(image.shape) < 0.02] = np.nan
+    disk = np.add.outer(np.arange(-6, 7) ** 2, np.arange(-6, 7) ** 2) <= 36
+    cases = [("median", (9, 9), None), ("percentile", (15, 15), None), ("median", None, disk),
+             ("std", (11, 11), None)]
+    try:
+        nf.set_autotune(0, "")
+        baseline = []
+        for kind, size, fp in cases:
+            shape = fp.shape if fp is not None else size
+            with _core.Plan(image.shape, np.float32, kind, shape, footprint=fp, omit_nan=True,
+                            percentile=84.0, parameter=1 if kind == "std" else 0) as plan:
+                baseline.append(plan.run_host(image))
+        nf.set_autotune(2, "")
+        assert nf.autotune_entries() == 0
+        for (kind, size, fp), want in zip(cases, baseline):
+            shape = fp.shape if fp is not None else size
+            for _ in range(2):
+                with _core.Plan(image.shape, np.float32, kind, shape, footprint=fp, omit_nan=True,
+                                percentile=84.0, parameter=1 if kind == "std" else 0) as plan:
+                    got = plan.run_host(image)
+                np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32), err_msg=kind)
+            if kind != "std":
+                ref = oracle.window_filter(image, kind, shape, footprint=fp, omit_nan=True, q=84.0)
+                np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+        # Keys with a single candidate (e.g. a 15 x 15 percentile, histogram
+        # only) need no measurement; every other key was measured once.
+        measured = nf.autotune_entries()
+        assert 1 <= measured < len(cases)
+        for kind, size, fp in cases:
+            shape = fp.shape if fp is not None else size
+            _core.Plan(image.shape, np.float32, kind, shape, footprint=fp, omit_nan=True).close()
+        assert nf.autotune_entries() == measured
+    finally:
+        nf.set_autotune(0, "")
