@@ -95,14 +95,77 @@ def precision_image(n: int = 4096, seed: int = 4, dtype=np.float32) -> np.ndarra
     return image.astype(dtype)
 
 
+def cube_image(seed: int = 2) -> np.ndarray:
+    """64 x 1024 x 1024 float32 cube with the robust image's distribution."""
+    rng = np.random.default_rng(seed)
+    shape = (64, 1024, 1024)
+    x = np.arange(shape[2], dtype=np.float32)
+    image = (np.float32(1000) + np.float32(50) * x / np.float32(shape[2]))[None, None, :] + \
+        rng.standard_normal(shape, dtype=np.float32) * np.float32(10)
+    outliers = rng.random(shape, dtype=np.float32) < 0.002
+    image[outliers] = rng.uniform(2000.0, 60000.0, size=int(outliers.sum())).astype(np.float32)
+    image[rng.random(shape, dtype=np.float32) < 0.005] = np.nan
+    image[rng.random(shape, dtype=np.float32) < 0.001] = np.inf
+    return image
+
+
+def _ring() -> np.ndarray:
+    from ndfiltrs_gb300 import kernels
+
+    return kernels.ring(4, 6, 2) != 0
+
+
+def _tophat() -> np.ndarray:
+    from ndfiltrs_gb300 import kernels
+
+    return kernels.tophat(1, 2) != 0
+
+
+class Workload:
+    """One benchmark configuration: an image generator and the filter."""
+
+    def __init__(self, gen, kind, size, mode, omit=True, ignore_inf=False, min_count=1, parameter=0,
+                 q=50.0, footprint=None, origin=None):
+        self.gen, self.kind, self.size, self.mode = gen, kind, size, mode
+        self.omit, self.ignore_inf, self.min_count, self.parameter = omit, ignore_inf, min_count, parameter
+        self.q, self.footprint_fn, self.origin = q, footprint, origin
+
+    def footprint(self):
+        return self.footprint_fn() if self.footprint_fn is not None else None
+
+    def window(self):
+        fp = self.footprint()
+        return tuple(fp.shape) if fp is not None else tuple(self.size)
+
+
 WORKLOADS = {
-    # name: (generator, kind, size, mode, omit_nan, ignore_inf, min_count, parameter)
-    "nanmedian_sortnet_5x5_4096_f32": (lambda: robust_image(4096), "median_network", (5, 5), "reflect", True, False, 1, 0),
-    "nanmedian_direct_3x3_2048_f32": (lambda: gaussian_image(2048), "median", (3, 3), "reflect", True, False, 1, 0),
-    "nanmedian_sortnet_7x7_4096_f32": (lambda: robust_image(4096), "median_network", (7, 7), "reflect", True, False, 1, 0),
-    "rank2_5x5_4096_f32": (lambda: robust_image(4096), "rank", (5, 5), "reflect", False, False, 1, 2),
-    "nanmedian_hist_65x65_4096_f32": (lambda: sky_image(4096), "median_histogram", (65, 65), "nearest", True, False, 1, 0),
-    "nanstd_31x31_4096_f32": (lambda: precision_image(4096), "std", (31, 31), "reflect", True, True, 5, 1),
+    # Robust-statistics image, 4096 x 4096 float32 (sortnet / box kernels).
+    "nanmedian_sortnet_5x5_4096_f32": Workload(lambda: robust_image(4096), "median_network", (5, 5), "reflect"),
+    "nanmedian_sortnet_7x7_4096_f32": Workload(lambda: robust_image(4096), "median_network", (7, 7), "reflect"),
+    "rank2_5x5_4096_f32": Workload(lambda: robust_image(4096), "rank", (5, 5), "reflect", omit=False, parameter=2),
+    "nanpercentile84_5x5_4096_f32": Workload(lambda: robust_image(4096), "percentile", (5, 5), "reflect", q=84.0),
+    "nanmedian_ring_4_6_4096_f32": Workload(lambda: robust_image(4096), "median_network", None, "reflect",
+                                            footprint=_ring),
+    "nanmedian_tophat1_4096_f32": Workload(lambda: robust_image(4096), "median_network", None, "constant",
+                                           footprint=_tophat, origin=(1, -1)),
+    "nanmedian_sortnet_3x5x5_cube_f32": Workload(cube_image, "median_network", (3, 5, 5), "reflect"),
+    # Gaussian image, 2048 x 2048 float32, direct 3 x 3.
+    "nanmedian_direct_3x3_2048_f32": Workload(lambda: gaussian_image(2048), "median", (3, 3), "reflect"),
+    # Sky image, histogram method, mode nearest.
+    "nanmedian_hist_65x65_4096_f32": Workload(lambda: sky_image(4096), "median_histogram", (65, 65), "nearest"),
+    "nanmedian_hist_65x65_8192_f32": Workload(lambda: sky_image(8192), "median_histogram", (65, 65), "nearest"),
+    "nanmedian_hist_129x129_8192_f32": Workload(lambda: sky_image(8192), "median_histogram", (129, 129), "nearest"),
+    "nanmedian_hist_65x65_8192_f64": Workload(lambda: sky_image(8192, dtype=np.float64), "median_histogram",
+                                              (65, 65), "nearest"),
+    "nanmedian_hist_129x129_8192_f64": Workload(lambda: sky_image(8192, dtype=np.float64), "median_histogram",
+                                                (129, 129), "nearest"),
+    # Precision image, nanstd (FP32-compensated moments).
+    "nanstd_31x31_4096_f32": Workload(lambda: precision_image(4096), "std", (31, 31), "reflect", ignore_inf=True,
+                                      min_count=5, parameter=1),
+    "nanstd_7x51_4096_f32": Workload(lambda: precision_image(4096), "std", (7, 51), "reflect", ignore_inf=True,
+                                     min_count=5, parameter=1),
+    "nanstd_31x31_4096_f64": Workload(lambda: precision_image(4096, dtype=np.float64), "std", (31, 31), "reflect",
+                                      ignore_inf=True, min_count=5, parameter=1),
 }
 DEFAULT_WORKLOAD = "nanmedian_sortnet_5x5_4096_f32"
 
@@ -189,32 +252,38 @@ def cpu_baseline(image: np.ndarray, spec, budget_s: float = 3.0, threads: int | 
     from oracle import oracle
 
     oracle.build()
-    _, kind, size, mode, omit, ignore_inf, min_count, parameter = spec
     threads = threads or (os.cpu_count() or 1)
-    width = image.shape[1]
+    per_row = image[0].size
+    first = 16 if image.ndim < 3 else 2
 
     def run(rows: int) -> float:
         strip = np.ascontiguousarray(image[:rows])
         start = time.perf_counter()
-        oracle.window_filter(strip, oracle_kind(kind), size, mode=mode, omit_nan=omit,
-                             ignore_inf=ignore_inf, min_count=min_count, parameter=parameter,
-                             threads=threads)
+        oracle_filter(oracle, spec, strip, threads)
         return time.perf_counter() - start
 
-    rows = 16
-    elapsed = run(rows)
-    rows = int(min(image.shape[0], max(16, rows * budget_s / max(elapsed, 1e-6) / 3)))
+    elapsed = run(first)
+    rows = int(min(image.shape[0], max(first, first * budget_s / max(elapsed, 1e-6) / 3)))
     times = [run(rows) for _ in range(3)]
     seconds = statistics.median(times)
-    mpix = rows * width / seconds / 1e6
+    mpix = rows * per_row / seconds / 1e6
+    sample_shape = "x".join(str(v) for v in (rows,) + image.shape[1:])
     return {
         "value": round(mpix, 3),
         "unit": "Mpix/s",
         "cores": threads,
         "kind": "port",
-        "sample": f"{rows}x{width} strip of the same image, median of 3 calls, "
-                  f"oracle restatement of the reference algorithm ({kind}), {threads} threads",
+        "rows": rows,
+        "sample": f"{sample_shape} leading slab of the same image, median of 3 calls, "
+                  f"oracle restatement of the reference algorithm ({spec.kind}), {threads} threads",
     }
+
+
+def oracle_filter(oracle, spec, array, threads=None):
+    return oracle.window_filter(array, spec.kind, spec.window(), footprint=spec.footprint(),
+                                origin=spec.origin if spec.origin is not None else 0, mode=spec.mode, omit_nan=spec.omit,
+                                ignore_inf=spec.ignore_inf, min_count=spec.min_count,
+                                parameter=spec.parameter, q=spec.q, threads=threads)
 
 
 # ---------------------------------------------------------------------------
@@ -425,22 +494,19 @@ def precision_study(rows: int = 192, width: int = 4096) -> dict:
 # ---------------------------------------------------------------------------
 
 def run_reference(args, spec, workload: str) -> None:
-    image = spec[0]()
+    image = spec.gen()
     steps, warmup = args.steps, args.warmup
     base = cpu_baseline(image, spec, budget_s=1.0)
     from oracle import oracle
 
-    _, kind, size, mode, omit, ignore_inf, min_count, parameter = spec
-    rows = int(base["sample"].split("x")[0])
+    rows = base["rows"]
     strip = np.ascontiguousarray(image[:rows])
     threads = base["cores"]
     for _ in range(warmup):
-        oracle.window_filter(strip, kind, size, mode=mode, omit_nan=omit, ignore_inf=ignore_inf,
-                             min_count=min_count, parameter=parameter, threads=threads)
+        oracle_filter(oracle, spec, strip, threads)
     start = time.perf_counter()
     for _ in range(steps):
-        oracle.window_filter(strip, kind, size, mode=mode, omit_nan=omit, ignore_inf=ignore_inf,
-                             min_count=min_count, parameter=parameter, threads=threads)
+        oracle_filter(oracle, spec, strip, threads)
     elapsed = time.perf_counter() - start
     value = strip.size * steps / elapsed / 1e6
     base["value"] = round(value, 3)
@@ -456,7 +522,7 @@ def run_reference(args, spec, workload: str) -> None:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32" if image.dtype == np.float32 else "f64",
         "data": "synthetic",
         "config": {"workload": workload, "sample_rows": rows, "image": list(image.shape)},
         "cpu_baseline": base,
@@ -507,22 +573,30 @@ def main() -> None:
     __graft_entry__.build()
     import ndfiltrs_gb300 as nf
 
-    gen, kind, size, mode, omit, ignore_inf, min_count, parameter = spec
-    image = gen() if rank == 0 or world == 1 else None
-    if image is None:
-        image = gen()  # every rank builds its own replica of the workload
+    image = spec.gen()  # every rank builds its own replica of the workload
     shape = image.shape
     pixels = image.size
-    plan = nf.Plan(shape, image.dtype, kind, size, mode=[mode] * image.ndim, omit_nan=omit,
-                   ignore_inf=ignore_inf, min_count=min_count, parameter=parameter)
+    kind, mode = spec.kind, spec.mode
+
+    def make_plan(shape_):
+        return nf.Plan(shape_, image.dtype, kind, spec.window(), footprint=spec.footprint(),
+                       origin=spec.origin, mode=[mode] * image.ndim, omit_nan=spec.omit,
+                       ignore_inf=spec.ignore_inf, min_count=spec.min_count, parameter=spec.parameter,
+                       percentile=spec.q)
+
+    plan = make_plan(shape)
     device = torch.device("cuda", local_rank)
-    buffers = [torch.from_numpy(np.roll(image, k * 97, axis=1).copy()).to(device) for k in range(4)]
+    # Rotate over enough input buffers that together they exceed the 129 MB L2
+    # three times over, so no step reads an input the previous ones left in L2.
+    image_bytes = image.nbytes
+    n_buffers = max(4, -(-3 * 129 * 2**20 // image_bytes))
+    buffers = [torch.from_numpy(np.roll(image, k * 97, axis=-1).copy()).to(device) for k in range(n_buffers)]
     outputs = [torch.empty_like(buffers[0]) for _ in range(2)]
     stream = torch.cuda.Stream(device)
     handle = stream.cuda_stream
 
     def step(i: int) -> None:
-        plan.run_device(buffers[i % 4].data_ptr(), outputs[i % 2].data_ptr(), handle)
+        plan.run_device(buffers[i % n_buffers].data_ptr(), outputs[i % 2].data_ptr(), handle)
 
     for i in range(args.warmup):
         step(i)
@@ -551,18 +625,18 @@ def main() -> None:
     if rank == 0:
         from oracle import oracle
 
-        rows = 64
+        rows = 64 if image.ndim < 3 else 4
         sample = np.ascontiguousarray(image[:rows])
-        gpu_sample = nf.Plan(sample.shape, sample.dtype, kind, size, mode=[mode] * 2, omit_nan=omit,
-                             ignore_inf=ignore_inf, min_count=min_count, parameter=parameter).run_host(sample)
-        expected = oracle.window_filter(sample, kind, size, mode=mode, omit_nan=omit, ignore_inf=ignore_inf,
-                                        min_count=min_count, parameter=parameter)
-        check = bool(np.array_equal(gpu_sample.view(np.uint32), expected.view(np.uint32))) \
+        with make_plan(sample.shape) as sample_plan:
+            gpu_sample = sample_plan.run_host(sample)
+        expected = oracle_filter(oracle, spec, sample)
+        ubits = np.uint32 if image.dtype == np.float32 else np.uint64
+        check = bool(np.array_equal(gpu_sample.view(ubits), expected.view(ubits))) \
             if kind not in ("mean", "var", "std") else None
 
     # End to end through the C-ABI host entry point with pinned buffers.
     host_in = torch.from_numpy(image).pin_memory()
-    host_out = torch.empty(shape, dtype=torch.float32).pin_memory()
+    host_out = torch.empty(shape, dtype=torch.float32 if image.dtype == np.float32 else torch.float64).pin_memory()
     in_np, out_np = host_in.numpy(), host_out.numpy()
     e2e_steps = max(3, min(args.steps, 50))
     for _ in range(2):
@@ -601,17 +675,21 @@ def main() -> None:
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32",
+            "dtype": "f32" if image.dtype == np.float32 else "f64",
             "data": "synthetic",
             "config": {
                 "workload": args.workload,
                 "image": list(shape),
                 "kind": kind,
-                "size": list(size),
+                "size": list(spec.window()),
+                "footprint": None if spec.footprint_fn is None else int(spec.footprint().sum()),
+                "origin": spec.origin,
+                "percentile": spec.q if kind == "percentile" else None,
                 "mode": mode,
-                "omit_nan": omit,
+                "omit_nan": spec.omit,
                 "algorithm": plan.algorithm,
-                "l2": "inputs rotate over 4 device buffers (4 x 67 MB > 129 MB L2)",
+                "l2": f"inputs rotate over {n_buffers} device buffers "
+                      f"({n_buffers} x {image_bytes / 1e6:.0f} MB > 129 MB L2)",
                 "parallelism": f"replicas x{world}",
             },
             "e2e": {

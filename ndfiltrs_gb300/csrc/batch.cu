@@ -26,6 +26,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/ndfiltrs_gb300.h"
@@ -56,17 +57,15 @@ struct BatchTask {
   int count;
 };
 
-enum Family : int {
-  kNet8 = 0,
-  kNet16,
-  kNet32,
-  kNet64,
-  kNet128,
-  kRadix,
-  kMomentsFP32C,
-  kMomentsFP64,
-  kFamilies,
-};
+// Kernel families: a register network per (width, epilogue) pair (the
+// widths of network_width_for; epilogue 0 = any selection kind, 1 = medians
+// only), the radix select and the two moments precisions.
+constexpr int kNetWidths[] = {8, 16, 32, 48, 64, 80, 96, 112, 128};
+constexpr int kNumNetWidths = sizeof(kNetWidths) / sizeof(kNetWidths[0]);
+constexpr int kRadix = 2 * kNumNetWidths;
+constexpr int kMomentsFP32C = kRadix + 1;
+constexpr int kMomentsFP64 = kRadix + 2;
+constexpr int kFamilies = kRadix + 3;
 
 __device__ __forceinline__ int find_task(const BatchTask* tasks, int ntasks, long long tile) {
   int lo = 0, hi = ntasks - 1;
@@ -111,7 +110,7 @@ __device__ __forceinline__ bool load_task(SharedTask& st, const BatchTask* tasks
   return changed;
 }
 
-template <int N>
+template <int N, int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     batch_network_kernel(const BatchTask* __restrict__ tasks, int ntasks, long long total_tiles,
                          const int32_t* __restrict__ pool) {
@@ -123,7 +122,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   for (long long tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
     load_task(st, tasks, ntasks, tile, pool, taps_s, N);
     const BatchTask& t = st.task;
-    net::tile_network_body<float, N, 0, 0>(t.in, t.out, t.tile, tile - t.first_tile, smem_raw,
+    net::tile_network_body<float, N, 0, MODE>(t.in, t.out, t.tile, tile - t.first_tile, smem_raw,
                                            [&](int i) { return taps_s[i]; });
     __syncthreads();
   }
@@ -162,26 +161,20 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-const void* family_kernel(int family) {
-  switch (family) {
-    case kNet8:
-      return (const void*)batch_network_kernel<8>;
-    case kNet16:
-      return (const void*)batch_network_kernel<16>;
-    case kNet32:
-      return (const void*)batch_network_kernel<32>;
-    case kNet64:
-      return (const void*)batch_network_kernel<64>;
-    case kNet128:
-      return (const void*)batch_network_kernel<128>;
-    case kRadix:
-      return (const void*)batch_radix_kernel;
-    case kMomentsFP32C:
-      return (const void*)batch_moments_kernel<0>;
-    default:
-      return (const void*)batch_moments_kernel<1>;
-  }
+template <int... I>
+const void* network_kernel_at(int family, std::integer_sequence<int, I...>) {
+  static const void* const table[] = {(const void*)batch_network_kernel<kNetWidths[I / 2], I % 2>...};
+  return table[family];
 }
+
+const void* family_kernel(int family) {
+  if (family < kRadix)
+    return network_kernel_at(family, std::make_integer_sequence<int, 2 * kNumNetWidths>{});
+  if (family == kRadix) return (const void*)batch_radix_kernel;
+  if (family == kMomentsFP32C) return (const void*)batch_moments_kernel<0>;
+  return (const void*)batch_moments_kernel<1>;
+}
+
 
 // One image group's launches: a persistent launch per kernel family over the
 // group's images of that family, plus the images that run their own plan's
@@ -342,20 +335,10 @@ namespace {
 int family_for(const Plan& p) {
   if (p.algo == Algo::kMomentsTile) return p.r.moments == NDF_MOMENTS_FP64 ? kMomentsFP64 : kMomentsFP32C;
   if (p.algo == Algo::kTileNetwork) {
-    switch (p.network) {
-      case 8:
-        return kNet8;
-      case 16:
-        return kNet16;
-      case 32:
-        return kNet32;
-      case 64:
-        return kNet64;
-      case 128:
-        return kNet128;
-      default:
-        return -1;
-    }
+    const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork || p.r.kind == kMedianHistogram;
+    for (int w = 0; w < kNumNetWidths; ++w)
+      if (kNetWidths[w] == p.network) return 2 * w + (median ? 1 : 0);
+    return -1;
   }
   if (p.algo == Algo::kTileRadix) return kRadix;
   return -1;  // box pair, histogram and generic kernels keep their own launch
@@ -456,35 +439,10 @@ int build_segment(ndf_batch* b, Segment& s, const std::vector<int>& images) {
   return NDF_OK;
 }
 
-void launch_family(int fam, const FamilyState& f, cudaStream_t s) {
-  const int ntasks = (int)f.tasks.size();
-  dim3 grid(f.grid), block(kThreads);
-  switch (fam) {
-    case kNet8:
-      batch_network_kernel<8><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    case kNet16:
-      batch_network_kernel<16><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    case kNet32:
-      batch_network_kernel<32><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    case kNet64:
-      batch_network_kernel<64><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    case kNet128:
-      batch_network_kernel<128><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    case kRadix:
-      batch_radix_kernel<<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    case kMomentsFP32C:
-      batch_moments_kernel<0><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-    default:
-      batch_moments_kernel<1><<<grid, block, f.smem, s>>>(f.d_tasks, ntasks, f.tiles, f.d_pool);
-      break;
-  }
+cudaError_t launch_family(int fam, FamilyState& f, cudaStream_t s) {
+  int ntasks = (int)f.tasks.size();
+  void* args[] = {&f.d_tasks, &ntasks, &f.tiles, &f.d_pool};
+  return cudaLaunchKernel(family_kernel(fam), dim3(f.grid), dim3(kThreads), args, f.smem, s);
 }
 
 // (Re)capture a segment's graph for the given buffers when they changed.
@@ -529,8 +487,7 @@ int capture_segment(ndf_batch* b, Segment& s, const void* const* d_in, void* con
     cudaStream_t st = branch();
     e = cudaMemcpyAsync(f.d_tasks, f.h_tasks, f.tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) break;
-    launch_family(fam, f, st);
-    e = cudaGetLastError();
+    e = launch_family(fam, f, st);
     ++launches;
   }
   for (size_t k = 0; k < s.own.size() && e == cudaSuccess && rc == NDF_OK; ++k) {

@@ -5,8 +5,9 @@
 //   odd-even merge network sorts them (replaces Network::new/apply,
 //   src/median_network.rs:116-209, and the per-output selection of
 //   Reduction::finish, src/reduction.rs:78-130). The network width is a
-//   compile-time power of two; padding wires hold the sentinel key, so the
-//   compiler folds their comparators away, and comparators whose outputs no
+//   compile-time constant (8, 16, 32, then multiples of 16); padding wires
+//   hold the sentinel key, so the compiler folds their comparators away, and
+//   comparators whose outputs no
 //   rank of the reduction can reach are removed as dead code (the backward
 //   liveness pruning of the reference's Network::new).
 // * tile_radix: windows too wide for a register network run a bit-serial
@@ -18,19 +19,15 @@
 // key, the largest key, so a sorted window holds its `nv` retained samples
 // first. Propagate windows are NaN when nv != V.
 #include "network.cuh"
+#include "select_launch.cuh"
 
 namespace ndf {
+
+cudaError_t launch_network_wide(const Plan& p, const void* in, void* out, cudaStream_t s);
+
 namespace {
 using namespace net;
-
-template <typename T, int N, int VFIX, int MODE>
-__global__ void __launch_bounds__(kThreads, 1)
-    tile_network_kernel(const T* __restrict__ in, T* __restrict__ out,
-                        const __grid_constant__ TileArgs a, const __grid_constant__ TapTable<N> taps) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  tile_network_body<T, N, VFIX, MODE>(in, out, a, blockIdx.x, smem_raw,
-                                      [&](int i) { return taps.off[i]; });
-}
+using namespace netlaunch;
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -82,40 +79,6 @@ __global__ void __launch_bounds__(kThreads)
 // ---------------------------------------------------------------------------
 // Host launchers.
 
-template <typename T, int N, int VFIX, int MODE>
-cudaError_t launch_network(const Plan& p, const T* in, T* out, cudaStream_t s) {
-  TapTable<N> taps{};
-  const TileArgs& a = p.tile;
-  for (int i = 0; i < N; ++i) {
-    if (i < p.r.count) {
-      const int* bt = &p.box_taps[(size_t)i * 3];
-      taps.off[i] = (bt[0] * a.t.SH + bt[1]) * a.t.SW + bt[2];
-    } else {
-      taps.off[i] = 0;
-    }
-  }
-  auto kernel = tile_network_kernel<T, N, VFIX, MODE>;
-  cudaError_t e =
-      allow_max_smem((const void*)kernel);
-  if (e != cudaSuccess) return e;
-  kernel<<<(unsigned)a.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, a, taps);
-  return cudaGetLastError();
-}
-
-template <typename T, int N>
-cudaError_t dispatch_network_mode(const Plan& p, const T* in, T* out, cudaStream_t s) {
-  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork ||
-                      p.r.kind == kMedianHistogram;
-  if (!median) return launch_network<T, N, 0, 0>(p, in, out, s);
-  if constexpr (sizeof(T) == 4) {
-    // Fixed tap counts of the hot configurations: 3x3, 5x5 and 7x7 boxes.
-    if (N == 16 && p.r.count == 9) return launch_network<T, 16, 9, 1>(p, in, out, s);
-    if (N == 32 && p.r.count == 25) return launch_network<T, 32, 25, 1>(p, in, out, s);
-    if (N == 64 && p.r.count == 49) return launch_network<T, 64, 49, 1>(p, in, out, s);
-  }
-  return launch_network<T, N, 0, 1>(p, in, out, s);
-}
-
 template <typename T>
 cudaError_t launch_tile_select_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   if (p.algo == Algo::kTileBox) return launch_tile_box(p, in, out, s);
@@ -127,12 +90,13 @@ cudaError_t launch_tile_select_t(const Plan& p, const T* in, T* out, cudaStream_
         return dispatch_network_mode<T, 16>(p, in, out, s);
       case 32:
         return dispatch_network_mode<T, 32>(p, in, out, s);
+      case 48:
+        return dispatch_network_mode<T, 48>(p, in, out, s);
       case 64:
         return dispatch_network_mode<T, 64>(p, in, out, s);
-      case 128:
-        if constexpr (sizeof(T) == 4) return dispatch_network_mode<T, 128>(p, in, out, s);
-        return cudaErrorInvalidValue;
       default:
+        // Widths 80 to 128 (float32 keys only).
+        if constexpr (sizeof(T) == 4) return launch_network_wide(p, in, out, s);
         return cudaErrorInvalidValue;
     }
   }
@@ -146,12 +110,20 @@ cudaError_t launch_tile_select_t(const Plan& p, const T* in, T* out, cudaStream_
 
 }  // namespace
 
+// Network width for `count` taps: 8, 16 or 32, then multiples of 16 up to the
+// key type's register limit. A width that is not a power of two is the
+// power-of-two network with its top wires removed (they would hold the
+// sentinel, so their comparators are no-ops), e.g. 849 comparators for 80
+// wires against 1471 for 128.
 int network_width_for(int dtype, int count) {
   int limit = dtype == 0 ? kMaxNetwork32 : kMaxNetwork64;
   if (count > limit) return 0;
-  int n = 8;
-  while (n < count) n <<= 1;
-  return n;
+  if (count <= 32) {
+    int n = 8;
+    while (n < count) n <<= 1;
+    return n;
+  }
+  return (count + 15) / 16 * 16;
 }
 
 size_t tile_select_smem(const Plan& p, const Tile& t) {

@@ -1,0 +1,56 @@
+// Tile network kernels and their launchers, shared by select.cu (network
+// widths up to 64) and select_wide.cu (widths 80 to 128), which compile in
+// parallel.
+#pragma once
+
+#include "network.cuh"
+
+namespace ndf {
+namespace netlaunch {
+using namespace net;
+
+template <typename T, int N, int VFIX, int MODE>
+__global__ void __launch_bounds__(kThreads, 1)
+    tile_network_kernel(const T* __restrict__ in, T* __restrict__ out,
+                        const __grid_constant__ TileArgs a, const __grid_constant__ TapTable<N> taps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  tile_network_body<T, N, VFIX, MODE>(in, out, a, blockIdx.x, smem_raw,
+                                      [&](int i) { return taps.off[i]; });
+}
+
+template <typename T, int N, int VFIX, int MODE>
+cudaError_t launch_network(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  TapTable<N> taps{};
+  const TileArgs& a = p.tile;
+  for (int i = 0; i < N; ++i) {
+    if (i < p.r.count) {
+      const int* bt = &p.box_taps[(size_t)i * 3];
+      taps.off[i] = (bt[0] * a.t.SH + bt[1]) * a.t.SW + bt[2];
+    } else {
+      taps.off[i] = 0;
+    }
+  }
+  auto kernel = tile_network_kernel<T, N, VFIX, MODE>;
+  cudaError_t e =
+      allow_max_smem((const void*)kernel);
+  if (e != cudaSuccess) return e;
+  kernel<<<(unsigned)a.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, a, taps);
+  return cudaGetLastError();
+}
+
+template <typename T, int N>
+cudaError_t dispatch_network_mode(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork ||
+                      p.r.kind == kMedianHistogram;
+  if (!median) return launch_network<T, N, 0, 0>(p, in, out, s);
+  if constexpr (sizeof(T) == 4) {
+    // Fixed tap counts of the hot configurations: 3x3, 5x5 and 7x7 boxes.
+    if (N == 16 && p.r.count == 9) return launch_network<T, 16, 9, 1>(p, in, out, s);
+    if (N == 32 && p.r.count == 25) return launch_network<T, 32, 25, 1>(p, in, out, s);
+    if (N == 64 && p.r.count == 49) return launch_network<T, 64, 49, 1>(p, in, out, s);
+  }
+  return launch_network<T, N, 0, 1>(p, in, out, s);
+}
+
+}  // namespace netlaunch
+}  // namespace ndf
