@@ -220,6 +220,22 @@ int ndf_set_autotune(int32_t mode, const char* cache_path);
 /* Number of measured choices known (loading the file first). */
 int32_t ndf_autotune_entries(void);
 
+/* ---- TMA staging and bounded waits. Interior halo tiles of the tile
+ * kernels are staged by one TMA (cp.async.bulk.tensor) copy each; every
+ * device wait is bounded and a wait that runs out is reported as
+ * NDF_ERR_TIMEOUT by the next synchronizing call. No counterpart in the
+ * reference. */
+/* Turn TMA staging on (default; NDF_TMA=0 in the environment turns it off)
+ * or off. Results are identical either way. */
+int ndf_set_tma(int32_t enabled);
+/* Synchronize the device and read (and clear) the status flags; returns
+ * NDF_ERR_TIMEOUT when a device wait gave up since the last check. */
+int ndf_device_status(uint32_t* flags);
+/* Self-test of the bounded wait: runs a kernel whose barrier wait can never
+ * complete; returns NDF_ERR_TIMEOUT when the wait gave up and reported it,
+ * as it must. */
+int ndf_selftest_wait_timeout(void);
+
 /* Number of SMs, device name and compute capability of device 0. */
 int ndf_device_info(int32_t* sm_count, int32_t* major, int32_t* minor, char* name,
                     size_t name_capacity);

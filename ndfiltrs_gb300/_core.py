@@ -150,6 +150,11 @@ def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
                 handle.ndf_set_autotune.argtypes = [ctypes.c_int32, ctypes.c_char_p]
                 handle.ndf_set_autotune.restype = ctypes.c_int
                 handle.ndf_autotune_entries.restype = ctypes.c_int32
+                handle.ndf_set_tma.argtypes = [ctypes.c_int32]
+                handle.ndf_set_tma.restype = ctypes.c_int
+                handle.ndf_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+                handle.ndf_device_status.restype = ctypes.c_int
+                handle.ndf_selftest_wait_timeout.restype = ctypes.c_int
                 handle.ndf_batch_launches.argtypes = [plan_p]
                 handle.ndf_batch_launches.restype = ctypes.c_int32
             _lib, _pylib = lib, pylib
@@ -556,3 +561,17 @@ def autotune_entries() -> int:
     """Number of measured kernel choices known to the autotuner."""
     lib, _ = _load()
     return int(lib.ndf_autotune_entries())
+
+
+def set_tma(enabled: bool) -> None:
+    """Turn TMA staging of interior tiles on (default) or off; results are
+    identical either way."""
+    lib, _ = _load()
+    _check(lib.ndf_set_tma(int(bool(enabled))), lib)
+
+
+def selftest_wait_timeout() -> int:
+    """Run the bounded-wait self-test; returns the library status code, which
+    is 7 (NDF_ERR_TIMEOUT) when the wait gave up and reported it."""
+    lib, _ = _load()
+    return int(lib.ndf_selftest_wait_timeout())

@@ -33,6 +33,7 @@
 #include "moments.cuh"
 #include "network.cuh"
 #include "plan.h"
+#include "tma.cuh"
 
 struct ndf_plan {
   ndf::Plan p;
@@ -719,7 +720,7 @@ int ndf_batch_run_host(ndf_batch* b, const void* const* h_in, void* const* h_out
     cudaDeviceSynchronize();
     return cuda_fail(e, "batch host run");
   }
-  return NDF_OK;
+  return status_take() ? fail(NDF_ERR_TIMEOUT, "a bounded device wait gave up") : NDF_OK;
 }
 
 }  // extern "C"

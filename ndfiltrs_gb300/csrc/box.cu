@@ -19,7 +19,8 @@ constexpr int kBoxPairs = 2;  // pairs per thread: tile height 16 * kBoxPairs
 
 template <typename T, int KH, int KW, int MODE>
 __global__ void __launch_bounds__(kThreads)
-    tile_box_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a) {
+    tile_box_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
+                    const __grid_constant__ CUtensorMap tmap) {
   using K = typename KeyOf<T>::K;
   constexpr K kSent = KeyOf<T>::kSentinel;
   constexpr int SW = kBoxTW + KW - 1;
@@ -33,11 +34,11 @@ __global__ void __launch_bounds__(kThreads)
   K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
   long long z, y0, x0;
   tile_coords(a, blockIdx.x, z, y0, x0);
-  build_maps(maps, g, t, z, y0, x0);
-  __syncthreads();
   const bool drop_inf = a.r.drop_inf;
   const K outside = sample_key<T>((T)a.r.cval, drop_inf);
-  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  if (!stage_tile(s, maps, smem_raw, in, a, &tmap, z, y0, x0, outside,
+                  [&](T v) { return sample_key<T>(v, drop_inf); }))
+    return;
   __syncthreads();
 
   const int tx = threadIdx.x % kBoxTW;
@@ -94,7 +95,11 @@ cudaError_t launch_box(const Plan& p, const T* in, T* out, cudaStream_t s) {
   cudaError_t e =
       allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
-  kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile);
+  TileArgs args = p.tile;
+  CUtensorMap map{};
+  size_t smem = p.smem_bytes;
+  tma_prepare(p, p.tile.t, in, &map, &args, &smem);
+  kernel<<<(unsigned)p.tile.t.tiles, kThreads, smem, s>>>(in, out, args, map);
   return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@
 #include "../../include/ndfiltrs_gb300.h"
 #include "common.cuh"
 #include "plan.h"
+#include "tma.cuh"
 
 struct ndf_plan {
   ndf::Plan p;
@@ -554,6 +555,11 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
 
 size_t element_bytes(const Plan& p) { return p.dtype == NDF_FLOAT32 ? 4 : 8; }
 
+// After a synchronization: a device wait that timed out fails the call.
+int check_status() {
+  return status_take() ? fail(NDF_ERR_TIMEOUT, "a bounded device wait gave up") : NDF_OK;
+}
+
 int ensure_buffers(Plan& p) {
   size_t bytes = (size_t)p.n_out * element_bytes(p);
   if (bytes == 0 || (p.d_in && p.buffer_bytes >= bytes)) return NDF_OK;
@@ -734,7 +740,7 @@ int ndf_plan_compute_download(ndf_plan* plan, void* h_out) {
   if (rc != NDF_OK) return rc;
   cudaError_t e = cudaMemcpy(h_out, p.d_out, (size_t)p.n_out * element_bytes(p), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(output)");
-  return NDF_OK;
+  return check_status();
 }
 
 int ndf_plan_run_host(ndf_plan* plan, const void* h_in, void* h_out, void* stream) {
@@ -753,7 +759,7 @@ int ndf_plan_run_host(ndf_plan* plan, const void* h_in, void* h_out, void* strea
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(output)");
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-  return NDF_OK;
+  return check_status();
 }
 
 int ndf_window_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim,

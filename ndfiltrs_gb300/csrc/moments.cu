@@ -24,9 +24,10 @@ constexpr int kThreads = 256;
 template <typename T, int PREC>
 __global__ void __launch_bounds__(kThreads)
     tile_moments_kernel(const T* __restrict__ in, T* __restrict__ out,
-                        const __grid_constant__ TileArgs a, const int32_t* __restrict__ taps) {
+                        const __grid_constant__ TileArgs a, const int32_t* __restrict__ taps,
+                        const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  tile_moments_body<T, PREC>(in, out, a, blockIdx.x, smem_raw, taps);
+  tile_moments_body<T, PREC>(in, out, a, blockIdx.x, smem_raw, taps, &tmap);
 }
 
 // Generic N-D gather (rank > 3 or supports beyond shared memory): the FP64
@@ -70,7 +71,11 @@ cudaError_t launch_tile_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   cudaError_t e =
       allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
-  kernel<<<(unsigned)p.tile.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, p.tile, p.d_tile_taps);
+  TileArgs args = p.tile;
+  CUtensorMap map{};
+  size_t smem = p.smem_bytes;
+  tma_prepare(p, p.tile.t, in, &map, &args, &smem);
+  kernel<<<(unsigned)p.tile.t.tiles, kThreads, smem, s>>>(in, out, args, p.d_tile_taps, map);
   return cudaGetLastError();
 }
 

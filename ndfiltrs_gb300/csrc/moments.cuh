@@ -342,7 +342,8 @@ __device__ __forceinline__ Triple split3(double x) {
 template <typename T, int PREC>
 __device__ __forceinline__ void tile_moments_body(const T* __restrict__ in, T* __restrict__ out,
                                                   const TileArgs& a, long long tile,
-                                                  unsigned char* smem_raw, const int32_t* taps) {
+                                                  unsigned char* smem_raw, const int32_t* taps,
+                                                  const CUtensorMap* tmap = nullptr) {
   const Geom3& g = a.g;
   const Tile& t = a.t;
   long long* maps = reinterpret_cast<long long*>(smem_raw);
@@ -350,9 +351,7 @@ __device__ __forceinline__ void tile_moments_body(const T* __restrict__ in, T* _
   const int support = g.kd * t.SH * t.SW;
   long long z, y0, x0;
   net::tile_coords(a, tile, z, y0, x0);
-  build_maps(maps, g, t, z, y0, x0);
-  __syncthreads();
-  stage_support(s, maps, in, g, t, (T)a.r.cval, [](T v) { return v; });
+  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, (T)a.r.cval, [](T v) { return v; })) return;
   Triple* s3 = reinterpret_cast<Triple*>(s + support);
   if constexpr (PREC == 0 && sizeof(T) == 8) {
     __syncthreads();

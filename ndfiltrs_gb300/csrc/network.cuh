@@ -178,7 +178,8 @@ __device__ __forceinline__ void tile_coords(const TileArgs& a, long long tile, l
 template <typename T, int N, int VFIX, int MODE, typename Tap>
 __device__ __forceinline__ void tile_network_body(const T* __restrict__ in, T* __restrict__ out,
                                                   const TileArgs& a, long long tile,
-                                                  unsigned char* smem_raw, Tap tap) {
+                                                  unsigned char* smem_raw, Tap tap,
+                                                  const CUtensorMap* tmap = nullptr) {
   using K = typename KeyOf<T>::K;
   const Geom3& g = a.g;
   const Tile& t = a.t;
@@ -186,11 +187,11 @@ __device__ __forceinline__ void tile_network_body(const T* __restrict__ in, T* _
   K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
   long long z, y0, x0;
   tile_coords(a, tile, z, y0, x0);
-  build_maps(maps, g, t, z, y0, x0);
-  __syncthreads();
   const bool drop_inf = a.r.drop_inf;
   const K outside = sample_key<T>((T)a.r.cval, drop_inf);
-  stage_support(s, maps, in, g, t, outside, [&](T v) { return sample_key<T>(v, drop_inf); });
+  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, outside,
+                  [&](T v) { return sample_key<T>(v, drop_inf); }))
+    return;
   __syncthreads();
 
   const int tx = threadIdx.x % t.TW;

@@ -62,6 +62,14 @@ struct TileArgs {
   Geom3 g;
   Tile t;
   Reduce r;
+  // TMA staging of interior tiles, set per launch (0 in plans and batch
+  // tasks): box width in elements (a multiple of 16 bytes; 0 = off), tensor
+  // rank (2 or 3), byte offset of the staging area in dynamic shared memory,
+  // and the host-mapped status word a timed-out wait writes.
+  int tma_bw;
+  int tma_rank;
+  int tma_offset;
+  unsigned int* status;
 };
 
 // Generic N-D gather (any rank): one thread per output.

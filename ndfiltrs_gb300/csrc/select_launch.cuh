@@ -12,10 +12,11 @@ using namespace net;
 template <typename T, int N, int VFIX, int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     tile_network_kernel(const T* __restrict__ in, T* __restrict__ out,
-                        const __grid_constant__ TileArgs a, const __grid_constant__ TapTable<N> taps) {
+                        const __grid_constant__ TileArgs a, const __grid_constant__ TapTable<N> taps,
+                        const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   tile_network_body<T, N, VFIX, MODE>(in, out, a, blockIdx.x, smem_raw,
-                                      [&](int i) { return taps.off[i]; });
+                                      [&](int i) { return taps.off[i]; }, &tmap);
 }
 
 template <typename T, int N, int VFIX, int MODE>
@@ -34,7 +35,11 @@ cudaError_t launch_network(const Plan& p, const T* in, T* out, cudaStream_t s) {
   cudaError_t e =
       allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
-  kernel<<<(unsigned)a.t.tiles, kThreads, p.smem_bytes, s>>>(in, out, a, taps);
+  TileArgs args = a;
+  CUtensorMap map{};
+  size_t smem = p.smem_bytes;
+  tma_prepare(p, a.t, in, &map, &args, &smem);
+  kernel<<<(unsigned)a.t.tiles, kThreads, smem, s>>>(in, out, args, taps, map);
   return cudaGetLastError();
 }
 

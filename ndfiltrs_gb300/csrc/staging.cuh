@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "plan.h"
+#include "tma.cuh"
 
 namespace ndf {
 
@@ -63,6 +64,60 @@ __device__ __forceinline__ void stage_support(S* smem, const long long* maps,
       dst[sx] = ox < 0 ? outside : conv(__ldg(src + ox));
     }
   }
+}
+
+// Stage a tile's support: one TMA copy for an interior tile when the launch
+// enabled TMA (a.tma_bw > 0), else the boundary-remapped loads above. Uses
+// `maps` (the remap tables) only on the remapped path. Returns false, in
+// every thread, when the TMA wait timed out; the caller then returns without
+// writing outputs. The caller synchronizes the block after a true return.
+template <typename T, typename S, typename Conv>
+__device__ __forceinline__ bool stage_tile(S* s, long long* maps, unsigned char* smem_raw,
+                                           const T* __restrict__ in, const TileArgs& a,
+                                           const CUtensorMap* tmap, long long z, long long y0,
+                                           long long x0, S outside, Conv conv) {
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  constexpr int kAlign = 16 / (int)sizeof(T);
+  const long long xs = x0 - g.ax, ys = y0 - g.ay, zs = z - g.az;
+  const long long xa = xs >= 0 ? xs - xs % kAlign : -1;
+  const bool interior = a.tma_bw > 0 && xa >= 0 && ys >= 0 && zs >= 0 && xa + a.tma_bw <= g.W &&
+                        ys + t.SH <= g.H && zs + g.kd <= g.D;
+  if (!interior) {
+    build_maps(maps, g, t, z, y0, x0);
+    __syncthreads();
+    stage_support(s, maps, in, g, t, outside, conv);
+    return true;
+  }
+  __shared__ __align__(8) unsigned long long bar;
+  // The staging area starts at the first 128-byte aligned shared address at
+  // or after tma_offset (the launch reserves 127 bytes of slack for it).
+  const unsigned int base = tma::smem_addr(smem_raw + a.tma_offset);
+  T* raw = reinterpret_cast<T*>(smem_raw + a.tma_offset + ((128u - (base & 127u)) & 127u));
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&bar, 1);
+    tma::fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int bytes = (unsigned int)((size_t)a.tma_bw * t.SH * g.kd * sizeof(T));
+    tma::mbar_arrive_expect_tx(&bar, bytes);
+    if (a.tma_rank == 2)
+      tma::load_2d(raw, tmap, &bar, (int)xa, (int)ys);
+    else
+      tma::load_3d(raw, tmap, &bar, (int)xa, (int)ys, (int)zs);
+  }
+  const bool ok = __syncthreads_and(tma::mbar_wait(&bar, 0, kWaitLimitNs, a.status) ? 1 : 0) != 0;
+  if (!ok) return false;
+  const int r = (int)(xs - xa);
+  const int rows = g.kd * t.SH;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  for (int row = warp; row < rows; row += warps) {
+    const T* src = raw + (size_t)row * a.tma_bw + r;
+    S* dst = s + (size_t)row * t.SW;
+    for (int sx = lane; sx < t.SW; sx += 32) dst[sx] = conv(src[sx]);
+  }
+  return true;
 }
 
 }  // namespace ndf

@@ -138,3 +138,57 @@ def test_autotuner_changes_speed_not_results(gpu, oracle) -> None:
         assert nf.autotune_entries() == measured
     finally:
         nf.set_autotune(0, "")
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_tma_staging_matches_remapped_staging(gpu, oracle, dtype) -> None:
+    """Interior tiles staged by one TMA copy give the same bits as the
+    boundary-remapped loads, for the box, network and moments kernels, 2-D and
+    3-D, every mode at the edges, shifted origins, and widths whose rows are
+    not 16-byte aligned (TMA off for those)."""
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(17)
+    cases = [
+        ((300, 260), "median", (5, 5), None),
+        ((300, 262), "median", (5, 5), None),  # rows not 16-byte aligned for float32
+        ((300, 260), "percentile", (7, 7), None),
+        ((300, 260), "median", None, np.add.outer(np.arange(-4, 5) ** 2, np.arange(-4, 5) ** 2) <= 16),
+        ((300, 260), "std", (9, 11), None),
+        ((12, 70, 68), "median", (3, 5, 5), None),
+        ((12, 70, 68), "mean", (3, 3, 5), None),
+    ]
+    try:
+        for shape, kind, size, fp in cases:
+            image = rng.normal(1000, 10, size=shape).astype(dtype)
+            image[rng.random(shape) < 0.02] = np.nan
+            window = fp.shape if fp is not None else size
+            for mode in ("reflect", "constant", "wrap"):
+                origin = tuple([1] + [-1] * (len(shape) - 1))
+                kw = dict(footprint=fp, origin=origin, mode=[mode] * len(shape), cval=2.5, omit_nan=True,
+                          percentile=84.0, parameter=1 if kind == "std" else 0, moments="fp64")
+                results = []
+                for enabled in (True, False):
+                    _core.set_tma(enabled)
+                    with _core.Plan(shape, dtype, kind, window, **kw) as plan:
+                        results.append(plan.run_host(image))
+                ubits = np.uint32 if dtype == np.float32 else np.uint64
+                np.testing.assert_array_equal(results[0].view(ubits), results[1].view(ubits),
+                                              err_msg=str((shape, kind, mode)))
+                if kind not in ("std", "mean"):
+                    ref = oracle.window_filter(image, kind, window, footprint=fp, origin=origin, mode=mode,
+                                               cval=2.5, omit_nan=True, q=84.0)
+                    np.testing.assert_array_equal(results[0].view(ubits), ref.view(ubits))
+    finally:
+        _core.set_tma(True)
+
+
+def test_bounded_wait_reports_timeout(gpu) -> None:
+    """A device wait that can never complete gives up after its limit and is
+    reported as NDF_ERR_TIMEOUT (7); the device stays usable."""
+    import ndfiltrs_gb300 as nf
+    from ndfiltrs_gb300 import _core
+
+    assert _core.selftest_wait_timeout() == 7
+    image = np.arange(64.0, dtype=np.float32).reshape(8, 8)
+    np.testing.assert_array_equal(nf.median_filter(image, size=1), image)
