@@ -169,6 +169,16 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "nanmedian_sortnet_5x5_4096_f32"
 
+# DRAM bytes (read + write) per launch of the workload's kernel, from one ncu
+# capture each (profiles/<kernel>_<workload>.md). Writes that are still in L2
+# when the kernel ends are not counted there.
+MEASURED_TRAFFIC = {
+    "nanmedian_sortnet_5x5_4096_f32": (67.154688e6 + 30.220032e6, "profiles/tile_box_kernel_nanmedian_sortnet_5x5_4096_f32.md"),
+    "nanmedian_hist_65x65_4096_f32": (172.860160e6 + 1.108634e9, "profiles/histogram_kernel_nanmedian_hist_65x65_4096_f32.md"),
+    "nanmedian_ring_4_6_4096_f32": (67.187968e6 + 32.040704e6, "profiles/tile_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
+    "nanstd_31x31_4096_f32": (69.093376e6 + 34.978048e6, "profiles/tile_moments_kernel_nanstd_31x31_4096_f32.md"),
+}
+
 
 def oracle_kind(kind: str) -> str:
     return kind
@@ -706,9 +716,11 @@ def main() -> None:
                 "peak": peak,
                 "unit": "GB/s",
                 "frac": round(achieved / peak, 5),
-                "traffic": None,
+                "traffic": MEASURED_TRAFFIC.get(args.workload, (None,))[0],
+                "traffic_source": MEASURED_TRAFFIC.get(args.workload, (None, None))[1],
                 "peak_source": peak_kind,
-                "note": "selection is instruction-bound; algorithmic bytes = 8 B/pixel",
+                "note": f"selection is instruction-bound; algorithmic bytes = 2 x {image.itemsize} B/pixel "
+                        "(one read, one write), halo re-reads excluded",
             },
             "cpu_baseline": base,
             "clocks": clocks.summary(),
