@@ -84,9 +84,12 @@ cudaError_t launch_tile_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
 size_t tile_moments_smem(const Plan& p, const Tile& t) {
   size_t elem = p.dtype == 0 ? 4 : 8;
   size_t support = (size_t)p.tile.g.kd * t.SH * t.SW;
-  size_t bytes = (size_t)(t.SW + t.SH + p.tile.g.kd) * 8 + support * elem;
-  if (p.dtype == 1 && p.r.moments == 0) bytes += support * sizeof(Triple);
-  return bytes;
+  // Remap tables | staged values (| triple-float copies) | tap offsets, laid
+  // out as tile_moments_body does.
+  size_t staged = support * elem;
+  if (p.dtype == 1 && p.r.moments == 0) staged += support * sizeof(Triple);
+  return (size_t)(t.SW + t.SH + p.tile.g.kd) * 8 + (staged + 15) / 16 * 16 +
+         (size_t)p.r.count * sizeof(int32_t);
 }
 
 cudaError_t launch_tile_moments(const Plan& p, const void* in, void* out, cudaStream_t s) {

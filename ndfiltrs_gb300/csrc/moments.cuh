@@ -198,32 +198,54 @@ __device__ __forceinline__ int decide_special(const Reduce& r, long long n, bool
   return 0;
 }
 
-// float32 input: samples staged as float.
-template <typename FetchF>
-__device__ __forceinline__ bool moments_fp32c_f32(FetchF&& fetch, const Reduce& r, double* out) {
+// Kahan sum in FP32: s - c is the running total.
+struct Kahan32 {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// float32 input: samples staged as float. `visit(f)` calls f(v) for every
+// tap of the window; `first(i)` returns tap i (for the pivot search).
+//
+// Every retained sample is shifted by the pivot p (the window's first finite
+// retained sample) exactly, as a two-sum (dh + dl = v - p); the sums of dh
+// and of dh^2 run as Kahan sums, and the rounding parts (dl, and the
+// two-product error of dh^2 plus 2 dh dl) are summed plainly: their total
+// is below an ulp of the result's scale.
+template <typename Visit, typename First>
+__device__ __forceinline__ bool moments_fp32c_f32(Visit&& visit, First&& first, const Reduce& r,
+                                                  double* out) {
   const int V = r.count;
-  long long n = 0;
-  bool nan = false, pinf = false, ninf = false;
-  float p = 0.0f, maxdev = 0.0f;
-  bool have_p = false;
-  Sum32 s1, s2;
-  float c1 = 0.0f, c2 = 0.0f;
+  const float kInf = __uint_as_float(0x7f800000u);
+  float p = 0.0f;
   for (int i = 0; i < V; ++i) {
-    float v = fetch(i);
-    if (isnan(v)) {
-      nan = nan || !r.omit;
-      continue;
-    }
-    if (isinf(v)) {
-      if (r.drop_inf) continue;
-      n += 1;
-      pinf = pinf || v > 0;
-      ninf = ninf || v < 0;
-      continue;
-    }
-    if (!have_p) {
+    const float v = first(i);
+    if (fabsf(v) < kInf) {
       p = v;
-      have_p = true;
+      break;
+    }
+  }
+  int n = 0;
+  bool nan = false, pinf = false, ninf = false;
+  float maxdev = 0.0f, c1 = 0.0f, c2 = 0.0f;
+  Kahan32 s1, s2;
+  const bool omit = r.omit, drop_inf = r.drop_inf;
+  visit([&](float v) {
+    if (!(fabsf(v) < kInf)) {
+      if (isnan(v)) {
+        nan = nan || !omit;
+      } else if (!drop_inf) {
+        n += 1;
+        pinf = pinf || v > 0.0f;
+        ninf = ninf || v < 0.0f;
+      }
+      return;
     }
     n += 1;
     float dh, dl;
@@ -231,16 +253,17 @@ __device__ __forceinline__ bool moments_fp32c_f32(FetchF&& fetch, const Reduce& 
     maxdev = fmaxf(maxdev, fabsf(dh));
     s1.add(dh);
     c1 = __fadd_rn(c1, dl);
-    float sq = __fmul_rn(dh, dh);
+    const float sq = __fmul_rn(dh, dh);
     float sqe = fmaf(dh, dh, -sq);
     sqe = fmaf(__fmul_rn(2.0f, dh), dl, sqe);
     s2.add(sq);
     c2 = __fadd_rn(c2, sqe);
-  }
+  });
+  (void)V;
   if (decide_special(r, n, nan, pinf, ninf, out)) return true;
   if (maxdev != 0.0f && (maxdev < kSafeLow || maxdev > kSafeHigh || !isfinite(maxdev))) return false;
-  double S1 = ((double)s1.s + (double)s1.c) + (double)c1;
-  double S2 = ((double)s2.s + (double)s2.c) + (double)c2;
+  const double S1 = s1.value() + (double)c1;
+  const double S2 = s2.value() + (double)c2;
   return combine(r, n, (double)p, S1, S2, out);
 }
 
@@ -353,6 +376,12 @@ __device__ __forceinline__ void tile_moments_body(const T* __restrict__ in, T* _
   net::tile_coords(a, tile, z, y0, x0);
   if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, (T)a.r.cval, [](T v) { return v; })) return;
   Triple* s3 = reinterpret_cast<Triple*>(s + support);
+  // Tap offsets in shared memory (broadcast reads), after the staged values.
+  const size_t staged = (size_t)support * sizeof(T) + (PREC == 0 && sizeof(T) == 8 ? (size_t)support * sizeof(Triple) : 0);
+  int32_t* taps_s = reinterpret_cast<int32_t*>(
+      reinterpret_cast<unsigned char*>(s) + ((staged + 15) & ~(size_t)15));
+  for (int i = threadIdx.x; i < a.r.count; i += blockDim.x) taps_s[i] = taps[i];
+  taps = taps_s;
   if constexpr (PREC == 0 && sizeof(T) == 8) {
     __syncthreads();
     for (int i = threadIdx.x; i < support; i += blockDim.x) s3[i] = split3((double)s[i]);
@@ -369,7 +398,25 @@ __device__ __forceinline__ void tile_moments_body(const T* __restrict__ in, T* _
   if constexpr (PREC == 0) {
     if constexpr (sizeof(T) == 4) {
       auto fetch32 = [&](int i) -> float { return (float)s[base + taps[i]]; };
-      done = moments_fp32c_f32(fetch32, a.r, &result);
+      if (g.kd * g.kh * g.kw == a.r.count) {
+        // A full box: taps in row-major order without the offset table.
+        const int plane = t.SH * t.SW;
+        auto visit = [&](auto&& f) {
+          for (int kz = 0; kz < g.kd; ++kz)
+            for (int ky = 0; ky < g.kh; ++ky) {
+              const T* row = s + base + kz * plane + ky * t.SW;
+#pragma unroll 4
+              for (int kx = 0; kx < g.kw; ++kx) f((float)row[kx]);
+            }
+        };
+        done = moments_fp32c_f32(visit, fetch32, a.r, &result);
+      } else {
+        auto visit = [&](auto&& f) {
+#pragma unroll 4
+          for (int i = 0; i < a.r.count; ++i) f((float)s[base + taps[i]]);
+        };
+        done = moments_fp32c_f32(visit, fetch32, a.r, &result);
+      }
     } else {
       auto fetch3 = [&](int i) -> Triple { return s3[base + taps[i]]; };
       done = moments_fp32c_f64(fetch3, a.r, &result);
