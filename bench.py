@@ -166,6 +166,12 @@ WORKLOADS = {
                                      min_count=5, parameter=1),
     "nanstd_31x31_4096_f64": Workload(lambda: precision_image(4096, dtype=np.float64), "std", (31, 31), "reflect",
                                       ignore_inf=True, min_count=5, parameter=1),
+    # Exact rolling means (method="boxcar"), correctly rounded.
+    "nanmean_boxcar_31x31_4096_f32": Workload(lambda: precision_image(4096), "mean_rolling", (31, 31), "reflect",
+                                              ignore_inf=True, min_count=5),
+    "nanmean_boxcar_129x129_8192_f32": Workload(lambda: sky_image(8192), "mean_rolling", (129, 129), "nearest"),
+    "nanmean_boxcar_31x31_4096_f64": Workload(lambda: precision_image(4096, dtype=np.float64), "mean_rolling",
+                                              (31, 31), "reflect", ignore_inf=True, min_count=5),
 }
 DEFAULT_WORKLOAD = "nanmedian_sortnet_5x5_4096_f32"
 
@@ -642,7 +648,7 @@ def main() -> None:
         expected = oracle_filter(oracle, spec, sample)
         ubits = np.uint32 if image.dtype == np.float32 else np.uint64
         check = bool(np.array_equal(gpu_sample.view(ubits), expected.view(ubits))) \
-            if kind not in ("mean", "var", "std") else None
+            if kind not in ("mean", "var", "std") else None  # FP32C moments: tolerance, not bits
 
     # End to end through the C-ABI host entry point with pinned buffers.
     host_in = torch.from_numpy(image).pin_memory()

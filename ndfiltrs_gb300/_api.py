@@ -12,8 +12,10 @@ tile), and "histogram" runs the sliding rank-histogram kernel for
 rectangular 1-D/2-D windows; windows too wide for a register network use the
 histogram kernel (rectangular) or a radix select (footprints).
 
-Out of scope on this path: ``mean_filter(method="separable" | "boxcar")``
-(separable and exact rolling means) raise NotImplementedError.
+``mean_filter`` / ``nanmean_filter(method="boxcar")`` run the exact rolling
+mean (kind "mean_rolling"): the window's finite samples summed exactly and the
+mean rounded once. ``method="separable"`` (the reference's separable
+float64 mean) is outside this path and raises NotImplementedError.
 """
 
 from __future__ import annotations
@@ -56,14 +58,15 @@ def _median_kind(method: object, args: Arguments) -> str:
     ]
 
 
-def _mean_method(method: object, args: Arguments) -> None:
+def _mean_kind(method: object, args: Arguments) -> str:
     check_method(method, ("direct", "separable", "boxcar"))
     if method == "boxcar" and args.footprint is not None:
         raise ValueError("method='boxcar' requires size, not footprint")
-    if method != "direct":
+    if method == "separable":
         raise NotImplementedError(
-            f"mean method {method!r} is outside this library's scope; use method='direct'"
+            "mean method 'separable' is outside this library's scope; use 'direct' or 'boxcar'"
         )
+    return "mean_rolling" if method == "boxcar" else "mean"
 
 
 def median_filter(
@@ -118,8 +121,7 @@ def mean_filter(
 ) -> FloatArray:
     """Arithmetic mean of each window; NaNs propagate locally."""
     args = validate(array, size, mode, cval, footprint=footprint, origin=origin, min_count=1)
-    _mean_method(method, args)
-    return _run("mean", args)
+    return _run(_mean_kind(method, args), args)
 
 
 def nanmean_filter(
@@ -137,8 +139,7 @@ def nanmean_filter(
     """Mean of each window omitting NaNs (and infinities with ``ignore_inf``)."""
     check_flag(ignore_inf, "ignore_inf")
     args = validate(array, size, mode, cval, footprint=footprint, origin=origin, min_count=min_count)
-    _mean_method(method, args)
-    return _run("mean", args, ignore_inf=bool(ignore_inf))
+    return _run(_mean_kind(method, args), args, ignore_inf=bool(ignore_inf))
 
 
 def min_filter(

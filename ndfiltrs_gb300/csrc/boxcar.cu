@@ -1,0 +1,551 @@
+// Exact rectangular means: kind mean_rolling (method="boxcar").
+//
+// Replaces mean_into and ExactSum (src/boxcar.rs:142-399,
+// src/exact_sum.rs:215-349). A window's result is the exact sum of its finite
+// samples divided by their count, rounded once to the output type (nearest,
+// ties to even); the counts of NaN (propagate policy) and of each signed
+// infinity decide NaN / +-inf first (Counts::value, src/boxcar.rs:59-77).
+//
+// GB300 design:
+//  * one thread block per output tile (32 x TH outputs; 256 x 1 for
+//    single-row arrays); the block stages its support (one TMA copy for an
+//    interior tile) and finds the bit span of the support's finite nonzero
+//    samples;
+//  * every sample becomes a W-word two's-complement fixed-point integer in
+//    units of 2^(E0 + 64 * low_word), E0 being the type's smallest subnormal
+//    exponent and low_word the tile's lowest occupied 64-bit word, so sums
+//    and differences are exact;
+//  * the horizontal window sum of every support row slides along the row
+//    (add the entering sample, subtract the leaving one), then each thread
+//    slides its column's vertical sum of those row sums down its rows: the
+//    work per output does not grow with the window;
+//  * the quotient by the count is rounded with one integer division;
+//  * a tile whose span needs more than W words is appended to a list that a
+//    second kernel finishes with full-width direct sums (5 words for float32,
+//    34 for float64, every finite value times any count); that kernel also
+//    serves arrays of rank 3 or more and windows whose counts exceed 16 bits.
+#include <algorithm>
+#include <climits>
+
+#include "network.cuh"
+#include "plan.h"
+#include "staging.cuh"
+#include "tma.cuh"
+
+namespace ndf {
+namespace {
+
+constexpr int kBThreads = 256;
+
+template <typename T>
+struct Bits;
+template <>
+struct Bits<float> {
+  using U = unsigned int;
+  static constexpr int kP = 24, kF = 23, kExpMask = 0xFF, kFull = 5, kWords = 2;
+};
+template <>
+struct Bits<double> {
+  using U = unsigned long long;
+  static constexpr int kP = 53, kF = 52, kExpMask = 0x7FF, kFull = 34, kWords = 3;
+};
+
+template <typename T>
+__device__ __forceinline__ typename Bits<T>::U bits_of(T v) {
+  if constexpr (sizeof(T) == 4) return __float_as_uint(v);
+  else return (unsigned long long)__double_as_longlong(v);
+}
+
+template <typename T>
+__device__ __forceinline__ T from_bits(typename Bits<T>::U b) {
+  if constexpr (sizeof(T) == 4) return __uint_as_float(b);
+  else return __longlong_as_double((long long)b);
+}
+
+// Window counts, 16 bits each: finite | NaN (propagate policy) << 16 |
+// +inf << 32 | -inf << 48 (Counts::sample, src/boxcar.rs:19-36).
+template <typename T>
+__device__ __forceinline__ unsigned long long sample_counts(T v, bool omit, bool drop_inf) {
+  if (isnan(v)) return omit ? 0ull : (1ull << 16);
+  if (isinf(v)) return drop_inf ? 0ull : (v > (T)0 ? (1ull << 32) : (1ull << 48));
+  return 1ull;
+}
+
+// A finite nonzero sample as m * 2^pos (units of the type's smallest
+// subnormal) with m odd. Returns false for zero, NaN and infinities.
+template <typename T>
+__device__ __forceinline__ bool decompose(T v, unsigned long long& m, int& pos, bool& neg) {
+  using B = Bits<T>;
+  const typename B::U b = bits_of(v);
+  const int e = (int)((b >> B::kF) & B::kExpMask);
+  if (e == B::kExpMask) return false;
+  const unsigned long long frac = (unsigned long long)b & ((1ull << B::kF) - 1);
+  m = e ? (frac | (1ull << B::kF)) : frac;
+  if (m == 0) return false;
+  const int tz = __ffsll((long long)m) - 1;
+  m >>= tz;
+  pos = (e ? e - 1 : 0) + tz;
+  neg = (b >> (sizeof(T) * 8 - 1)) != 0;
+  return true;
+}
+
+template <int W>
+struct Wide {
+  unsigned long long w[W];
+};
+
+template <int W>
+__device__ __forceinline__ void wide_add(Wide<W>& a, const Wide<W>& b) {
+  unsigned long long carry = 0;
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    const unsigned long long s = a.w[i] + b.w[i];
+    const unsigned long long t = s + carry;
+    carry = (s < a.w[i]) | (t < s);
+    a.w[i] = t;
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void wide_sub(Wide<W>& a, const Wide<W>& b) {
+  unsigned long long borrow = 0;
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    const unsigned long long d = a.w[i] - b.w[i];
+    const unsigned long long t = d - borrow;
+    borrow = (a.w[i] < b.w[i]) | (d < borrow);
+    a.w[i] = t;
+  }
+}
+
+// The sample as a W-word two's-complement integer in units of
+// 2^(E0 + 64 * low_word); zero for zero and non-finite samples. The tile's
+// span guarantees pos >= 64 * low_word and that the value fits.
+template <typename T, int W>
+__device__ __forceinline__ Wide<W> encode(T v, int low_word) {
+  Wide<W> r;
+  unsigned long long m;
+  int pos;
+  bool neg;
+  const bool finite = decompose(v, m, pos, neg);
+  const int local = finite ? pos - 64 * low_word : 0;
+  const int wi = local >> 6, off = local & 63;
+  const unsigned long long lo = finite ? m << off : 0ull;
+  const unsigned long long hi = (finite && off) ? m >> (64 - off) : 0ull;
+#pragma unroll
+  for (int i = 0; i < W; ++i) r.w[i] = i == wi ? lo : (i == wi + 1 ? hi : 0ull);
+  if (finite && neg) {
+    unsigned long long carry = 1;
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      r.w[i] = ~r.w[i] + carry;
+      carry = (carry && r.w[i] == 0) ? 1ull : 0ull;
+    }
+  }
+  return r;
+}
+
+__device__ __forceinline__ int bitlen64(unsigned long long x) { return x ? 64 - __clzll((long long)x) : 0; }
+
+// RN_T(S / n) for the NW-word two's-complement sum S in units of
+// 2^(E0 + 64 * low_word) and a count n >= 1, rounded once: with B the bit
+// length of |S| and t that of n, q = floor(|S| / (n 2^s)) for
+// s = max(B - t - p - 1, 0) has p + 1 or p + 2 bits (p, the precision), so
+// its low bits and the remainder decide the rounding exactly; s = 0 is the
+// subnormal grid, where no sample has bits below.
+template <typename T, int NW>
+__device__ __forceinline__ T exact_mean(const unsigned long long (&sum)[NW], int low_word, unsigned int n) {
+  using B = Bits<T>;
+  constexpr int p = B::kP;
+  const bool negative = (sum[NW - 1] >> 63) != 0;
+  unsigned long long m[NW];
+  unsigned long long carry = 1;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    m[i] = negative ? ~sum[i] + carry : sum[i];
+    carry = (negative && carry && m[i] == 0) ? 1ull : 0ull;
+  }
+  int blocal = 0;
+#pragma unroll
+  for (int i = 0; i < NW; ++i)
+    if (m[i]) blocal = 64 * i + bitlen64(m[i]);
+  const typename B::U sign = negative ? (typename B::U)1 << (sizeof(T) * 8 - 1) : 0;
+  if (blocal == 0) return from_bits<T>(0);  // exact cancellation gives +0
+  const int bits = blocal + 64 * low_word;
+  const int t = 32 - __clz((int)n);
+  const int s = max(bits - t - p - 1, 0);
+  const int sl = s - 64 * low_word;  // shift of the local words
+  unsigned __int128 high = 0;
+  bool sticky = false;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) {
+    const int sh = 64 * i - sl;  // position of word i in `high`
+    if (sh >= 128 || sh <= -64) {
+      if (sh <= -64) sticky = sticky || m[i] != 0;
+      continue;
+    }
+    if (sh >= 0) {
+      high |= (unsigned __int128)m[i] << sh;
+    } else {
+      high |= (unsigned __int128)(m[i] >> (-sh));
+      sticky = sticky || (m[i] & ((1ull << (-sh)) - 1)) != 0;
+    }
+  }
+  unsigned __int128 q, r;
+  if constexpr (sizeof(T) == 4) {
+    const unsigned long long h = (unsigned long long)high;  // at most 58 bits
+    q = h / n;
+    r = h % n;
+  } else {
+    q = high / n;
+    r = high % n;
+  }
+  const int qbits = (q >> 64) ? 128 - __clzll((long long)(unsigned long long)(q >> 64))
+                              : bitlen64((unsigned long long)q);
+  const int k = max(qbits - p, 0);
+  unsigned long long mant;
+  bool up;
+  if (k > 0) {
+    mant = (unsigned long long)(q >> k);
+    const bool guard = ((q >> (k - 1)) & 1) != 0;
+    const bool rest = (q & (((unsigned __int128)1 << (k - 1)) - 1)) != 0 || r != 0 || sticky;
+    up = guard && (rest || (mant & 1));
+  } else {
+    mant = (unsigned long long)q;
+    const unsigned __int128 twice = 2 * r;
+    up = twice > n || (twice == n && (sticky || (mant & 1)));
+  }
+  const typename B::U out =
+      (typename B::U)((((unsigned long long)(s + k)) << (p - 1)) + mant + (up ? 1ull : 0ull)) | sign;
+  return from_bits<T>(out);
+}
+
+// Counts::value (src/boxcar.rs:59-77) over packed counts; `mean` is only
+// called for windows that need it.
+template <typename T, typename Mean>
+__device__ __forceinline__ T finish(unsigned long long c, const Reduce& r, Mean&& mean) {
+  const unsigned int finite = (unsigned int)(c & 0xFFFF), nan = (unsigned int)((c >> 16) & 0xFFFF);
+  const unsigned int pos = (unsigned int)((c >> 32) & 0xFFFF), neg = (unsigned int)(c >> 48);
+  const unsigned int kept = finite + pos + neg;
+  if (nan || kept == 0 || (r.omit && (long long)kept < r.min_count) || (pos && neg)) return nan_of(T());
+  if (pos) return from_bits<T>(sizeof(T) == 4 ? (typename Bits<T>::U)0x7f800000u
+                                              : (typename Bits<T>::U)0x7ff0000000000000ull);
+  if (neg) return from_bits<T>(sizeof(T) == 4 ? (typename Bits<T>::U)0xff800000u
+                                              : (typename Bits<T>::U)0xfff0000000000000ull);
+  return mean(finite);
+}
+
+struct BoxcarArgs {
+  int count_bits;          // bit length of (window volume + 1)
+  unsigned int* list;      // tiles left to the full-width kernel
+  unsigned int* list_len;  // their number
+};
+
+template <typename T, int W>
+__global__ void __launch_bounds__(kBThreads)
+    boxcar_tile_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
+                       const __grid_constant__ BoxcarArgs b, const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int red_lo[kBThreads / 32], red_hi[kBThreads / 32];
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  T* s = reinterpret_cast<T*>(maps + (t.SW + t.SH + g.kd));
+  const size_t staged = ((size_t)t.SH * t.SW * sizeof(T) + 15) & ~(size_t)15;
+  unsigned long long* hs = reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(s) + staged);
+  unsigned long long* hc = hs + (size_t)t.SH * W * t.TW;
+  long long z, y0, x0;
+  net::tile_coords(a, blockIdx.x, z, y0, x0);
+  if (!stage_tile(s, maps, smem_raw, in, a, &tmap, z, y0, x0, (T)a.r.cval, [](T v) { return v; })) return;
+  __syncthreads();
+
+  // Bit span of the support's finite nonzero samples.
+  const int support = t.SH * t.SW;
+  int lo = INT_MAX, hi = -1;
+  for (int e = threadIdx.x; e < support; e += blockDim.x) {
+    unsigned long long m;
+    int pos;
+    bool neg;
+    if (decompose(s[e], m, pos, neg)) {
+      lo = min(lo, pos);
+      hi = max(hi, pos + bitlen64(m) - 1);
+    }
+  }
+  for (int o = 16; o >= 1; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red_lo[threadIdx.x >> 5] = lo;
+    red_hi[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  lo = INT_MAX;
+  hi = -1;
+  for (int w = 0; w < kBThreads / 32; ++w) {
+    lo = min(lo, red_lo[w]);
+    hi = max(hi, red_hi[w]);
+  }
+  const int low_word = lo == INT_MAX ? 0 : lo >> 6;
+  const int need = hi < 0 ? 1 : ((hi + 2 + b.count_bits + 63) >> 6) - low_word;
+  if (need > W) {
+    if (threadIdx.x == 0) b.list[atomicAdd(b.list_len, 1u)] = blockIdx.x;
+    return;
+  }
+
+  // Horizontal window sums of every support row, 8 outputs per work item.
+  const bool omit = a.r.omit, drop_inf = a.r.drop_inf;
+  const int kw = g.kw, kh = g.kh, TW = t.TW, SW = t.SW;
+  const int nseg = TW / 8;
+  for (int item = threadIdx.x; item < t.SH * nseg; item += blockDim.x) {
+    const int y = item / nseg;
+    const int xs = (item - y * nseg) * 8;
+    const T* row = s + (size_t)y * SW + xs;
+    Wide<W> sum = {};
+    unsigned long long cnt = 0;
+    for (int k = 0; k < kw; ++k) {
+      wide_add(sum, encode<T, W>(row[k], low_word));
+      cnt += sample_counts(row[k], omit, drop_inf);
+    }
+#pragma unroll 1
+    for (int j = 0; j < 8; ++j) {
+      if (j > 0) {
+        const T enter = row[j + kw - 1], leave = row[j - 1];
+        wide_add(sum, encode<T, W>(enter, low_word));
+        wide_sub(sum, encode<T, W>(leave, low_word));
+        cnt += sample_counts(enter, omit, drop_inf);
+        cnt -= sample_counts(leave, omit, drop_inf);
+      }
+#pragma unroll
+      for (int i = 0; i < W; ++i) hs[((size_t)y * W + i) * TW + xs + j] = sum.w[i];
+      hc[(size_t)y * TW + xs + j] = cnt;
+    }
+  }
+  __syncthreads();
+
+  // Vertical sums down each column, L rows per thread.
+  const int x = threadIdx.x % TW;
+  const int nsegs = kBThreads / TW;
+  const int L = t.TH / nsegs;
+  const int r0 = (threadIdx.x / TW) * L;
+  const long long gx = x0 + x;
+  auto row_sum = [&](int y, Wide<W>& v, unsigned long long& c) {
+#pragma unroll
+    for (int i = 0; i < W; ++i) v.w[i] = hs[((size_t)y * W + i) * TW + x];
+    c = hc[(size_t)y * TW + x];
+  };
+  Wide<W> sum = {};
+  unsigned long long cnt = 0;
+  for (int k = 0; k < kh; ++k) {
+    Wide<W> v;
+    unsigned long long c;
+    row_sum(r0 + k, v, c);
+    wide_add(sum, v);
+    cnt += c;
+  }
+  for (int rr = 0; rr < L; ++rr) {
+    const int r = r0 + rr;
+    const long long gy = y0 + r;
+    if (gy < g.H && gx < g.W) {
+      const T v = finish<T>(cnt, a.r, [&](unsigned int n) { return exact_mean<T, W>(sum.w, low_word, n); });
+      out[(z * g.H + gy) * g.W + gx] = canonical(v);
+    }
+    if (rr + 1 < L) {
+      Wide<W> va, vr;
+      unsigned long long ca, cr;
+      row_sum(r + kh, va, ca);
+      row_sum(r, vr, cr);
+      wide_add(sum, va);
+      wide_sub(sum, vr);
+      cnt += ca - cr;
+    }
+  }
+}
+
+// Full-width direct sums: every output of the listed tiles (list mode) or
+// of the whole array (list == nullptr), gathered through the per-axis
+// boundary maps (Window::visit, src/window.rs:232-294).
+template <typename T>
+__global__ void __launch_bounds__(kBThreads)
+    boxcar_direct_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ GenericArgs a,
+                         const long long* __restrict__ taps, const __grid_constant__ TileArgs tile,
+                         const unsigned int* __restrict__ list, const unsigned int* __restrict__ list_len) {
+  constexpr int NW = Bits<T>::kFull;
+  const int rank = a.rank;
+  const bool omit = a.r.omit, drop_inf = a.r.drop_inf;
+  const T cval = (T)a.r.cval;
+  const long long per_tile = (long long)tile.t.TW * tile.t.TH;
+  const long long total = list ? (long long)(*list_len) * per_tile : a.n_out;
+  for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
+       item += (long long)gridDim.x * blockDim.x) {
+    long long o = item;
+    if (list) {
+      const long long tl = list[item / per_tile];
+      const long long within = item % per_tile;
+      long long z, y0, x0;
+      net::tile_coords(tile, tl, z, y0, x0);
+      const long long y = y0 + within / tile.t.TW, x = x0 + within % tile.t.TW;
+      if (y >= tile.g.H || x >= tile.g.W) continue;
+      o = (z * tile.g.H + y) * tile.g.W + x;
+    }
+    long long coord[kMaxGenericRank];
+    long long rem = o;
+    for (int d = 0; d < rank; ++d) {
+      coord[d] = rem / a.stride[d];
+      rem -= coord[d] * a.stride[d];
+    }
+    unsigned long long acc[NW];
+    for (int i = 0; i < NW; ++i) acc[i] = 0;
+    unsigned long long finite = 0, nan = 0, pos = 0, neg = 0;
+    for (int i = 0; i < a.r.count; ++i) {
+      const long long* tap = taps + (long long)i * rank;
+      long long src = 0;
+      bool inside = true;
+      for (int d = 0; d < rank && inside; ++d) {
+        long long m;
+        inside = map_index(coord[d] + tap[d], a.shape[d], a.mode[d], &m);
+        src += m * a.stride[d];
+      }
+      const T v = inside ? __ldg(in + src) : cval;
+      if (isnan(v)) {
+        if (!omit) ++nan;
+        continue;
+      }
+      if (isinf(v)) {
+        if (!drop_inf) (v > (T)0 ? pos : neg) += 1;
+        continue;
+      }
+      ++finite;
+      unsigned long long mm;
+      int p;
+      bool negative;
+      if (!decompose(v, mm, p, negative)) continue;
+      int wi = p >> 6;
+      const int off = p & 63;
+      const unsigned long long parts[2] = {mm << off, off ? mm >> (64 - off) : 0ull};
+      if (!negative) {
+        unsigned long long carry = 0;
+        for (int j = 0; wi < NW && (j < 2 || carry); ++j, ++wi) {
+          const unsigned long long add = j < 2 ? parts[j] : 0ull;
+          const unsigned long long s1 = acc[wi] + add;
+          const unsigned long long s2 = s1 + carry;
+          carry = (s1 < add) | (s2 < s1);
+          acc[wi] = s2;
+        }
+      } else {
+        unsigned long long borrow = 0;
+        for (int j = 0; wi < NW && (j < 2 || borrow); ++j, ++wi) {
+          const unsigned long long sub = j < 2 ? parts[j] : 0ull;
+          const unsigned long long d1 = acc[wi] - sub;
+          const unsigned long long d2 = d1 - borrow;
+          borrow = (acc[wi] < sub) | (d1 < borrow);
+          acc[wi] = d2;
+        }
+      }
+    }
+    const unsigned long long kept = finite + pos + neg;
+    T result;
+    if (nan || kept == 0 || (omit && (long long)kept < a.r.min_count) || (pos && neg))
+      result = nan_of(T());
+    else if (pos)
+      result = from_bits<T>(sizeof(T) == 4 ? (typename Bits<T>::U)0x7f800000u
+                                           : (typename Bits<T>::U)0x7ff0000000000000ull);
+    else if (neg)
+      result = from_bits<T>(sizeof(T) == 4 ? (typename Bits<T>::U)0xff800000u
+                                           : (typename Bits<T>::U)0xfff0000000000000ull);
+    else
+      result = exact_mean<T, NW>(acc, 0, (unsigned int)finite);
+    out[o] = canonical(result);
+  }
+}
+
+template <typename T>
+size_t tile_smem(const Tile& t, int kd) {
+  constexpr int W = Bits<T>::kWords;
+  const size_t staged = ((size_t)t.SH * t.SW * sizeof(T) + 15) & ~(size_t)15;
+  return (size_t)(t.SW + t.SH + kd) * 8 + staged + (size_t)t.SH * t.TW * (W + 1) * 8;
+}
+
+template <typename T>
+cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  constexpr int W = Bits<T>::kWords;
+  const long long direct_grid = std::max(1, p.sm_count) * 8ll;
+  if (p.algo == Algo::kBoxcarDirect) {
+    boxcar_direct_kernel<T><<<(unsigned)direct_grid, kBThreads, 0, s>>>(in, out, p.generic, p.d_gen_taps, p.tile,
+                                                                       nullptr, nullptr);
+    return cudaGetLastError();
+  }
+  unsigned int* list = reinterpret_cast<unsigned int*>(p.d_scratch);
+  unsigned int* list_len = list + p.tile.t.tiles;
+  cudaError_t e = cudaMemsetAsync(list_len, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  auto kernel = boxcar_tile_kernel<T, W>;
+  e = allow_max_smem((const void*)kernel);
+  if (e != cudaSuccess) return e;
+  BoxcarArgs b;
+  b.count_bits = 64 - __builtin_clzll((unsigned long long)p.r.count + 1);
+  b.list = list;
+  b.list_len = list_len;
+  TileArgs args = p.tile;
+  CUtensorMap map{};
+  size_t smem = p.smem_bytes;
+  tma_prepare(p, p.tile.t, in, &map, &args, &smem);
+  kernel<<<(unsigned)p.tile.t.tiles, kBThreads, smem, s>>>(in, out, args, b, map);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  boxcar_direct_kernel<T><<<(unsigned)direct_grid, kBThreads, 0, s>>>(in, out, p.generic, p.d_gen_taps, p.tile,
+                                                                     list, list_len);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Tile shape and shared memory of the tiled exact-mean kernel: 32 x TH
+// outputs (TH the largest of 64, 32, 16, 8 within 96 KB of shared memory),
+// or 256 x 1 for single-row arrays. Returns false when the direct kernel
+// must run instead (rank 3 or more, window counts beyond 16 bits, or no tile
+// fitting in `smem_limit`).
+bool boxcar_configure(Plan& p, int smem_limit) {
+  const Geom3& g = p.tile.g;
+  if (p.ndim > 2 || g.D != 1) return false;
+  const long long volume = (long long)g.kh * g.kw;
+  if (volume + g.kw + g.kh >= 65535) return false;
+  auto shape = [&](int tw, int th) {
+    Tile t = p.tile.t;
+    t.TW = tw;
+    t.TH = th;
+    t.SW = tw + g.kw - 1;
+    t.SH = th + g.kh - 1;
+    t.tiles_x = (g.W + tw - 1) / tw;
+    t.tiles_y = (g.H + th - 1) / th;
+    t.tiles = t.tiles_x * t.tiles_y * g.D;
+    return t;
+  };
+  auto bytes = [&](const Tile& t) {
+    return p.dtype == 0 ? tile_smem<float>(t, g.kd) : tile_smem<double>(t, g.kd);
+  };
+  if (g.H == 1 && g.kh == 1) {
+    Tile t = shape(256, 1);
+    if (bytes(t) > (size_t)smem_limit) return false;
+    p.tile.t = t;
+    p.smem_bytes = bytes(t);
+    return true;
+  }
+  const size_t budget = std::min<size_t>(96 * 1024, (size_t)smem_limit);
+  for (int th : {64, 32, 16, 8}) {
+    Tile t = shape(32, th);
+    if (bytes(t) <= budget || (th == 8 && bytes(t) <= (size_t)smem_limit)) {
+      p.tile.t = t;
+      p.smem_bytes = bytes(t);
+      return true;
+    }
+  }
+  return false;
+}
+
+cudaError_t launch_boxcar(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  if (p.dtype == 0) return launch_t<float>(p, (const float*)in, (float*)out, s);
+  return launch_t<double>(p, (const double*)in, (double*)out, s);
+}
+
+}  // namespace ndf

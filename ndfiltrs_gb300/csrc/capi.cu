@@ -52,6 +52,10 @@ const char* algo_name(Algo a) {
       return "moments_tile";
     case Algo::kMomentsGeneric:
       return "moments_generic";
+    case Algo::kBoxcarTile:
+      return "boxcar_tile";
+    case Algo::kBoxcarDirect:
+      return "boxcar_direct";
   }
   return "unknown";
 }
@@ -315,6 +319,11 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
       return fail(NDF_ERR_OVERFLOW, "shape or index arithmetic overflowed");
   p.n_out = (long long)n_out;
   if (volume > (1ull << 31)) return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+  const int kind = d->kind;
+  // RollingMean plans reject footprints before anything else about them
+  // (src/plan.rs:280-285).
+  if (kind == kMeanRolling && d->footprint)
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "rolling means require rectangular size, not footprint");
   size_t count = 0;
   if (d->footprint) {
     p.footprint.assign(d->footprint, d->footprint + volume);
@@ -324,11 +333,7 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
   }
   if (count == 0)
     return fail(NDF_ERR_INVALID_CONFIGURATION, "footprint must select at least one element");
-  const int kind = d->kind;
-  if (kind == kMeanRolling)
-    return fail(NDF_ERR_UNSUPPORTED,
-                "kind 'mean_rolling' (method='boxcar') is outside this library's scope");
-  if (!is_selection(kind) && !is_moment(kind))
+  if (!is_selection(kind) && !is_moment(kind) && kind != kMeanRolling)
     return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported window filter kind");
   Reduce& r = p.r;
   r.kind = kind;
@@ -509,6 +514,27 @@ int choose_algorithm(Plan& p, int smem_limit) {
     if (rc != NDF_OK) return rc;
   }
   const bool tileable = p.ndim <= 3 && p.r.count <= (1 << 24);
+  if (p.r.kind == kMeanRolling) {
+    // Exact rolling mean: the tiled kernel when a tile fits, with the direct
+    // kernel for tiles whose bit span is too wide (or for the whole array).
+    int rc = setup_generic(p);
+    if (rc != NDF_OK) return rc;
+    if (tileable) {
+      setup_tile(p);
+      if (boxcar_configure(p, smem_limit)) {
+        p.algo = Algo::kBoxcarTile;
+        p.scratch_bytes = ((size_t)p.tile.t.tiles + 1) * sizeof(unsigned int);
+        cudaError_t e = cudaMalloc(&p.d_scratch, p.scratch_bytes);
+        if (e != cudaSuccess) {
+          cudaGetLastError();
+          return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+        }
+        return NDF_OK;
+      }
+    }
+    p.algo = Algo::kBoxcarDirect;
+    return NDF_OK;
+  }
   if (tileable) {
     setup_tile(p);
     std::vector<Candidate> cands = plan_candidates_impl(p, smem_limit);
@@ -547,6 +573,10 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
       break;
     case Algo::kMomentsGeneric:
       e = launch_generic_moments(p, in, out, s);
+      break;
+    case Algo::kBoxcarTile:
+    case Algo::kBoxcarDirect:
+      e = launch_boxcar(p, in, out, s);
       break;
   }
   if (e != cudaSuccess) return cuda_fail(e, algo_name(p.algo));

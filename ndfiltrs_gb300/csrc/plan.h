@@ -92,6 +92,8 @@ enum class Algo {
   kHistogram,
   kMomentsTile,
   kMomentsGeneric,
+  kBoxcarTile,    // exact rolling mean, tiled sliding integer sums
+  kBoxcarDirect,  // exact rolling mean, full-width direct sums
 };
 
 struct Plan {
@@ -177,6 +179,8 @@ cudaError_t launch_generic_select(const Plan& p, const void* in, void* out, cuda
 cudaError_t launch_tile_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_generic_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_boxcar(const Plan& p, const void* in, void* out, cudaStream_t s);
+bool boxcar_configure(Plan& p, int smem_limit);
 
 // Shared-memory bytes a tile kernel needs for `t` (0 when it does not fit).
 size_t tile_select_smem(const Plan& p, const Tile& t);

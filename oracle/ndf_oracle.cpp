@@ -27,6 +27,7 @@
 #include <limits>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -599,6 +600,153 @@ void filter_offsets(const Window& w, const T* input, double cval, const Reductio
     visit(w, input, center, cval, index.data(), [&](double v) { scratch.push_back(v); });
     output[center - start] = cast_out<T>(finish(r, scratch));
   }
+}
+
+// ---------------------------------------------------------------------------
+// Exact rectangular mean (kind mean_rolling, method="boxcar"):
+// src/boxcar.rs:142-399 with src/exact_sum.rs:215-349. Per window, the finite
+// samples are summed exactly as a two's-complement fixed-point integer in
+// units of 2^-1074 (35 words cover every finite binary64 value times any
+// count below 2^64), and the mean is the exact quotient by the finite count,
+// rounded once to nearest (ties to even) directly to the output type.
+// Counts decide NaN / +-inf first, as Counts::value (src/boxcar.rs:59-77).
+
+using u128 = unsigned __int128;
+
+struct ExactAcc {
+  static constexpr int kWords = 35;
+  uint64_t w[kWords] = {};
+
+  void add(double v) {
+    uint64_t bits;
+    std::memcpy(&bits, &v, 8);
+    const int e = (int)((bits >> 52) & 0x7ff);
+    const uint64_t frac = bits & ((1ull << 52) - 1);
+    const uint64_t m = e ? (frac | (1ull << 52)) : frac;
+    if (m == 0) return;
+    const int shift = e ? e - 1 : 0;  // v = m * 2^(shift - 1074)
+    const u128 payload = (u128)m << (shift % 64);
+    int i = shift / 64;
+    const uint64_t lo = (uint64_t)payload, hi = (uint64_t)(payload >> 64);
+    if ((bits >> 63) == 0) {
+      u128 carry = 0;
+      for (uint64_t part : {lo, hi}) {
+        const u128 t = (u128)w[i] + part + carry;
+        w[i++] = (uint64_t)t;
+        carry = t >> 64;
+      }
+      while (carry && i < kWords) {
+        const u128 t = (u128)w[i] + carry;
+        w[i++] = (uint64_t)t;
+        carry = t >> 64;
+      }
+    } else {
+      uint64_t borrow = 0;
+      for (uint64_t part : {lo, hi}) {
+        const uint64_t a = w[i];
+        const uint64_t d = a - part - borrow;
+        borrow = (a < part || (a - part) < borrow) ? 1 : 0;
+        w[i++] = d;
+      }
+      while (borrow && i < kWords) {
+        const uint64_t a = w[i];
+        w[i++] = a - 1;
+        borrow = a == 0 ? 1 : 0;
+      }
+    }
+  }
+};
+
+inline int bitlen128(u128 x) {
+  const uint64_t hi = (uint64_t)(x >> 64), lo = (uint64_t)x;
+  if (hi) return 128 - __builtin_clzll(hi);
+  return lo ? 64 - __builtin_clzll(lo) : 0;
+}
+
+// RN_T(S * 2^-1074 / n) for the exact sum S and a positive count n.
+template <class T>
+T exact_mean(const ExactAcc& acc, uint64_t n) {
+  constexpr int kW = ExactAcc::kWords;
+  constexpr int p = std::numeric_limits<T>::digits;             // 24 or 53
+  constexpr int unit = sizeof(T) == 4 ? 1074 - 149 : 0;           // T's subnormal unit
+  uint64_t m[kW];
+  const bool negative = (acc.w[kW - 1] >> 63) != 0;
+  uint64_t carry = 1;
+  for (int i = 0; i < kW; ++i) {
+    m[i] = negative ? ~acc.w[i] + carry : acc.w[i];
+    if (negative) carry = (carry && m[i] == 0) ? 1 : 0;
+  }
+  int top = kW - 1;
+  while (top >= 0 && m[top] == 0) --top;
+  using U = std::conditional_t<sizeof(T) == 4, uint32_t, uint64_t>;
+  const U sign = negative ? (U)1 << (sizeof(T) * 8 - 1) : 0;
+  T out;
+  if (top < 0) {
+    const U zero = 0;  // exact cancellation gives +0
+    std::memcpy(&out, &zero, sizeof(T));
+    return out;
+  }
+  const long B = (long)top * 64 + (64 - __builtin_clzll(m[top]));
+  const int t = 64 - __builtin_clzll(n);
+  const long s = std::max<long>(B - t - p - 1, unit);
+  auto word = [&](long i) -> uint64_t { return i >= 0 && i < kW ? m[i] : 0; };
+  const long wi = s / 64;
+  const int off = (int)(s % 64);
+  u128 high = (u128)(word(wi) >> off);
+  if (off) {
+    high |= (u128)word(wi + 1) << (64 - off);
+    high |= (u128)word(wi + 2) << (128 - off);
+  } else {
+    high |= (u128)word(wi + 1) << 64;
+  }
+  bool sticky = off && (word(wi) & ((1ull << off) - 1)) != 0;
+  for (long i = 0; i < wi && !sticky; ++i) sticky = m[i] != 0;
+  const u128 q = high / n, r = high % n;
+  const int k = std::max(bitlen128(q) - p, 0);
+  u128 mant;
+  bool up;
+  if (k > 0) {
+    mant = q >> k;
+    const bool guard = ((q >> (k - 1)) & 1) != 0;
+    const bool rest = (q & (((u128)1 << (k - 1)) - 1)) != 0 || r != 0 || sticky;
+    up = guard && (rest || (mant & 1));
+  } else {
+    // Only at the subnormal grid (s == unit), where no sample has bits below.
+    mant = q;
+    const u128 twice = 2 * r;
+    up = twice > n || (twice == n && (sticky || (mant & 1)));
+  }
+  const U bits = (U)(((u128)(s - unit + k) << (p - 1)) + mant + (up ? 1 : 0)) | sign;
+  std::memcpy(&out, &bits, sizeof(T));
+  return out;
+}
+
+struct BoxcarCounts {
+  uint64_t finite = 0, nan = 0, positive = 0, negative = 0;
+};
+
+// One window of the exact boxcar mean (Counts::sample / Counts::value).
+template <class T>
+T boxcar_window(const Window& w, const T* input, size_t center, double cval, const Policy& pol,
+                int64_t* index) {
+  ExactAcc acc;
+  BoxcarCounts c;
+  visit(w, input, center, cval, index, [&](double v) {
+    if (std::isnan(v)) {
+      if (!pol.omit) ++c.nan;
+    } else if (std::isfinite(v)) {
+      ++c.finite;
+      acc.add(v);
+    } else if (!(pol.omit && pol.ignore_inf)) {
+      if (v > 0) ++c.positive; else ++c.negative;
+    }
+  });
+  const uint64_t kept = c.finite + c.positive + c.negative;
+  if (c.nan || kept == 0 || (pol.omit && kept < pol.min_count) || (c.positive && c.negative))
+    return std::numeric_limits<T>::quiet_NaN();
+  if (c.positive) return std::numeric_limits<T>::infinity();
+  if (c.negative) return -std::numeric_limits<T>::infinity();
+  return exact_mean<T>(acc, c.finite);
 }
 
 // ---------------------------------------------------------------------------
@@ -1272,7 +1420,8 @@ int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* 
                               : "min_count must be between 1 and the number of window elements");
   if (kind == kPercentile && (!std::isfinite(q) || q < 0.0 || q > 100.0))
     return fail(kInvalid, "percentile must be finite and between zero and 100");
-  if (kind == kMeanRolling) return fail(kInvalid, "rolling means are not part of this oracle");
+  if (kind == kMeanRolling && footprint)
+    return fail(kInvalid, "rolling means require rectangular size, not footprint");
   bool hist = kind == kMedianHistogram || kind == kRankHistogram;
   if (hist) {
     if (footprint)
@@ -1292,6 +1441,21 @@ int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* 
                               parameter, threads, (float*)output);
     return histogram_filter(w, size, origin, (const double*)input, cval, r.policy, median,
                             parameter, threads, (double*)output);
+  }
+  if (kind == kMeanRolling) {
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      run_parallel(n, threads, [&](size_t s, size_t e) {
+        std::vector<int64_t> index(w.rank);
+        for (size_t center = s; center < e; ++center)
+          ((T*)output)[center] = boxcar_window<T>(w, (const T*)input, center, cval, r.policy, index.data());
+      });
+    };
+    if (f32)
+      run(float());
+    else
+      run(double());
+    return kOk;
   }
   if (kind == kMedianNetwork) {
     auto net = network_new(w.count, r.policy);

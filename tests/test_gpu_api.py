@@ -88,7 +88,9 @@ def test_validation_errors_before_device_work(gpu) -> None:
     with pytest.raises(ValueError, match="min_count"):
         nf.nanmedian_filter(np.ones(3), size=3, min_count=4)
     with pytest.raises(NotImplementedError):
-        nf.mean_filter(np.ones((5, 5)), 3, method="boxcar")
+        nf.mean_filter(np.ones((5, 5)), 3, method="separable")
+    with pytest.raises(ValueError, match="requires size, not footprint"):
+        nf.mean_filter(np.ones((5, 5)), footprint=np.ones((2, 3)), method="boxcar")
 
 
 def test_get_num_threads_is_device_parallelism(gpu) -> None:

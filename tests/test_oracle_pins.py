@@ -255,3 +255,75 @@ def test_histogram_rejects_oversized_support(oracle) -> None:
 
     with pytest.raises(OracleError):
         oracle.window_filter(np.zeros((1, 1)), "median_histogram", (70000, 70000))
+
+
+# ---------------------------------------------------------------------------
+# Exact boxcar mean (kind mean_rolling): src/boxcar.rs, src/exact_sum.rs.
+
+def _round_exact(value, dtype):
+    """The rational `value` rounded once to `dtype` (nearest, ties to even):
+    the nearest of the float64-derived candidate and its two neighbours."""
+    from fractions import Fraction
+
+    if value == 0:
+        return dtype(0)
+    candidate = dtype(float(value))
+    neighbours = [candidate, np.nextafter(candidate, dtype(-np.inf)), np.nextafter(candidate, dtype(np.inf))]
+    ubits = np.uint32 if dtype == np.float32 else np.uint64
+    return min((c for c in neighbours if np.isfinite(c)),
+               key=lambda c: (abs(Fraction(float(c)) - value), int(np.array(c, dtype=dtype).view(ubits)) & 1))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("odd_lower", [False, True])
+@pytest.mark.parametrize("direction", [-1, 0, 1])
+def test_boxcar_mean_rounds_once_beside_midpoints(oracle, dtype, odd_lower, direction) -> None:
+    """tests/test_rolling_mean.py:118-137: the mean (lower + upper) / 2 +
+    direction * tiny / 4 rounds once, directly to the dtype."""
+    lower = dtype(1)
+    if odd_lower:
+        lower = np.nextafter(lower, dtype(np.inf))
+    upper = np.nextafter(lower, dtype(np.inf))
+    tiny = np.nextafter(dtype(0), dtype(1))
+    array = np.array([2 * lower, 2 * upper, direction * tiny, 0], dtype=dtype)
+    expected = upper if direction > 0 or (direction == 0 and odd_lower) else lower
+    out = oracle.window_filter(array, "mean_rolling", (4,), mode="wrap")
+    np.testing.assert_array_equal(out, np.full(4, expected, dtype=dtype))
+
+
+def test_boxcar_mean_matches_rational_reference(oracle) -> None:
+    """Exact rational window means with NaN / inf counts, rounded once (the
+    rule of tests/test_rolling_mean.py:49-85), over wide-range values."""
+    import math
+    from fractions import Fraction
+
+    rng = np.random.default_rng(12)
+    for trial in range(120):
+        dtype = np.float32 if trial % 2 else np.float64
+        n = int(rng.integers(3, 10))
+        scale = 30 if dtype == np.float32 else 280
+        arr = (rng.normal(size=n) * 10.0 ** rng.integers(-scale, scale, size=n)).astype(dtype)
+        if trial % 3 == 0:
+            arr[rng.integers(0, n)] = [np.nan, np.inf, -np.inf, -0.0][trial % 4]
+        size = int(rng.integers(1, n + 1))
+        omit, ignore_inf = bool(trial % 2), bool(trial % 5 == 0)
+        out = oracle.window_filter(arr, "mean_rolling", (size,), mode="wrap", omit_nan=omit,
+                                   ignore_inf=ignore_inf)
+        for c in range(n):
+            values = [float(arr[(c + k - size // 2) % n]) for k in range(size)]
+            if omit:
+                values = [v for v in values if not (math.isnan(v) or (ignore_inf and math.isinf(v)))]
+            if not values or any(math.isnan(v) for v in values) or (math.inf in values and -math.inf in values):
+                expected = dtype(np.nan)
+            elif math.inf in values:
+                expected = dtype(np.inf)
+            elif -math.inf in values:
+                expected = dtype(-np.inf)
+            else:
+                expected = _round_exact(sum(map(Fraction, values), Fraction()) / len(values), dtype)
+            if np.isnan(expected):
+                assert np.isnan(out[c])
+            else:
+                ubits = np.uint32 if dtype == np.float32 else np.uint64
+                assert np.array(out[c]).view(ubits) == np.array(expected, dtype=dtype).view(ubits), \
+                    (trial, c, out[c], expected)
