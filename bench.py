@@ -251,6 +251,29 @@ class ClockSampler:
         }
 
 
+# ---------------------------------------------------------------------------
+# Replicas across ranks: every rank filters its own image; the job's time is
+# the slowest rank's and its throughput counts every rank's pixels.
+
+def max_over_ranks(value: float, dist, device, barrier: bool = True) -> float:
+    """The maximum of `value` over all ranks (the value itself without a
+    process group), after a barrier."""
+    if dist is None:
+        return float(value)
+    import torch
+
+    if barrier:
+        dist.barrier()
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, pixels: int, steps: int, seconds: float) -> float:
+    """Whole-job Mpix/s: all ranks' pixels over the slowest rank's time."""
+    return world * pixels * steps / seconds / 1e6
+
+
 def measured_peak_hbm() -> tuple[float, str]:
     path = ROOT / "MEASURED_PEAKS.json"
     if path.exists():
@@ -627,14 +650,9 @@ def main() -> None:
             step(i)
         end.record(stream)
         torch.cuda.synchronize()
-    elapsed_ms = start.elapsed_time(end)
-    if dist is not None:
-        dist.barrier()
-        t = torch.tensor([elapsed_ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(start.elapsed_time(end), dist, device)
     ms_per_step = elapsed_ms / args.steps
-    value = world * pixels * args.steps / (elapsed_ms / 1e3) / 1e6
+    value = replica_throughput(world, pixels, args.steps, elapsed_ms / 1e3)
 
     # Correctness spot check of the timed kernel against the oracle (not timed).
     check = None
@@ -662,12 +680,8 @@ def main() -> None:
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         plan.run_host_async(in_np, out_np, handle)
-    e2e_seconds = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_seconds], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_seconds = float(t.item())
-    e2e_value = world * pixels * e2e_steps / e2e_seconds / 1e6
+    e2e_seconds = max_over_ranks(time.perf_counter() - t0, dist, device, barrier=False)
+    e2e_value = replica_throughput(world, pixels, e2e_steps, e2e_seconds)
 
     peak, peak_kind = measured_peak_hbm()
     bytes_per_launch = pixels * image.itemsize * 2
