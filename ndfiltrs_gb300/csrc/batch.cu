@@ -34,6 +34,7 @@
 #include "network.cuh"
 #include "plan.h"
 #include "tma.cuh"
+#include "hostpool.h"
 
 struct ndf_plan {
   ndf::Plan p;
@@ -207,87 +208,6 @@ struct Segment {
 
 constexpr int kBranches = 8;
 constexpr int kChunks = 8;             // image groups of the host pipeline
-constexpr size_t kCopyPiece = 4 << 20; // bytes per host copy task
-
-// A fixed pool of host threads for the pageable <-> pinned copies of the
-// host pipeline (page faults and memcpy run in parallel).
-class CopyPool {
- public:
-  struct Piece {
-    void* dst;
-    const void* src;
-    size_t bytes;
-  };
-
-  explicit CopyPool(int threads) {
-    for (int i = 0; i < threads; ++i) workers_.emplace_back([this] { loop(); });
-  }
-  ~CopyPool() {
-    {
-      std::lock_guard<std::mutex> g(m_);
-      stop_ = true;
-    }
-    cv_.notify_all();
-    for (auto& t : workers_) t.join();
-  }
-  // Copies every piece and returns when all are done.
-  void run(const std::vector<Piece>& pieces) {
-    if (pieces.empty()) return;
-    {
-      std::lock_guard<std::mutex> g(m_);
-      job_ = &pieces;
-      next_ = 0;
-      done_ = 0;
-      ++generation_;
-    }
-    cv_.notify_all();
-    work();
-    std::unique_lock<std::mutex> g(m_);
-    done_cv_.wait(g, [&] { return done_ == pieces.size(); });
-    job_ = nullptr;
-  }
-
- private:
-  void work() {
-    for (;;) {
-      const Piece* p = nullptr;
-      {
-        std::lock_guard<std::mutex> g(m_);
-        if (!job_ || next_ >= job_->size()) return;
-        p = &(*job_)[next_++];
-      }
-      std::memcpy(p->dst, p->src, p->bytes);
-      std::lock_guard<std::mutex> g(m_);
-      if (++done_ == job_->size()) done_cv_.notify_all();
-    }
-  }
-  void loop() {
-    unsigned long long seen = 0;
-    for (;;) {
-      {
-        std::unique_lock<std::mutex> g(m_);
-        cv_.wait(g, [&] { return stop_ || (generation_ != seen && job_ && next_ < job_->size()); });
-        if (stop_) return;
-        seen = generation_;
-      }
-      work();
-    }
-  }
-
-  std::vector<std::thread> workers_;
-  std::mutex m_;
-  std::condition_variable cv_, done_cv_;
-  const std::vector<Piece>* job_ = nullptr;
-  size_t next_ = 0, done_ = 0;
-  unsigned long long generation_ = 0;
-  bool stop_ = false;
-};
-
-void add_pieces(std::vector<CopyPool::Piece>& out, void* dst, const void* src, size_t bytes) {
-  for (size_t off = 0; off < bytes; off += kCopyPiece)
-    out.push_back({(unsigned char*)dst + off, (const unsigned char*)src + off,
-                   std::min(kCopyPiece, bytes - off)});
-}
 
 }  // namespace
 
