@@ -56,7 +56,7 @@ extern "C" {
 #define NDF_KIND_MEDIAN_NETWORK 1
 #define NDF_KIND_MEDIAN_HISTOGRAM 2
 #define NDF_KIND_MEAN 3
-#define NDF_KIND_MEAN_ROLLING 4 /* out of scope: returns NDF_ERR_UNSUPPORTED */
+#define NDF_KIND_MEAN_ROLLING 4 /* exact boxcar mean (method="boxcar"), rectangular windows */
 #define NDF_KIND_MIN 5
 #define NDF_KIND_MAX 6
 #define NDF_KIND_VAR 7
