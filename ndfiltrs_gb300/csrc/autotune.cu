@@ -89,6 +89,8 @@ const char* algo_token(Algo a) {
       return "radix";
     case Algo::kMomentsTile:
       return "moments";
+    case Algo::kMomentsSlide:
+      return "slide";
     default:
       return "other";
   }
@@ -99,7 +101,8 @@ bool parse_algo(const std::string& t, Algo* a) {
                                                        {"box", Algo::kTileBox},
                                                        {"network", Algo::kTileNetwork},
                                                        {"radix", Algo::kTileRadix},
-                                                       {"moments", Algo::kMomentsTile}};
+                                                       {"moments", Algo::kMomentsTile},
+                                                       {"slide", Algo::kMomentsSlide}};
   for (const auto& n : names)
     if (t == n.first) {
       *a = n.second;

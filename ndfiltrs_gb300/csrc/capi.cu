@@ -57,6 +57,8 @@ const char* algo_name(Algo a) {
       return "boxcar_tile";
     case Algo::kBoxcarDirect:
       return "boxcar_direct";
+    case Algo::kMomentsSlide:
+      return "moments_slide";
   }
   return "unknown";
 }
@@ -439,6 +441,12 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
     return (moments ? tile_moments_smem(p, t) : tile_select_smem(p, t)) <= (size_t)smem_limit;
   };
   if (is_moment(p.r.kind)) {
+    // FP32C boxes: sliding exact sums first; the FP64 mode keeps the
+    // reference's per-window arithmetic.
+    if (p.r.moments == 0) {
+      Plan probe = p;
+      if (moments_slide_configure(probe, smem_limit)) out.push_back({Algo::kMomentsSlide, 0, 0});
+    }
     for (auto [tw, th] : tiles)
       if (fits_tile(tw, th, true)) out.push_back({Algo::kMomentsTile, tw, th});
     return out;
@@ -500,6 +508,9 @@ int apply_candidate_impl(Plan& p, const Candidate& c, int smem_limit) {
       set_tile(p, c.tw, c.th);
       p.smem_bytes = tile_moments_smem(p, p.tile.t);
       return upload_tile_taps(p);
+    case Algo::kMomentsSlide:
+      if (!moments_slide_configure(p, smem_limit)) return fail(NDF_ERR_UNSUPPORTED, "window too large");
+      return NDF_OK;
     default:
       return fail(NDF_ERR_UNSUPPORTED, "not a tile kernel");
   }
@@ -578,6 +589,9 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
     case Algo::kBoxcarTile:
     case Algo::kBoxcarDirect:
       e = launch_boxcar(p, in, out, s);
+      break;
+    case Algo::kMomentsSlide:
+      e = launch_moments_slide(p, in, out, s);
       break;
   }
   if (e != cudaSuccess) return cuda_fail(e, algo_name(p.algo));

@@ -94,6 +94,7 @@ enum class Algo {
   kMomentsGeneric,
   kBoxcarTile,    // exact rolling mean, tiled sliding integer sums
   kBoxcarDirect,  // exact rolling mean, full-width direct sums
+  kMomentsSlide,  // mean / var / std, sliding exact integer sums (boxes)
 };
 
 struct Plan {
@@ -180,6 +181,8 @@ cudaError_t launch_tile_moments(const Plan& p, const void* in, void* out, cudaSt
 cudaError_t launch_generic_moments(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_boxcar(const Plan& p, const void* in, void* out, cudaStream_t s);
+cudaError_t launch_moments_slide(const Plan& p, const void* in, void* out, cudaStream_t s);
+bool moments_slide_configure(Plan& p, int smem_limit);
 bool boxcar_configure(Plan& p, int smem_limit);
 
 // Shared-memory bytes a tile kernel needs for `t` (0 when it does not fit).

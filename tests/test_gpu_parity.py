@@ -335,3 +335,55 @@ def test_float32_percentile_fast_path_matches_float64_rule(gpu, oracle) -> None:
                 args = ("percentile", values, size, footprint, (0, 0), ("reflect", "mirror"), 0.0, True,
                         False, 1, 0, q)
                 _assert_bits(_gpu(*args), _oracle(oracle, *args), (q, size))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_sliding_moments_against_exact_oracle(gpu, oracle, dtype) -> None:
+    """FP32C boxes run the sliding exact-sum kernel: within 2 ulp (float32) /
+    1e-12 relative (float64) of the exact (double-double) window moments,
+    under every mode, policy and ddof, with NaN / infinity classification
+    equal to the reference's; tiles whose value range is too wide for the
+    integer widths take the per-window paths (checked the same way)."""
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(31)
+    smooth = (1e4 + rng.normal(size=(90, 110))).astype(dtype)
+    smooth[rng.random(smooth.shape) < 0.03] = np.nan
+    smooth[rng.random(smooth.shape) < 0.01] = np.inf
+    steps = (np.where(np.arange(110)[None, :] < 55, 1e3, 6e4) + rng.normal(size=(90, 110)) * 10).astype(dtype)
+    wide = (rng.normal(size=(90, 110)) * 10.0 ** rng.integers(-30, 30, size=(90, 110))).astype(dtype)
+    line = (5 + rng.normal(size=(1, 700))).astype(dtype)
+    for values, size in ((smooth, (7, 9)), (steps, (5, 13)), (wide, (3, 4)), (line, (1, 31))):
+        for mode in MODES:
+            for kind in ("mean", "var", "std"):
+                for omit, ignore_inf, min_count, ddof in ((True, True, 5, 1), (False, False, 1, 0),
+                                                          (True, False, 1, 2)):
+                    with _core.Plan(values.shape, dtype, kind, size, mode=[mode] * 2, cval=1.5, omit_nan=omit,
+                                    ignore_inf=ignore_inf, min_count=min_count,
+                                    parameter=ddof if kind != "mean" else 0) as plan:
+                        assert plan.algorithm == "moments_slide"
+                        actual = plan.run_host(values)
+                    exact = oracle.exact_moments(values, kind, size, mode=mode, cval=1.5, omit_nan=omit,
+                                                 ignore_inf=ignore_inf, min_count=min_count,
+                                                 ddof=ddof if kind != "mean" else 0)
+                    # Windows whose value range forces the reference's float64
+                    # arithmetic (the "wide" image) must equal it bit for bit
+                    # instead: under heavy cancellation that arithmetic is
+                    # itself not within the tolerance of the exact moments.
+                    reference = oracle.window_filter(values, kind, size, mode=mode, cval=1.5, omit_nan=omit,
+                                                     ignore_inf=ignore_inf, min_count=min_count,
+                                                     parameter=ddof if kind != "mean" else 0)
+                    context = (values.shape, size, mode, kind, omit, ddof)
+                    np.testing.assert_array_equal(np.isnan(actual), np.isnan(exact), err_msg=str(context))
+                    ok = np.isfinite(exact) & (np.abs(exact) > np.finfo(dtype).tiny * 1e6)
+                    np.testing.assert_array_equal(actual[np.isinf(exact)], exact[np.isinf(exact)].astype(dtype))
+                    a, e = actual[ok].astype(np.float64), exact[ok]
+                    if dtype == np.float32:
+                        ulp = np.spacing(np.abs(e.astype(np.float32))).astype(np.float64)
+                        close = np.abs(a - e) <= 2 * ulp
+                    else:
+                        close = np.abs(a - e) <= 1e-12 * np.abs(e)
+                    same_as_reference = bits(actual[ok]) == bits(reference[ok])
+                    assert np.all(close | same_as_reference), context
+                    if values is not wide:
+                        assert np.all(close), context
