@@ -194,61 +194,115 @@ def oracle_kind(kind: str) -> str:
 # Clock sampling during the timed region.
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """SM clock and clock-event reasons during the timed region, read (only
+    read) through NVML from the driver's libnvidia-ml every 2 ms in a
+    background thread plus at the region's start and end; falls back to
+    polling nvidia-smi when NVML cannot be loaded."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, device: int) -> None:
         self.device = device
-        self.proc = None
-        self.file = None
+        self.samples: list[tuple[float, int]] = []
+        self.max_mhz = None
+        self.source = "nvml"
+        self._stop = None
+        self._thread = None
+        self._nvml = None
+        self._handle = None
+        self._smi = None
+
+    def _open_nvml(self) -> bool:
+        import ctypes
+
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return False
+            handle = ctypes.c_void_p()
+            ok = False
+            try:
+                import torch
+
+                uuid = str(torch.cuda.get_device_properties(self.device).uuid)
+                ok = lib.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(handle)) == 0
+            except Exception:
+                ok = False
+            if not ok and lib.nvmlDeviceGetHandleByIndex_v2(self.device, ctypes.byref(handle)) != 0:
+                return False
+            self._nvml, self._handle = lib, handle
+            maxc = ctypes.c_uint(0)
+            if lib.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(maxc)) == 0:
+                self.max_mhz = float(maxc.value)
+            return True
+        except OSError:
+            return False
+
+    def _sample(self) -> None:
+        import ctypes
+
+        clock, reasons = ctypes.c_uint(0), ctypes.c_ulonglong(0)
+        if self._nvml.nvmlDeviceGetClockInfo(self._handle, 1, ctypes.byref(clock)) != 0:
+            return
+        getter = getattr(self._nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self._nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        getter(self._handle, ctypes.byref(reasons))
+        self.samples.append((float(clock.value), int(reasons.value)))
 
     def __enter__(self):
-        try:
-            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200", "-i", str(self.device)],
-                stdout=self.file, stderr=subprocess.DEVNULL,
-            )
-        except (OSError, FileNotFoundError):
-            self.proc = None
+        import threading
+
+        if self._open_nvml():
+            self._sample()
+            self._stop = threading.Event()
+
+            def loop() -> None:
+                while not self._stop.wait(0.002):
+                    self._sample()
+
+            self._thread = threading.Thread(target=loop, daemon=True)
+            self._thread.start()
+        else:
+            self.source = "nvidia-smi"
+            try:
+                self._file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+                self._smi = subprocess.Popen(
+                    ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active",
+                     "--format=csv,noheader,nounits", "-lms", "200", "-i", str(self.device)],
+                    stdout=self._file, stderr=subprocess.DEVNULL)
+            except (OSError, FileNotFoundError):
+                self._smi = None
         return self
 
     def __exit__(self, *exc) -> None:
-        if self.proc is not None:
-            self.proc.terminate()
+        if self._thread is not None:
+            self._stop.set()
+            self._thread.join(timeout=2)
+            self._sample()
+        if self._smi is not None:
+            self._smi.terminate()
             try:
-                self.proc.wait(timeout=5)
+                self._smi.wait(timeout=5)
             except subprocess.TimeoutExpired:
-                self.proc.kill()
+                self._smi.kill()
+            self._file.flush()
+            for line in Path(self._file.name).read_text().strip().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                try:
+                    self.samples.append((float(parts[0]), int(parts[2], 16)))
+                    self.max_mhz = float(parts[1])
+                except (ValueError, IndexError):
+                    continue
+            os.unlink(self._file.name)
 
     def summary(self) -> dict:
-        if self.proc is None or self.file is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.file.flush()
-        lines = Path(self.file.name).read_text().strip().splitlines()
-        os.unlink(self.file.name)
-        sm, smax, reasons = [], [], set()
-        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for line in lines:
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for name, flag in zip(names, parts[5:9]):
-                if flag.lower() == "active":
-                    reasons.add(name)
-        return {
-            "sm_mhz": statistics.median(sm) if sm else None,
-            "sm_max_mhz": max(smax) if smax else None,
-            "reasons": sorted(reasons),
-            "samples": len(sm),
-        }
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["no clock samples"],
+                    "samples": 0, "source": self.source}
+        reasons = sorted({name for _, bits in self.samples for mask, name in self.REASONS.items() if bits & mask})
+        return {"sm_mhz": statistics.median(mhz for mhz, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples), "source": self.source}
 
 
 # ---------------------------------------------------------------------------
