@@ -166,6 +166,9 @@ WORKLOADS = {
                                      min_count=5, parameter=1),
     "nanstd_31x31_4096_f64": Workload(lambda: precision_image(4096, dtype=np.float64), "std", (31, 31), "reflect",
                                       ignore_inf=True, min_count=5, parameter=1),
+    # Separable rectangular extrema (van Herk / Gil-Werman).
+    "nanmin_31x31_4096_f32": Workload(lambda: robust_image(4096), "min", (31, 31), "reflect"),
+    "nanmax_65x65_8192_f32": Workload(lambda: sky_image(8192), "max", (65, 65), "nearest"),
     # Exact rolling means (method="boxcar"), correctly rounded.
     "nanmean_boxcar_31x31_4096_f32": Workload(lambda: precision_image(4096), "mean_rolling", (31, 31), "reflect",
                                               ignore_inf=True, min_count=5),

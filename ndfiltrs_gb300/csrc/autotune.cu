@@ -91,6 +91,8 @@ const char* algo_token(Algo a) {
       return "moments";
     case Algo::kMomentsSlide:
       return "slide";
+    case Algo::kExtremaTile:
+      return "extrema";
     default:
       return "other";
   }
@@ -102,7 +104,8 @@ bool parse_algo(const std::string& t, Algo* a) {
                                                        {"network", Algo::kTileNetwork},
                                                        {"radix", Algo::kTileRadix},
                                                        {"moments", Algo::kMomentsTile},
-                                                       {"slide", Algo::kMomentsSlide}};
+                                                       {"slide", Algo::kMomentsSlide},
+                                                       {"extrema", Algo::kExtremaTile}};
   for (const auto& n : names)
     if (t == n.first) {
       *a = n.second;

@@ -59,6 +59,8 @@ const char* algo_name(Algo a) {
       return "boxcar_direct";
     case Algo::kMomentsSlide:
       return "moments_slide";
+    case Algo::kExtremaTile:
+      return "extrema_tile";
   }
   return "unknown";
 }
@@ -459,6 +461,14 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
     histogram_configure(probe);
     hist_ok = histogram_smem(probe) <= (size_t)smem_limit;
   }
+  // Rectangular minima / maxima: the separable kernel (its cost does not grow
+  // with the window) ahead of everything for windows wider than 5 x 5.
+  bool extrema_ok = false;
+  if (p.r.kind == kMin || p.r.kind == kMax) {
+    Plan probe = p;
+    extrema_ok = extrema_configure(probe, smem_limit);
+  }
+  if (extrema_ok && p.r.count > 25) out.push_back({Algo::kExtremaTile, 0, 0});
   if (hist_ok && (hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
   if (p.footprint.empty() && g.kd == 1 && !line && box_supported(p.dtype, g.kh, g.kw)) {
     Tile bt = box_tile(g);
@@ -472,6 +482,7 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
       out.push_back({Algo::kTileRadix, tw, th});
   }
   if (hist_ok && !(hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
+  if (extrema_ok && p.r.count <= 25) out.push_back({Algo::kExtremaTile, 0, 0});
   if (out.empty() && fits_tile(tiles[0].first, tiles[0].second, false))
     out.push_back({Algo::kTileRadix, tiles[0].first, tiles[0].second});
   return out;
@@ -510,6 +521,9 @@ int apply_candidate_impl(Plan& p, const Candidate& c, int smem_limit) {
       return upload_tile_taps(p);
     case Algo::kMomentsSlide:
       if (!moments_slide_configure(p, smem_limit)) return fail(NDF_ERR_UNSUPPORTED, "window too large");
+      return NDF_OK;
+    case Algo::kExtremaTile:
+      if (!extrema_configure(p, smem_limit)) return fail(NDF_ERR_UNSUPPORTED, "window too large");
       return NDF_OK;
     default:
       return fail(NDF_ERR_UNSUPPORTED, "not a tile kernel");
@@ -592,6 +606,9 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
       break;
     case Algo::kMomentsSlide:
       e = launch_moments_slide(p, in, out, s);
+      break;
+    case Algo::kExtremaTile:
+      e = launch_extrema(p, in, out, s);
       break;
   }
   if (e != cudaSuccess) return cuda_fail(e, algo_name(p.algo));

@@ -95,6 +95,7 @@ enum class Algo {
   kBoxcarTile,    // exact rolling mean, tiled sliding integer sums
   kBoxcarDirect,  // exact rolling mean, full-width direct sums
   kMomentsSlide,  // mean / var / std, sliding exact integer sums (boxes)
+  kExtremaTile,   // separable min / max (van Herk / Gil-Werman) over boxes
 };
 
 struct Plan {
@@ -183,6 +184,8 @@ cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStrea
 cudaError_t launch_boxcar(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_moments_slide(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool moments_slide_configure(Plan& p, int smem_limit);
+cudaError_t launch_extrema(const Plan& p, const void* in, void* out, cudaStream_t s);
+bool extrema_configure(Plan& p, int smem_limit);
 bool boxcar_configure(Plan& p, int smem_limit);
 
 // Shared-memory bytes a tile kernel needs for `t` (0 when it does not fit).
