@@ -663,20 +663,20 @@ inline int bitlen128(u128 x) {
   return lo ? 64 - __builtin_clzll(lo) : 0;
 }
 
-// RN_T(S * 2^-1074 / n) for the exact sum S and a positive count n.
+// RN_T(S * 2^(64 low - 1074) / n) for the exact sum S, held as `nw` words of
+// two's complement, and a positive count n.
 template <class T>
-T exact_mean(const ExactAcc& acc, uint64_t n) {
-  constexpr int kW = ExactAcc::kWords;
+T exact_mean(const uint64_t* words, int nw, int low, uint64_t n) {
   constexpr int p = std::numeric_limits<T>::digits;             // 24 or 53
   constexpr int unit = sizeof(T) == 4 ? 1074 - 149 : 0;           // T's subnormal unit
-  uint64_t m[kW];
-  const bool negative = (acc.w[kW - 1] >> 63) != 0;
+  uint64_t m[ExactAcc::kWords];
+  const bool negative = (words[nw - 1] >> 63) != 0;
   uint64_t carry = 1;
-  for (int i = 0; i < kW; ++i) {
-    m[i] = negative ? ~acc.w[i] + carry : acc.w[i];
+  for (int i = 0; i < nw; ++i) {
+    m[i] = negative ? ~words[i] + carry : words[i];
     if (negative) carry = (carry && m[i] == 0) ? 1 : 0;
   }
-  int top = kW - 1;
+  int top = nw - 1;
   while (top >= 0 && m[top] == 0) --top;
   using U = std::conditional_t<sizeof(T) == 4, uint32_t, uint64_t>;
   const U sign = negative ? (U)1 << (sizeof(T) * 8 - 1) : 0;
@@ -686,10 +686,11 @@ T exact_mean(const ExactAcc& acc, uint64_t n) {
     std::memcpy(&out, &zero, sizeof(T));
     return out;
   }
-  const long B = (long)top * 64 + (64 - __builtin_clzll(m[top]));
+  // Bit positions below are absolute (units of 2^-1074).
+  const long B = (long)(top + low) * 64 + (64 - __builtin_clzll(m[top]));
   const int t = 64 - __builtin_clzll(n);
   const long s = std::max<long>(B - t - p - 1, unit);
-  auto word = [&](long i) -> uint64_t { return i >= 0 && i < kW ? m[i] : 0; };
+  auto word = [&](long i) -> uint64_t { return i >= low && i < low + nw ? m[i - low] : 0; };
   const long wi = s / 64;
   const int off = (int)(s % 64);
   u128 high = (u128)(word(wi) >> off);
@@ -700,7 +701,7 @@ T exact_mean(const ExactAcc& acc, uint64_t n) {
     high |= (u128)word(wi + 1) << 64;
   }
   bool sticky = off && (word(wi) & ((1ull << off) - 1)) != 0;
-  for (long i = 0; i < wi && !sticky; ++i) sticky = m[i] != 0;
+  for (long i = low; i < wi && !sticky; ++i) sticky = word(i) != 0;
   const u128 q = high / n, r = high % n;
   const int k = std::max(bitlen128(q) - p, 0);
   u128 mant;
@@ -719,6 +720,11 @@ T exact_mean(const ExactAcc& acc, uint64_t n) {
   const U bits = (U)(((u128)(s - unit + k) << (p - 1)) + mant + (up ? 1 : 0)) | sign;
   std::memcpy(&out, &bits, sizeof(T));
   return out;
+}
+
+template <class T>
+T exact_mean(const ExactAcc& acc, uint64_t n) {
+  return exact_mean<T>(acc.w, ExactAcc::kWords, 0, n);
 }
 
 struct BoxcarCounts {
@@ -1347,6 +1353,321 @@ double exact_moment(const std::vector<double>& values, int which, uint64_t ddof)
   return root + (diff.hi + diff.lo) / (2.0 * root);
 }
 
+// ---------------------------------------------------------------------------
+// Separable passes for rectangular windows. WindowFilter::new
+// (src/plan.rs:267-289) routes minimum / maximum without a footprint to
+// extrema_into and every rolling mean to mean_into; both sweep one axis at a
+// time over lines of the array, padded through map_index.
+
+// A pass's boundary rule is the same for every line: source coordinate of
+// each padded position, or -1 for a constant-mode position outside.
+int map_line(int64_t length, int64_t first, int64_t count, int mode, std::vector<int64_t>* out) {
+  out->resize((size_t)count);
+  for (int64_t p = 0; p < count; ++p) {
+    int64_t m = 0;
+    int r = map_index(first + p, length, mode, &m);
+    if (r < 0) return fail(kInvalid, "zero-length axes cannot be padded");
+    (*out)[(size_t)p] = r == 1 ? m : -1;
+  }
+  return kOk;
+}
+
+// Summary, src/extrema.rs:11-62: the extremum so far and whether a
+// propagated NaN was seen; the empty summary holds NaN with nan == false.
+template <class T>
+struct Extremum {
+  T value;
+  bool nan;
+};
+
+template <class T>
+inline Extremum<T> extremum_sample(T v, const Policy& p) {
+  if (!p.omit) return {v, std::isnan(v)};
+  if (retained(v, p)) return {v, false};
+  return {std::numeric_limits<T>::quiet_NaN(), false};
+}
+
+template <class T>
+inline Extremum<T> extremum_combine(Extremum<T> a, Extremum<T> b, bool maximum) {
+  if (a.nan || b.nan) return {std::numeric_limits<T>::quiet_NaN(), true};
+  if (std::isnan(a.value)) return b;
+  if (std::isnan(b.value)) return a;
+  const uint64_t ka = total_key(a.value), kb = total_key(b.value);
+  return (maximum ? ka < kb : ka > kb) ? b : a;
+}
+
+// extrema_into, src/extrema.rs:124-437 (van Herk / Gil-Werman): along each
+// axis, prefix and suffix combinations within blocks of the window length
+// give every window as suffix[p] + prefix[p + w - 1]; retained counts follow
+// the same blocks when min_count > 1.
+template <class T>
+int extrema_separable(const Window& w, const uint64_t* size, const int64_t* origin,
+                      const T* input, double cval_d, const Policy& pol, bool maximum,
+                      int threads, T* output) {
+  const size_t n = w.out_len;
+  const T cval = (T)cval_d;
+  std::vector<Extremum<T>> prev(n), next(n);
+  const bool counting = pol.omit && pol.min_count > 1;
+  std::vector<uint64_t> prev_n, next_n;
+  run_parallel(n, threads, [&](size_t s, size_t e) {
+    for (size_t i = s; i < e; ++i) prev[i] = extremum_sample(input[i], pol);
+  });
+  if (counting) {
+    prev_n.resize(n);
+    next_n.resize(n);
+    for (size_t i = 0; i < n; ++i) prev_n[i] = retained(input[i], pol) ? 1 : 0;
+  }
+  uint64_t prior_volume = 1;
+  for (int axis = 0; axis < w.rank; ++axis) {
+    const int64_t length = w.shape[axis], stride = w.strides[axis], block = length * stride;
+    const int64_t win = (int64_t)size[axis], anchor = win / 2 + origin[axis];
+    const int64_t padded = length + win - 1;
+    std::vector<int64_t> source;
+    int rc = map_line(length, -anchor, padded, w.modes[axis], &source);
+    if (rc) return rc;
+    const Extremum<T> outside = extremum_sample(cval, pol);
+    const uint64_t outside_n = retained(cval, pol) ? prior_volume : 0;
+    run_parallel(n / (size_t)length, threads, [&](size_t s, size_t e) {
+      std::vector<Extremum<T>> pad(padded), pre(padded), suf(padded);
+      std::vector<uint64_t> pn, cpre, csuf;
+      if (counting) {
+        pn.resize(padded);
+        cpre.resize(padded);
+        csuf.resize(padded);
+      }
+      for (size_t line = s; line < e; ++line) {
+        const int64_t base = ((int64_t)line / stride) * block + (int64_t)line % stride;
+        for (int64_t p = 0; p < padded; ++p) {
+          const int64_t src = source[(size_t)p];
+          pad[p] = src >= 0 ? prev[(size_t)(base + src * stride)] : outside;
+          if (counting) pn[p] = src >= 0 ? prev_n[(size_t)(base + src * stride)] : outside_n;
+        }
+        for (int64_t p = 0; p < padded; ++p) {
+          const bool start = p % win == 0;
+          pre[p] = start ? pad[p] : extremum_combine(pre[p - 1], pad[p], maximum);
+          if (counting) cpre[p] = start ? pn[p] : cpre[p - 1] + pn[p];
+        }
+        for (int64_t p = padded - 1; p >= 0; --p) {
+          const bool stop = p == padded - 1 || p % win == win - 1;
+          suf[p] = stop ? pad[p] : extremum_combine(pad[p], suf[p + 1], maximum);
+          if (counting) csuf[p] = stop ? pn[p] : csuf[p + 1] + pn[p];
+        }
+        for (int64_t c = 0; c < length; ++c) {
+          const int64_t end = c + win - 1;
+          const size_t dst = (size_t)(base + c * stride);
+          next[dst] = extremum_combine(suf[c], pre[end], maximum);
+          if (counting)
+            next_n[dst] = c / win == end / win ? cpre[end] - cpre[c] + pn[c] : csuf[c] + cpre[end];
+        }
+      }
+    });
+    std::swap(prev, next);
+    std::swap(prev_n, next_n);
+    prior_volume *= (uint64_t)win;
+  }
+  run_parallel(n, threads, [&](size_t s, size_t e) {
+    for (size_t i = s; i < e; ++i) {
+      const bool missing = prev[i].nan || (counting && prev_n[i] < pol.min_count);
+      output[i] = missing ? std::numeric_limits<T>::quiet_NaN() : prev[i].value;
+    }
+  });
+  return kOk;
+}
+
+// Counts::sample, src/boxcar.rs:17-33.
+inline BoxcarCounts boxcar_sample(double v, const Policy& p) {
+  BoxcarCounts c;
+  if (std::isnan(v)) {
+    c.nan = p.omit ? 0 : 1;
+  } else if (std::isfinite(v)) {
+    c.finite = 1;
+  } else if (!(p.omit && p.ignore_inf)) {
+    c.positive = v > 0 ? 1 : 0;
+    c.negative = v < 0 ? 1 : 0;
+  }
+  return c;
+}
+
+// Significand bits of a finite nonzero binary64 as (lowest, highest) bit
+// positions in units of 2^-1074.
+inline void bit_range(double v, int* lowest, int* highest) {
+  const uint64_t bits = bits64(v);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  const uint64_t m = (bits & ((1ull << 52) - 1)) | (e ? 1ull << 52 : 0);
+  const int shift = e ? e - 1 : 0;
+  *lowest = shift + __builtin_ctzll(m);
+  *highest = shift + 63 - __builtin_clzll(m);
+}
+
+// v as a `words`-word two's-complement integer in units of 2^(64 low - 1074);
+// the span guarantees that no set bit falls below the unit or above the top.
+inline void encode_span(double v, int low, int words, uint64_t* out) {
+  std::fill(out, out + words, 0);
+  const uint64_t bits = bits64(v);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  uint64_t m = (bits & ((1ull << 52) - 1)) | (e ? 1ull << 52 : 0);
+  if (m == 0) return;
+  int pos = (e ? e - 1 : 0) - 64 * low;
+  if (pos < 0) {
+    m >>= -pos;
+    pos = 0;
+  }
+  const u128 payload = (u128)m << (pos % 64);
+  const int i = pos / 64;
+  out[i] = (uint64_t)payload;
+  if (i + 1 < words) out[i + 1] = (uint64_t)(payload >> 64);
+  if (bits >> 63) {
+    uint64_t carry = 1;
+    for (int k = 0; k < words; ++k) {
+      out[k] = ~out[k] + carry;
+      carry = (carry && out[k] == 0) ? 1 : 0;
+    }
+  }
+}
+
+inline void span_add(uint64_t* acc, const uint64_t* v, int words, bool subtract) {
+  uint64_t carry = subtract ? 1 : 0;
+  for (int k = 0; k < words; ++k) {
+    const uint64_t x = subtract ? ~v[k] : v[k];
+    const u128 t = (u128)acc[k] + x + carry;
+    acc[k] = (uint64_t)t;
+    carry = (uint64_t)(t >> 64);
+  }
+}
+
+// mean_into, src/boxcar.rs:140-342, with word_span (src/boxcar.rs:104-138):
+// one span of words for every intermediate sum, exact sliding sums along
+// each axis (each pass stores its axis innermost, so the last pass restores
+// C order), one correctly rounded division at the end.
+template <class T>
+int boxcar_separable(const Window& w, const uint64_t* size, const int64_t* origin,
+                     const T* input, double cval_d, const Policy& pol, int threads, T* output) {
+  const size_t n = w.out_len;
+  const int rank = w.rank;
+  const double cval = (double)(T)cval_d;
+  uint64_t volume = 1;
+  for (int a = 0; a < rank; ++a) volume *= size[a];
+  bool constant = false;
+  for (int a = 0; a < rank; ++a) constant = constant || w.modes[a] == kConstant;
+  int lowest = INT32_MAX, highest = 0;
+  for (size_t i = 0; i <= n; ++i) {
+    const double v = i < n ? (double)input[i] : cval;
+    if (i == n && !constant) break;
+    if (!std::isfinite(v) || v == 0.0) continue;
+    int lo, hi;
+    bit_range(v, &lo, &hi);
+    lowest = std::min(lowest, lo);
+    highest = std::max(highest, hi);
+  }
+  int low = 0, words = 1;
+  if (lowest != INT32_MAX) {
+    const int count_bits = volume > 1 ? 64 - __builtin_clzll(volume - 1) : 0;
+    low = lowest / 64;
+    words = (highest + 1 + count_bits + 1 + 63) / 64 - low;
+  }
+  std::vector<uint64_t> prev(n * words), next(n * words);
+  std::vector<BoxcarCounts> prev_c(n), next_c(n);
+  run_parallel(n, threads, [&](size_t s, size_t e) {
+    for (size_t i = s; i < e; ++i) {
+      const double v = (double)input[i];
+      prev_c[i] = boxcar_sample(v, pol);
+      if (std::isfinite(v)) encode_span(v, low, words, &prev[i * words]);
+    }
+  });
+  std::vector<uint64_t> padding(words, 0);
+  BoxcarCounts padding_c = boxcar_sample(cval, pol);
+  if (std::isfinite(cval) && constant) encode_span(cval, low, words, padding.data());
+  std::vector<int64_t> strides(w.strides.begin(), w.strides.end());
+  for (int axis = 0; axis < rank; ++axis) {
+    const int64_t length = w.shape[axis], stride = strides[axis];
+    const int64_t win = (int64_t)size[axis], anchor = win / 2 + origin[axis];
+    std::vector<int64_t> first, leaving, entering;
+    int rc = map_line(length, -anchor, win, w.modes[axis], &first);
+    if (!rc) rc = map_line(length, -anchor, length - 1, w.modes[axis], &leaving);
+    if (!rc) rc = map_line(length, win - anchor, length - 1, w.modes[axis], &entering);
+    if (rc) return rc;
+    run_parallel(n / (size_t)length, threads, [&](size_t s, size_t e) {
+      std::vector<uint64_t> sum(words);
+      for (size_t line = s; line < e; ++line) {
+        int64_t base = 0, rest = (int64_t)line;
+        for (int other = rank - 1; other >= 0; --other) {
+          if (other == axis) continue;
+          base += (rest % w.shape[other]) * strides[other];
+          rest /= w.shape[other];
+        }
+        auto words_at = [&](int64_t src) -> const uint64_t* {
+          return src >= 0 ? &prev[(size_t)(base + src * stride) * words] : padding.data();
+        };
+        auto counts_at = [&](int64_t src) -> const BoxcarCounts& {
+          return src >= 0 ? prev_c[(size_t)(base + src * stride)] : padding_c;
+        };
+        auto add_counts = [](BoxcarCounts& a, const BoxcarCounts& b, bool subtract) {
+          if (subtract) {
+            a.finite -= b.finite; a.nan -= b.nan; a.positive -= b.positive; a.negative -= b.negative;
+          } else {
+            a.finite += b.finite; a.nan += b.nan; a.positive += b.positive; a.negative += b.negative;
+          }
+        };
+        std::fill(sum.begin(), sum.end(), 0);
+        BoxcarCounts count;
+        for (int64_t t = 0; t < win; ++t) {
+          span_add(sum.data(), words_at(first[(size_t)t]), words, false);
+          add_counts(count, counts_at(first[(size_t)t]), false);
+        }
+        uint64_t* dst = &next[(size_t)line * (size_t)length * words];
+        BoxcarCounts* dst_c = &next_c[(size_t)line * (size_t)length];
+        for (int64_t c = 0; c < length; ++c) {
+          std::copy(sum.begin(), sum.end(), dst + (size_t)c * words);
+          dst_c[c] = count;
+          if (c + 1 < length) {
+            span_add(sum.data(), words_at(leaving[(size_t)c]), words, true);
+            add_counts(count, counts_at(leaving[(size_t)c]), true);
+            span_add(sum.data(), words_at(entering[(size_t)c]), words, false);
+            add_counts(count, counts_at(entering[(size_t)c]), false);
+          }
+        }
+      }
+    });
+    std::swap(prev, next);
+    std::swap(prev_c, next_c);
+    strides[axis] = 1;
+    int64_t step = length;
+    for (int other = rank - 1; other >= 0; --other) {
+      if (other == axis) continue;
+      strides[other] = step;
+      step *= w.shape[other];
+    }
+    u128 carry = 0;
+    for (int k = 0; k < words; ++k) {
+      const u128 t = (u128)padding[k] * (uint64_t)win + carry;
+      padding[k] = (uint64_t)t;
+      carry = t >> 64;
+    }
+    padding_c.finite *= win;
+    padding_c.nan *= win;
+    padding_c.positive *= win;
+    padding_c.negative *= win;
+  }
+  run_parallel(n, threads, [&](size_t s, size_t e) {
+    for (size_t i = s; i < e; ++i) {
+      const BoxcarCounts& c = prev_c[i];
+      const uint64_t kept = c.finite + c.positive + c.negative;
+      T v;
+      if (c.nan || kept == 0 || (pol.omit && kept < pol.min_count) || (c.positive && c.negative)) {
+        v = std::numeric_limits<T>::quiet_NaN();
+      } else if (c.positive) {
+        v = std::numeric_limits<T>::infinity();
+      } else if (c.negative) {
+        v = -std::numeric_limits<T>::infinity();
+      } else {
+        v = exact_mean<T>(&prev[i * words], words, low, c.finite);
+      }
+      output[i] = v;
+    }
+  });
+  return kOk;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1396,16 +1717,21 @@ uint64_t ndfo_network_size(uint64_t count, int32_t omit) {
 
 // window_filter / robust_filter(kind="percentile") over one C-contiguous
 // array; `dtype` 0 = float32, 1 = float64. `kind` uses the C-ABI numbering.
-int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* input,
-                void* output, const uint64_t* size, const uint8_t* footprint,
-                const int64_t* origin, const int32_t* modes, double cval, int32_t kind,
-                int32_t omit_nan, int32_t ignore_inf, uint64_t min_count, uint64_t parameter,
-                double q, int32_t threads) {
+// `direct` != 0 visits every window (the traversal that the separable
+// passes must equal bit for bit, as src/extrema.rs:459-894 and
+// src/boxcar.rs:344-421 check); 0 follows WindowFilter::new's choice.
+int ndfo_filter_ex(int32_t dtype, int32_t rank, const uint64_t* shape, const void* input,
+                   void* output, const uint64_t* size, const uint8_t* footprint,
+                   const int64_t* origin, const int32_t* modes, double cval, int32_t kind,
+                   int32_t omit_nan, int32_t ignore_inf, uint64_t min_count, uint64_t parameter,
+                   double q, int32_t threads, int32_t direct) {
   Window w;
-  // Histogram plans validate the rectangle without materializing taps
-  // (src/plan.rs:294-312 calls validate_rectangular, not Window::new).
+  // Histogram and separable plans validate the rectangle without
+  // materializing taps (src/plan.rs:267-312 calls validate_rectangular, not
+  // Window::new).
   bool hist_plan = kind == kMedianHistogram || kind == kRankHistogram;
-  int rc = window_new(rank, shape, size, footprint, origin, modes, &w, !hist_plan);
+  bool separable = !direct && ((!footprint && (kind == kMin || kind == kMax)) || kind == kMeanRolling);
+  int rc = window_new(rank, shape, size, footprint, origin, modes, &w, !hist_plan && !separable);
   if (rc) return rc;
   Reduction r;
   r.kind = kind;
@@ -1441,6 +1767,18 @@ int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* 
                               parameter, threads, (float*)output);
     return histogram_filter(w, size, origin, (const double*)input, cval, r.policy, median,
                             parameter, threads, (double*)output);
+  }
+  if (separable) {
+    const bool maximum = kind == kMax;
+    if (kind == kMeanRolling)
+      return f32 ? boxcar_separable(w, size, origin, (const float*)input, cval, r.policy, threads,
+                                    (float*)output)
+                 : boxcar_separable(w, size, origin, (const double*)input, cval, r.policy,
+                                    threads, (double*)output);
+    return f32 ? extrema_separable(w, size, origin, (const float*)input, cval, r.policy, maximum,
+                                   threads, (float*)output)
+               : extrema_separable(w, size, origin, (const double*)input, cval, r.policy,
+                                   maximum, threads, (double*)output);
   }
   if (kind == kMeanRolling) {
     auto run = [&](auto tag) {
@@ -1480,6 +1818,15 @@ int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* 
     });
   }
   return kOk;
+}
+
+int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* input,
+                void* output, const uint64_t* size, const uint8_t* footprint,
+                const int64_t* origin, const int32_t* modes, double cval, int32_t kind,
+                int32_t omit_nan, int32_t ignore_inf, uint64_t min_count, uint64_t parameter,
+                double q, int32_t threads) {
+  return ndfo_filter_ex(dtype, rank, shape, input, output, size, footprint, origin, modes, cval,
+                        kind, omit_nan, ignore_inf, min_count, parameter, q, threads, 0);
 }
 
 // Exact (double-double) mean/var/std of every window, rounded to float64,

@@ -107,6 +107,8 @@ def lib() -> ctypes.CDLL:
             ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_int32,
         ]
         handle.ndfo_filter.restype = ctypes.c_int
+        handle.ndfo_filter_ex.argtypes = handle.ndfo_filter.argtypes + [ctypes.c_int32]
+        handle.ndfo_filter_ex.restype = ctypes.c_int
         handle.ndfo_exact_moments.argtypes = [
             ctypes.c_int32, ctypes.c_int32, u64p, vp, vp, u64p, u8p, i64p, i32p,
             ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
@@ -172,8 +174,13 @@ def window_filter(
     parameter: int = 0,
     q: float = 50.0,
     threads: int | None = None,
+    direct: bool = False,
 ) -> np.ndarray:
-    """Run one reduction of the CPU restatement over a C-contiguous array."""
+    """Run one reduction of the CPU restatement over a C-contiguous array.
+
+    Rectangular minimum / maximum and rolling means take the reference's
+    separable passes unless ``direct`` asks for a traversal of every window.
+    """
     array = np.ascontiguousarray(array)
     if array.dtype not in (np.float32, np.float64):
         raise TypeError("oracle input must be float32 or float64")
@@ -182,7 +189,7 @@ def window_filter(
     fp_ptr = (
         fp.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) if fp is not None else None
     )
-    rc = lib().ndfo_filter(
+    rc = lib().ndfo_filter_ex(
         0 if array.dtype == np.float32 else 1,
         array.ndim,
         shape,
@@ -200,6 +207,7 @@ def window_filter(
         int(parameter),
         float(q),
         int(threads or default_threads()),
+        int(bool(direct)),
     )
     if rc != 0:
         raise OracleError(rc, lib().ndfo_last_error().decode())
