@@ -646,6 +646,8 @@ def main() -> None:
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--precision", action=argparse.BooleanOptionalAction, default=True,
                         help="add the nanstd precision study to the line")
+    parser.add_argument("--pin-kernel", default=None,
+                        help="kernel family the plan takes when it is a candidate (A/B comparisons)")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload == "batch_mixed":
@@ -677,6 +679,8 @@ def main() -> None:
     __graft_entry__.build()
     import ndfiltrs_gb300 as nf
 
+    if args.pin_kernel:
+        nf._core.pin_kernel(args.pin_kernel)
     image = spec.gen()  # every rank builds its own replica of the workload
     shape = image.shape
     pixels = image.size

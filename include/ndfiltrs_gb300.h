@@ -219,6 +219,12 @@ int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32_t dtype, i
 int ndf_set_autotune(int32_t mode, const char* cache_path);
 /* Number of measured choices known (loading the file first). */
 int32_t ndf_autotune_entries(void);
+/* Pin the kernel family ("histogram", "box", "network", "radix", "moments",
+ * "slide", "extrema", "passes", "boxcar", "band") that plans take whenever
+ * it is one of their candidates, ahead of the autotuner; NULL or "" unpins.
+ * For A/B comparisons and tests: every family gives the same results. No
+ * counterpart in the reference. */
+int ndf_pin_kernel(const char* family);
 
 /* ---- TMA staging and bounded waits. Interior halo tiles of the tile
  * kernels are staged by one TMA (cp.async.bulk.tensor) copy each; every

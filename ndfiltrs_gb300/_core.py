@@ -150,6 +150,8 @@ def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
                 handle.ndf_set_autotune.argtypes = [ctypes.c_int32, ctypes.c_char_p]
                 handle.ndf_set_autotune.restype = ctypes.c_int
                 handle.ndf_autotune_entries.restype = ctypes.c_int32
+                handle.ndf_pin_kernel.argtypes = [ctypes.c_char_p]
+                handle.ndf_pin_kernel.restype = ctypes.c_int
                 handle.ndf_set_tma.argtypes = [ctypes.c_int32]
                 handle.ndf_set_tma.restype = ctypes.c_int
                 handle.ndf_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
@@ -561,6 +563,15 @@ def autotune_entries() -> int:
     """Number of measured kernel choices known to the autotuner."""
     lib, _ = _load()
     return int(lib.ndf_autotune_entries())
+
+
+def pin_kernel(family: str | None) -> None:
+    """Make plans take kernel ``family`` ("histogram", "box", "network",
+    "radix", "moments", "slide", "extrema", "passes", "boxcar", "band")
+    whenever it is one of their candidates; None unpins. Results never
+    depend on it."""
+    lib, _ = _load()
+    _check(lib.ndf_pin_kernel(None if family is None else str(family).encode()), lib)
 
 
 def set_tma(enabled: bool) -> None:

@@ -49,6 +49,7 @@ struct TuneCache {
   std::string path;  // "" keeps choices in memory only
   bool loaded = false;
   std::map<std::string, TuneEntry> entries;
+  std::string pinned;  // kernel family every choice takes when offered
 };
 
 TuneCache& cache() {
@@ -93,6 +94,12 @@ const char* algo_token(Algo a) {
       return "slide";
     case Algo::kExtremaTile:
       return "extrema";
+    case Algo::kBoxcarTile:
+      return "boxcar";
+    case Algo::kBoxcarBand:
+      return "band";
+    case Algo::kExtremaPasses:
+      return "passes";
     default:
       return "other";
   }
@@ -105,7 +112,10 @@ bool parse_algo(const std::string& t, Algo* a) {
                                                        {"radix", Algo::kTileRadix},
                                                        {"moments", Algo::kMomentsTile},
                                                        {"slide", Algo::kMomentsSlide},
-                                                       {"extrema", Algo::kExtremaTile}};
+                                                       {"extrema", Algo::kExtremaTile},
+                                                       {"boxcar", Algo::kBoxcarTile},
+                                                       {"band", Algo::kBoxcarBand},
+                                                       {"passes", Algo::kExtremaPasses}};
   for (const auto& n : names)
     if (t == n.first) {
       *a = n.second;
@@ -168,6 +178,8 @@ const char* statistic_class(const Reduce& r) {
     case kVar:
     case kStd:
       return r.moments ? "moments64" : "moments32c";
+    case kMeanRolling:
+      return "boxcar";
     default:
       return "other";
   }
@@ -317,6 +329,9 @@ TuneEntry measure(const Plan& p, const std::vector<Candidate>& cands, int smem_l
 Candidate autotune_pick(const Plan& p, const std::vector<Candidate>& cands, int smem_limit) {
   TuneCache& c = cache();
   std::lock_guard<std::mutex> guard(c.lock);
+  if (!c.pinned.empty())
+    for (const Candidate& k : cands)
+      if (c.pinned == algo_token(k.algo)) return k;
   const int mode = mode_locked(c);
   if (mode == 0) return cands[0];
   load_locked(c);
@@ -350,6 +365,17 @@ int ndf_set_autotune(int32_t mode, const char* cache_path) {
     c.loaded = false;
     c.entries.clear();
   }
+  return NDF_OK;
+}
+
+int ndf_pin_kernel(const char* family) {
+  using namespace ndf;
+  Algo a;
+  if (family && *family && !parse_algo(family, &a))
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "unknown kernel family");
+  TuneCache& c = cache();
+  std::lock_guard<std::mutex> guard(c.lock);
+  c.pinned = family ? family : "";
   return NDF_OK;
 }
 

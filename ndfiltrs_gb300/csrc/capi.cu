@@ -57,6 +57,10 @@ const char* algo_name(Algo a) {
       return "boxcar_tile";
     case Algo::kBoxcarDirect:
       return "boxcar_direct";
+    case Algo::kBoxcarBand:
+      return "boxcar_band";
+    case Algo::kExtremaPasses:
+      return "extrema_passes";
     case Algo::kMomentsSlide:
       return "moments_slide";
     case Algo::kExtremaTile:
@@ -442,6 +446,15 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
     t.SH = th + g.kh - 1;
     return (moments ? tile_moments_smem(p, t) : tile_select_smem(p, t)) <= (size_t)smem_limit;
   };
+  if (p.r.kind == kMeanRolling) {
+    // Exact rolling means: the band kernel (its cost does not grow with the
+    // window) and the tiled kernel; the direct kernel when neither fits.
+    Plan probe = p;
+    if (boxcar_band_configure(probe, smem_limit)) out.push_back({Algo::kBoxcarBand, 0, 0});
+    probe = p;
+    if (boxcar_configure(probe, smem_limit)) out.push_back({Algo::kBoxcarTile, 0, 0});
+    return out;
+  }
   if (is_moment(p.r.kind)) {
     // FP32C boxes: sliding exact sums first; the FP64 mode keeps the
     // reference's per-window arithmetic.
@@ -463,11 +476,14 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
   }
   // Rectangular minima / maxima: the separable kernel (its cost does not grow
   // with the window) ahead of everything for windows wider than 5 x 5.
-  bool extrema_ok = false;
+  bool extrema_ok = false, passes_ok = false;
   if (p.r.kind == kMin || p.r.kind == kMax) {
     Plan probe = p;
     extrema_ok = extrema_configure(probe, smem_limit);
+    probe = p;
+    passes_ok = extrema_passes_configure(probe, smem_limit);
   }
+  if (passes_ok && p.r.count > 25) out.push_back({Algo::kExtremaPasses, 0, 0});
   if (extrema_ok && p.r.count > 25) out.push_back({Algo::kExtremaTile, 0, 0});
   if (hist_ok && (hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
   if (p.footprint.empty() && g.kd == 1 && !line && box_supported(p.dtype, g.kh, g.kw)) {
@@ -482,6 +498,7 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
       out.push_back({Algo::kTileRadix, tw, th});
   }
   if (hist_ok && !(hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
+  if (passes_ok && p.r.count <= 25) out.push_back({Algo::kExtremaPasses, 0, 0});
   if (extrema_ok && p.r.count <= 25) out.push_back({Algo::kExtremaTile, 0, 0});
   if (out.empty() && fits_tile(tiles[0].first, tiles[0].second, false))
     out.push_back({Algo::kTileRadix, tiles[0].first, tiles[0].second});
@@ -525,6 +542,35 @@ int apply_candidate_impl(Plan& p, const Candidate& c, int smem_limit) {
     case Algo::kExtremaTile:
       if (!extrema_configure(p, smem_limit)) return fail(NDF_ERR_UNSUPPORTED, "window too large");
       return NDF_OK;
+    case Algo::kExtremaPasses: {
+      if (!extrema_passes_configure(p, smem_limit)) return fail(NDF_ERR_UNSUPPORTED, "window too large");
+      cudaError_t e = cudaMalloc(&p.d_scratch, p.scratch_bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        p.d_scratch = nullptr;
+        return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+      }
+      return NDF_OK;
+    }
+    case Algo::kBoxcarBand:
+    case Algo::kBoxcarTile: {
+      // Both finish over-wide spans with the direct kernel's taps.
+      if (!p.d_gen_taps) {
+        int rc = setup_generic(p);
+        if (rc != NDF_OK) return rc;
+      }
+      const bool band = c.algo == Algo::kBoxcarBand;
+      if (!(band ? boxcar_band_configure(p, smem_limit) : boxcar_configure(p, smem_limit)))
+        return fail(NDF_ERR_UNSUPPORTED, "window too large");
+      p.scratch_bytes = ((size_t)p.tile.t.tiles * (band ? 2 : 1) + 2) * sizeof(unsigned int);
+      cudaError_t e = cudaMalloc(&p.d_scratch, p.scratch_bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        p.d_scratch = nullptr;
+        return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+      }
+      return NDF_OK;
+    }
     default:
       return fail(NDF_ERR_UNSUPPORTED, "not a tile kernel");
   }
@@ -541,21 +587,16 @@ int choose_algorithm(Plan& p, int smem_limit) {
   }
   const bool tileable = p.ndim <= 3 && p.r.count <= (1 << 24);
   if (p.r.kind == kMeanRolling) {
-    // Exact rolling mean: the tiled kernel when a tile fits, with the direct
-    // kernel for tiles whose bit span is too wide (or for the whole array).
+    // Exact rolling mean: the band or tiled kernel when one fits, with the
+    // direct kernel for spans too wide for them (or for the whole array).
     int rc = setup_generic(p);
     if (rc != NDF_OK) return rc;
     if (tileable) {
       setup_tile(p);
-      if (boxcar_configure(p, smem_limit)) {
-        p.algo = Algo::kBoxcarTile;
-        p.scratch_bytes = ((size_t)p.tile.t.tiles + 1) * sizeof(unsigned int);
-        cudaError_t e = cudaMalloc(&p.d_scratch, p.scratch_bytes);
-        if (e != cudaSuccess) {
-          cudaGetLastError();
-          return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
-        }
-        return NDF_OK;
+      std::vector<Candidate> cands = plan_candidates_impl(p, smem_limit);
+      if (!cands.empty()) {
+        Candidate pick = cands.size() > 1 ? autotune_pick(p, cands, smem_limit) : cands[0];
+        return apply_candidate_impl(p, pick, smem_limit);
       }
     }
     p.algo = Algo::kBoxcarDirect;
@@ -601,6 +642,7 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
       e = launch_generic_moments(p, in, out, s);
       break;
     case Algo::kBoxcarTile:
+    case Algo::kBoxcarBand:
     case Algo::kBoxcarDirect:
       e = launch_boxcar(p, in, out, s);
       break;
@@ -608,6 +650,7 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
       e = launch_moments_slide(p, in, out, s);
       break;
     case Algo::kExtremaTile:
+    case Algo::kExtremaPasses:
       e = launch_extrema(p, in, out, s);
       break;
   }

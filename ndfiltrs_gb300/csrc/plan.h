@@ -96,6 +96,8 @@ enum class Algo {
   kBoxcarDirect,  // exact rolling mean, full-width direct sums
   kMomentsSlide,  // mean / var / std, sliding exact integer sums (boxes)
   kExtremaTile,   // separable min / max (van Herk / Gil-Werman) over boxes
+  kBoxcarBand,    // exact rolling mean, column sums sliding down bands
+  kExtremaPasses, // separable min / max, two transposing column passes
 };
 
 struct Plan {
@@ -146,6 +148,7 @@ struct Plan {
 
   // Kernel choice: measure candidates not in the autotune cache (batches).
   bool may_tune = false;
+  int ext_rows[2] = {0, 0};  // rows per block of the two extrema column passes
 };
 
 const char* algo_name(Algo a);
@@ -186,7 +189,9 @@ cudaError_t launch_moments_slide(const Plan& p, const void* in, void* out, cudaS
 bool moments_slide_configure(Plan& p, int smem_limit);
 cudaError_t launch_extrema(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool extrema_configure(Plan& p, int smem_limit);
+bool extrema_passes_configure(Plan& p, int smem_limit);
 bool boxcar_configure(Plan& p, int smem_limit);
+bool boxcar_band_configure(Plan& p, int smem_limit);
 
 // Shared-memory bytes a tile kernel needs for `t` (0 when it does not fit).
 size_t tile_select_smem(const Plan& p, const Tile& t);

@@ -28,6 +28,7 @@
 #include <string>
 #include <thread>
 #include <type_traits>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -1668,6 +1669,403 @@ int boxcar_separable(const Window& w, const uint64_t* size, const int64_t* origi
   return kOk;
 }
 
+// ---------------------------------------------------------------------------
+// Robust reductions: RobustReduction::finish (src/robust.rs:244-299) for the
+// MAD, sigma clipping, the mode and the biweight location / scale, with the
+// helpers of src/robust.rs:376-697 and src/location.rs:36-240.
+
+enum RobustKind {
+  kRobustPercentile = 0,
+  kRobustMad = 1,
+  kRobustMode = 2,
+  kRobustBiweightLocation = 3,
+  kRobustBiweightScale = 4,
+  kRobustSigmaMean = 5,
+  kRobustSigmaMedian = 6,
+  kRobustSigmaMode = 7,
+};
+enum ModeRule { kModeSex = 0, kModeMmm = 1, kModeIraf = 2 };
+
+struct RobustSpec {
+  int kind = kRobustPercentile;
+  Policy policy;           // percentile / MAD / mode / biweight
+  double parameter = 0.0;  // q, MAD scale or biweight c
+  double lower = 3.0, upper = 3.0;
+  int64_t maxiters = 5;    // < 0: until stable
+  int center = 1;          // 0 mean, 1 median
+  int spread = 0;          // 0 std, 1 MAD
+  int estimator = kModeSex;
+  bool modify_sample_size = false;
+  double pearson = 2.5;
+  uint64_t clip_min_count = 1;
+};
+
+// Phi^-1(0.75), src/robust.rs:11.
+constexpr double kNormalUpperQuartile = 0.6744897501960817;
+
+inline int total_cmp(double a, double b) {
+  const uint64_t ka = total_key(a), kb = total_key(b);
+  return ka < kb ? -1 : (ka > kb ? 1 : 0);
+}
+
+// 2^n by binary powering with a final reciprocal for negative n (the
+// powi of the reference's toolchain): exact unless 2^|n| overflows, when
+// the reciprocal is zero.
+double powi2(int n) {
+  unsigned int m = n < 0 ? (unsigned int)(-(long long)n) : (unsigned int)n;
+  double r = 1.0, a = 2.0;
+  while (m) {
+    if (m & 1) r *= a;
+    a *= a;
+    m >>= 1;
+  }
+  return n < 0 ? 1.0 / r : r;
+}
+
+struct Scaled {
+  double value;
+  int exponent;
+};
+
+// binary_parts, src/robust.rs:498-511 (positive finite values).
+std::pair<double, int> binary_parts(double value) {
+  const uint64_t b = bits64(value);
+  const int exponent = (int)((b >> 52) & 0x7ff);
+  const uint64_t fraction = b & ((1ull << 52) - 1);
+  if (exponent == 0) {
+    const int leading = 63 - __builtin_clzll(fraction);
+    return {(double)fraction / (double)(1ull << leading), leading - 1074};
+  }
+  return {from_bits64(fraction | (1023ull << 52)), exponent - 1023};
+}
+
+// absolute_deviation, src/robust.rs:438-466.
+Scaled absolute_deviation(double value, Scaled center) {
+  if (center.exponent == -1 && std::isfinite(value * 2.0)) {
+    const double difference = value * 2.0 - center.value;
+    if (std::isfinite(difference)) return {std::fabs(difference), -1};
+  }
+  const double midpoint = center.exponent == -1 ? center.value / 2.0 : center.value;
+  const double difference = value - midpoint;
+  if (std::isfinite(difference) || std::isinf(value)) return {std::fabs(difference), 0};
+  return {std::fabs(value / 2.0 - midpoint / 2.0), 1};
+}
+
+// compare_scaled, src/robust.rs:468-481.
+int compare_scaled(Scaled left, Scaled right) {
+  if (left.value == 0.0 || right.value == 0.0 || std::isinf(left.value) || std::isinf(right.value))
+    return total_cmp(left.value, right.value);
+  const auto [lv, le] = binary_parts(left.value);
+  const auto [rv, re] = binary_parts(right.value);
+  const int a = le + left.exponent, b = re + right.exponent;
+  if (a != b) return a < b ? -1 : 1;
+  return total_cmp(lv, rv);
+}
+
+// scaled_midpoint, src/robust.rs:483-496.
+Scaled scaled_midpoint(Scaled left, Scaled right) {
+  if (std::isinf(right.value) || right.value == 0.0) return right;
+  const auto [rv, re] = binary_parts(right.value);
+  const int exponent = re + right.exponent;
+  double lv = 0.0;
+  if (left.value != 0.0) {
+    const auto [v, le] = binary_parts(left.value);
+    lv = v * powi2(le + left.exponent - exponent);
+  }
+  return {lv + rv, exponent - 1};
+}
+
+// mad_parts, src/robust.rs:376-436: the median absolute deviation as a
+// scaled magnitude, merging the deviations on both sides of the median.
+Scaled mad_parts(const std::vector<double>& values) {
+  std::vector<double> s(values);
+  std::sort(s.begin(), s.end(), key_less);
+  const size_t n = s.size();
+  const double lower = s[(n - 1) / 2], upper = s[n / 2];
+  Scaled center;
+  if (!std::isfinite(lower) || !std::isfinite(upper))
+    center = {interpolate(lower, upper, 0.5), 0};
+  else if (std::isfinite(lower + upper))
+    center = {lower + upper, -1};
+  else
+    center = {lower / 2.0 + upper / 2.0, 0};
+  if (!std::isfinite(center.value)) return {kNaN64, 0};
+  size_t left = n / 2, right = left;
+  Scaled previous{0.0, 0}, selected = previous;
+  for (size_t step = 0; step <= n / 2; ++step) {
+    previous = selected;
+    const bool take_left =
+        left > 0 && (right == n || compare_scaled(absolute_deviation(s[left - 1], center),
+                                                  absolute_deviation(s[right], center)) <= 0);
+    if (take_left) {
+      --left;
+      selected = absolute_deviation(s[left], center);
+    } else {
+      selected = absolute_deviation(s[right], center);
+      ++right;
+    }
+  }
+  return n % 2 == 1 ? selected : scaled_midpoint(previous, selected);
+}
+
+// multiply_scaled, src/robust.rs:513-534.
+double multiply_scaled(Scaled value, double multiplier) {
+  if (!std::isfinite(value.value)) return value.value * multiplier;
+  if (value.value == 0.0 || multiplier == 0.0) return 0.0;
+  const auto [left, le] = binary_parts(value.value);
+  const auto [right, re] = binary_parts(multiplier);
+  const auto [mantissa, adjustment] = binary_parts(left * right);
+  const int exponent = le + re + adjustment + value.exponent;
+  if (exponent > 1023) return INFINITY;
+  if (exponent < -1075) return 0.0;
+  if (exponent >= -1022) return mantissa * from_bits64((uint64_t)(exponent + 1023) << 52);
+  const double scale = from_bits64((uint64_t)(exponent + 2045) << 52);
+  return (mantissa * 2.2250738585072014e-308) * scale;
+}
+
+// within_limit, src/robust.rs:536-559.
+bool within_limit(double value, double center, Scaled spread, double sigma) {
+  if (value == center) return true;
+  if (spread.value == 0.0 || sigma == 0.0) return false;
+  const double difference = value - center;
+  double distance;
+  int distance_exp;
+  if (std::isfinite(difference)) {
+    std::tie(distance, distance_exp) = binary_parts(std::fabs(difference));
+  } else {
+    std::tie(distance, distance_exp) = binary_parts(std::fabs(value / 2.0 - center / 2.0));
+    distance_exp += 1;
+  }
+  const auto [scale, scale_exp] = binary_parts(spread.value);
+  const auto [multiplier, multiplier_exp] = binary_parts(sigma);
+  const auto [limit, adjustment] = binary_parts(scale * multiplier);
+  const int limit_exp = scale_exp + multiplier_exp + adjustment + spread.exponent;
+  return distance_exp < limit_exp || (distance_exp == limit_exp && distance <= limit);
+}
+
+// finite_mean, src/robust.rs:572-592.
+double finite_mean(const std::vector<double>& values) {
+  Sum sum;
+  for (double v : values) sum.add(v);
+  const double total = sum.total();
+  if (std::isfinite(total)) return total / (double)values.size();
+  const uint64_t m = (uint64_t)(values.size() - 1);
+  const int exponent = (m == 0 ? 0 : 64 - __builtin_clzll(m)) + 1;
+  const double scale = powi2(exponent);
+  Sum scaled;
+  double lower = INFINITY, upper = -INFINITY;
+  for (double v : values) {
+    scaled.add(v / scale);
+    lower = std::fmin(lower, v);
+    upper = std::fmax(upper, v);
+  }
+  return clamp_f64(scaled.total() / ((double)values.size() / scale), lower, upper);
+}
+
+// location, src/robust.rs:561-570 (the median is the 50th percentile).
+double clip_location(const std::vector<double>& values, int center) {
+  if (center == 0) return finite_mean(values);
+  std::vector<double> copy(values);
+  return percentile(copy, 50.0);
+}
+
+// std_parts, src/robust.rs:594-630.
+Scaled std_parts(const std::vector<double>& values) {
+  const double reference = values[0];
+  bool halve = false;
+  for (double v : values) halve = halve || !std::isfinite(v - reference);
+  auto delta = [&](double v) { return halve ? v / 2.0 - reference / 2.0 : v - reference; };
+  double scale = 0.0;
+  for (double v : values) scale = std::fmax(scale, std::fabs(delta(v)));
+  if (scale == 0.0) return {0.0, 0};
+  Sum sum;
+  for (double v : values) sum.add(delta(v) / scale);
+  const double center = sum.total() / (double)values.size();
+  Sum squares;
+  for (double v : values) {
+    const double residual = delta(v) / scale - center;
+    squares.add(residual * residual);
+  }
+  const auto [mantissa, exponent] = binary_parts(scale);
+  return {mantissa * std::sqrt(squares.total() / (double)values.size()), exponent + (halve ? 1 : 0)};
+}
+
+// mode_from_moments / mode_estimate, src/location.rs:36-84.
+double mode_from_moments(double mean, double median, double std_dev, int estimator, double pearson) {
+  const double difference = median - mean;
+  const double pearson_mode = median + (pearson - 1.0) * difference;
+  if (estimator == kModeMmm) return pearson_mode;
+  if (estimator == kModeIraf) return mean < median ? mean : pearson_mode;
+  if (std_dev == 0.0) return mean;
+  if (std::fabs(difference) / std_dev >= 0.3) return median;
+  return pearson_mode;
+}
+
+double mode_estimate(std::vector<double>& values, int estimator, double pearson) {
+  if (values.empty()) return kNaN64;
+  const double mean = mean_valid(values.data(), values.size());
+  const double std_dev =
+      estimator == kModeSex ? dispersion_valid(values.data(), values.size(), 0, true) : kNaN64;
+  const double median = median_valid(values);
+  return mode_from_moments(mean, median, std_dev, estimator, pearson);
+}
+
+// standardize, src/location.rs:104-150. The reference's in-place median
+// leaves the samples in an order its selection routine does not publish;
+// the deviations here follow ascending total order, and the biweight sums
+// below run in that order.
+struct Standardized {
+  int state = 0;  // 0 empty, 1 zero MAD, 2 spread
+  double median = 0.0, width = 0.0, factor = 1.0;
+  std::vector<double> u;
+};
+
+Standardized standardize(std::vector<double>& values, double c) {
+  Standardized out;
+  const size_t n = values.size();
+  if (n == 0) return out;
+  std::sort(values.begin(), values.end(), key_less);
+  out.median = median_valid(values);
+  std::sort(values.begin(), values.end(), key_less);
+  std::vector<double> dev(n);
+  double factor = 1.0;
+  bool overflow = false;
+  for (size_t i = 0; i < n; ++i) {
+    dev[i] = values[i] - out.median;
+    overflow = overflow || !std::isfinite(dev[i]);
+  }
+  if (overflow) {
+    factor = 2.0;
+    for (size_t i = 0; i < n; ++i) dev[i] = values[i] / 2.0 - out.median / 2.0;
+  }
+  std::vector<double> absolute(n);
+  for (size_t i = 0; i < n; ++i) absolute[i] = std::fabs(dev[i]);
+  double mad = median_valid(absolute);
+  if (mad == 0.0) {
+    out.state = 1;
+    return out;
+  }
+  double extra = 1.0;
+  while (!std::isfinite(c * mad)) {
+    mad /= 2.0;
+    extra *= 2.0;
+  }
+  const double width = c * mad;
+  for (size_t i = 0; i < n; ++i) dev[i] = dev[i] / extra / width;
+  out.state = 2;
+  out.width = width;
+  out.factor = factor * extra;
+  out.u = std::move(dev);
+  return out;
+}
+
+// biweight_location, src/location.rs:152-183.
+double biweight_location(std::vector<double>& values, double c) {
+  Standardized st = standardize(values, c);
+  if (st.state == 0) return kNaN64;
+  if (st.state == 1) return st.median;
+  Sum weighted, weights;
+  for (double u : st.u) {
+    if (!(std::fabs(u) < 1.0)) continue;
+    const double weight = (1.0 - u * u) * (1.0 - u * u);
+    weighted.add(u * weight);
+    weights.add(weight);
+  }
+  const double correction = st.width * (weighted.total() / weights.total());
+  const double unscaled = correction * st.factor;
+  if (std::isfinite(unscaled)) return st.median + unscaled;
+  return (st.median / st.factor + correction) * st.factor;
+}
+
+// biweight_scale, src/location.rs:185-240.
+double biweight_scale(std::vector<double>& values, double c, bool modify_sample_size) {
+  const size_t total = values.size();
+  Standardized st = standardize(values, c);
+  if (st.state == 0) return kNaN64;
+  if (st.state == 1) return 0.0;
+  Sum numerator, denominator;
+  size_t kept = 0;
+  for (double u : st.u) {
+    if (!(std::fabs(u) < 1.0)) continue;
+    const double u2 = u * u;
+    const double taper = (1.0 - u2) * (1.0 - u2);
+    numerator.add(u2 * taper * taper);
+    denominator.add((1.0 - u2) * (1.0 - 5.0 * u2));
+    ++kept;
+  }
+  const double count = (double)(modify_sample_size ? kept : total);
+  const double ratio = std::sqrt(count * numerator.total()) / std::fabs(denominator.total());
+  return st.width * ratio * st.factor;
+}
+
+// clipped, src/robust.rs:632-689: values are the finite samples in tap order.
+double clipped(std::vector<double>& values, const RobustSpec& spec) {
+  int64_t iteration = 0;
+  while (values.size() >= spec.clip_min_count && (spec.maxiters < 0 || iteration < spec.maxiters)) {
+    const double center = clip_location(values, spec.center);
+    Scaled spread;
+    if (spec.spread == 1) {
+      const Scaled deviation = mad_parts(values);
+      if (deviation.value > 0.0 && std::isfinite(deviation.value)) {
+        const auto [mantissa, exponent] = binary_parts(deviation.value);
+        spread = {mantissa / kNormalUpperQuartile, exponent + deviation.exponent};
+      } else {
+        spread = deviation;
+      }
+    } else {
+      spread = std_parts(values);
+    }
+    const size_t previous = values.size();
+    size_t write = 0;
+    for (size_t read = 0; read < values.size(); ++read) {
+      const double v = values[read];
+      if (within_limit(v, center, spread, v < center ? spec.lower : spec.upper)) values[write++] = v;
+    }
+    values.resize(write);
+    ++iteration;
+    if (values.size() == previous) break;
+  }
+  if (values.size() < spec.clip_min_count) return kNaN64;
+  if (spec.kind == kRobustSigmaMean) return clip_location(values, 0);
+  if (spec.kind == kRobustSigmaMedian) return clip_location(values, 1);
+  return mode_estimate(values, spec.estimator, spec.pearson);
+}
+
+// RobustReduction::finish, src/robust.rs:244-299.
+double robust_finish(const RobustSpec& spec, std::vector<double>& values) {
+  if (spec.kind >= kRobustSigmaMean) {
+    size_t write = 0;
+    for (size_t read = 0; read < values.size(); ++read)
+      if (std::isfinite(values[read])) values[write++] = values[read];
+    values.resize(write);
+    return clipped(values, spec);
+  }
+  if (!spec.policy.omit) {
+    for (double v : values)
+      if (std::isnan(v)) return kNaN64;
+  } else {
+    size_t write = 0;
+    for (size_t read = 0; read < values.size(); ++read)
+      if (retained(values[read], spec.policy)) values[write++] = values[read];
+    values.resize(write);
+    if (values.size() < spec.policy.min_count) return kNaN64;
+  }
+  if (values.empty()) return kNaN64;
+  switch (spec.kind) {
+    case kRobustPercentile:
+      return percentile(values, spec.parameter);
+    case kRobustMad:
+      return multiply_scaled(mad_parts(values), spec.parameter);
+    default:
+      break;
+  }
+  for (double v : values)
+    if (std::isinf(v)) return kNaN64;
+  if (spec.kind == kRobustMode) return mode_estimate(values, spec.estimator, spec.pearson);
+  if (spec.kind == kRobustBiweightLocation) return biweight_location(values, spec.parameter);
+  return biweight_scale(values, spec.parameter, spec.modify_sample_size);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1827,6 +2225,72 @@ int ndfo_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* 
                 double q, int32_t threads) {
   return ndfo_filter_ex(dtype, rank, shape, input, output, size, footprint, origin, modes, cval,
                         kind, omit_nan, ignore_inf, min_count, parameter, q, threads, 0);
+}
+
+// One robust reduction of `n` float64 samples (the pinned literal tests).
+// `kind` is a RobustKind; `maxiters` < 0 clips until stable.
+double ndfo_robust_values(int32_t kind, const double* values, uint64_t n, int32_t omit_nan,
+                          int32_t ignore_inf, uint64_t min_count, double parameter, double lower,
+                          double upper, int64_t maxiters, int32_t center, int32_t spread,
+                          int32_t estimator, int32_t modify_sample_size, double pearson) {
+  RobustSpec spec;
+  spec.kind = kind;
+  spec.policy.omit = omit_nan != 0;
+  spec.policy.ignore_inf = ignore_inf != 0;
+  spec.policy.min_count = min_count;
+  spec.parameter = parameter;
+  spec.lower = lower;
+  spec.upper = upper;
+  spec.maxiters = maxiters;
+  spec.center = center;
+  spec.spread = spread;
+  spec.estimator = estimator;
+  spec.modify_sample_size = modify_sample_size != 0;
+  spec.pearson = pearson;
+  spec.clip_min_count = min_count;
+  std::vector<double> v(values, values + n);
+  return robust_finish(spec, v);
+}
+
+// robust_into, src/robust.rs:725-785: every window gathered in tap order as
+// float64, reduced, and cast once (NaN as the canonical NaN).
+int ndfo_robust_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const void* input,
+                       void* output, const uint64_t* size, const uint8_t* footprint,
+                       const int64_t* origin, const int32_t* modes, double cval, int32_t kind,
+                       int32_t omit_nan, int32_t ignore_inf, uint64_t min_count, double parameter,
+                       double lower, double upper, int64_t maxiters, int32_t center, int32_t spread,
+                       int32_t estimator, int32_t modify_sample_size, double pearson,
+                       int32_t threads) {
+  Window w;
+  int rc = window_new(rank, shape, size, footprint, origin, modes, &w);
+  if (rc) return rc;
+  if (min_count == 0 || min_count > w.count)
+    return fail(kInvalid, "min_count must be between one and the number of window elements");
+  const size_t n = w.out_len;
+  if (n == 0) return kOk;
+  if (threads < 1) threads = 1;
+  const bool f32 = dtype == 0;
+  if (f32) cval = (double)(float)cval;
+  auto run = [&](auto tag) {
+    using T = decltype(tag);
+    run_parallel(n, threads, [&](size_t s, size_t e) {
+      std::vector<int64_t> index(w.rank);
+      std::vector<double> values;
+      for (size_t c = s; c < e; ++c) {
+        values.clear();
+        visit(w, (const T*)input, c, cval, index.data(), [&](double v) { values.push_back(v); });
+        const double r = ndfo_robust_values(kind, values.data(), values.size(), omit_nan, ignore_inf,
+                                            min_count, parameter, lower, upper, maxiters, center,
+                                            spread, estimator, modify_sample_size, pearson);
+        ((T*)output)[c] = cast_out<T>(r);
+      }
+    });
+  };
+  if (f32)
+    run(float());
+  else
+    run(double());
+  return kOk;
 }
 
 // Exact (double-double) mean/var/std of every window, rounded to float64,

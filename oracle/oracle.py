@@ -115,6 +115,18 @@ def lib() -> ctypes.CDLL:
             ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32,
         ]
         handle.ndfo_exact_moments.restype = ctypes.c_int
+        robust_args = [
+            ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+            ctypes.c_double, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+            ctypes.c_int32, ctypes.c_double,
+        ]
+        handle.ndfo_robust_values.argtypes = [ctypes.c_int32, dptr, ctypes.c_uint64] + robust_args
+        handle.ndfo_robust_values.restype = ctypes.c_double
+        handle.ndfo_robust_filter.argtypes = [
+            ctypes.c_int32, ctypes.c_int32, u64p, vp, vp, u64p, u8p, i64p, i32p,
+            ctypes.c_double, ctypes.c_int32,
+        ] + robust_args + [ctypes.c_int32]
+        handle.ndfo_robust_filter.restype = ctypes.c_int
         _lib = handle
     return _lib
 
@@ -209,6 +221,64 @@ def window_filter(
         int(threads or default_threads()),
         int(bool(direct)),
     )
+    if rc != 0:
+        raise OracleError(rc, lib().ndfo_last_error().decode())
+    return out
+
+
+ROBUST_KINDS = {
+    "percentile": 0,
+    "mad": 1,
+    "mode": 2,
+    "biweight_location": 3,
+    "biweight_scale": 4,
+    "sigma_mean": 5,
+    "sigma_median": 6,
+    "sigma_mode": 7,
+}
+ESTIMATORS = {"sex": 0, "mmm": 1, "iraf": 2}
+
+
+def _robust_args(omit_nan, ignore_inf, min_count, parameter, sigma_lower, sigma_upper, maxiters,
+                 center, spread, estimator, modify_sample_size, pearson):
+    return (
+        int(bool(omit_nan)), int(bool(ignore_inf)), int(min_count), float(parameter),
+        float(sigma_lower), float(sigma_upper), -1 if maxiters is None else int(maxiters),
+        {"mean": 0, "median": 1}[center], {"std": 0, "mad": 1}[spread], ESTIMATORS[estimator],
+        int(bool(modify_sample_size)), float(pearson),
+    )
+
+
+def robust_values(kind: str, values, *, omit_nan=False, ignore_inf=False, min_count=1,
+                  parameter=0.0, sigma_lower=3.0, sigma_upper=3.0, maxiters=5, center="median",
+                  spread="std", estimator="sex", modify_sample_size=False, pearson=2.5) -> float:
+    """One robust reduction of a float64 sample (RobustReduction::finish)."""
+    data = np.ascontiguousarray(values, dtype=np.float64)
+    return lib().ndfo_robust_values(
+        ROBUST_KINDS[kind], data.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), data.size,
+        *_robust_args(omit_nan, ignore_inf, min_count, parameter, sigma_lower, sigma_upper, maxiters,
+                      center, spread, estimator, modify_sample_size, pearson))
+
+
+def robust_filter(array: np.ndarray, kind: str, size=3, *, footprint=None, origin=0, mode="reflect",
+                  cval=0.0, omit_nan=False, ignore_inf=False, min_count=1, parameter=0.0,
+                  sigma_lower=3.0, sigma_upper=3.0, maxiters=5, center="median", spread="std",
+                  estimator="sex", modify_sample_size=False, pearson=2.5,
+                  threads: int | None = None) -> np.ndarray:
+    """robust_into over a C-contiguous array (src/robust.rs:725-785)."""
+    array = np.ascontiguousarray(array)
+    if array.dtype not in (np.float32, np.float64):
+        raise TypeError("oracle input must be float32 or float64")
+    shape, sz, fp, org, modes = _geometry(array, size, footprint, origin, mode)
+    out = np.empty_like(array)
+    fp_ptr = fp.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) if fp is not None else None
+    rc = lib().ndfo_robust_filter(
+        0 if array.dtype == np.float32 else 1, array.ndim, shape,
+        array.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p), sz, fp_ptr,
+        org, modes, float(cval), ROBUST_KINDS[kind],
+        *_robust_args(omit_nan, ignore_inf, min_count, parameter, sigma_lower, sigma_upper, maxiters,
+                      center, spread, estimator, modify_sample_size, pearson),
+        int(threads or default_threads()))
     if rc != 0:
         raise OracleError(rc, lib().ndfo_last_error().decode())
     return out

@@ -39,9 +39,22 @@ def _values(shape, dtype, seed, wide=False):
     return values
 
 
+KERNELS = {"band": "boxcar_band", "boxcar": "boxcar_tile"}
+
+
+@pytest.fixture(params=sorted(KERNELS))
+def kernel(request, gpu):
+    """Pin the band or the tiled kernel for the test."""
+    from ndfiltrs_gb300 import _core
+
+    _core.pin_kernel(request.param)
+    yield KERNELS[request.param]
+    _core.pin_kernel(None)
+
+
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("mode", MODES)
-def test_boxcar_matches_oracle(gpu, oracle, dtype, mode) -> None:
+def test_boxcar_matches_oracle(gpu, oracle, kernel, dtype, mode) -> None:
     for shape, size, origin in (((70, 90), (5, 7), (1, -2)), ((40, 33), (9, 4), (-4, 1)),
                                 ((300,), (11,), (3,)), ((1, 500), (1, 31), (0, 0)),
                                 ((6, 9, 8), (3, 2, 5), (0, 0, -1))):
@@ -56,24 +69,43 @@ def test_boxcar_matches_oracle(gpu, oracle, dtype, mode) -> None:
                                                 min_count=min_count)
                 np.testing.assert_array_equal(bits(actual), bits(expected),
                                               err_msg=str((shape, size, omit, cval, algorithm)))
-                assert algorithm == ("boxcar_direct" if len(shape) == 3 else "boxcar_tile")
+                assert algorithm == ("boxcar_direct" if len(shape) == 3 else kernel)
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-def test_boxcar_wide_ranges_use_the_full_width_kernel(gpu, oracle, dtype) -> None:
-    """Values from subnormals to near the overflow threshold in one tile:
-    the tiled kernel hands those tiles to the full-width kernel; results stay
-    exact. A second array mixes narrow and wide tiles."""
+def test_boxcar_wide_ranges_use_the_full_width_kernel(gpu, oracle, kernel, dtype) -> None:
+    """Values from subnormals to near the overflow threshold in one tile or
+    band: those go to a wider pass (bands) and then to the full-width
+    kernel; results stay exact. A second array mixes narrow and wide
+    regions."""
     wide = _values((64, 80), dtype, seed=3, wide=True)
-    mixed = _values((130, 150), dtype, seed=4)
-    mixed[100:, 120:] = _values((30, 30), dtype, seed=5, wide=True)
+    mixed = _values((130, 600), dtype, seed=4)
+    mixed[100:, 520:] = _values((30, 80), dtype, seed=5, wide=True)
     for values in (wide, mixed):
         for omit in (False, True):
             actual, algorithm = _gpu(values, (7, 5), (0, 0), ["reflect", "wrap"], 0.0, omit, False, 1)
             expected = oracle.window_filter(values, "mean_rolling", (7, 5), mode=("reflect", "wrap"),
                                             omit_nan=omit)
-            assert algorithm == "boxcar_tile"
+            assert algorithm == kernel
             np.testing.assert_array_equal(bits(actual), bits(expected))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_boxcar_wide_windows(gpu, oracle, kernel, dtype) -> None:
+    """Windows of 33 x 65 and 129 x 129 over images a few bands wide and
+    tall, every mode, with the band height cut short at the bottom."""
+    values = _values((700, 611), dtype, seed=9)
+    for size, origin, mode in (((33, 65), (-3, 7), "reflect"), ((129, 129), (0, 0), "nearest"),
+                               ((65, 17), (5, -8), "wrap"), ((17, 129), (0, 60), "constant"),
+                               ((129, 3), (-64, 0), "mirror")):
+        for omit, min_count in ((False, 1), (True, 100)):
+            actual, algorithm = _gpu(values, size, origin, [mode] * 2, -1.5, omit, True, min_count)
+            expected = oracle.window_filter(values, "mean_rolling", size, origin=origin, mode=mode,
+                                            cval=-1.5, omit_nan=omit, ignore_inf=True,
+                                            min_count=min_count)
+            # A tile too large for shared memory leaves the band kernel.
+            assert algorithm in (kernel, "boxcar_band")
+            np.testing.assert_array_equal(bits(actual), bits(expected), err_msg=str((size, mode, omit)))
 
 
 def test_boxcar_rounds_once_and_public_api(gpu, oracle) -> None:

@@ -389,26 +389,36 @@ def test_sliding_moments_against_exact_oracle(gpu, oracle, dtype) -> None:
                         assert np.all(close), context
 
 
+@pytest.mark.parametrize("family,algorithm", [("passes", "extrema_passes"), ("extrema", "extrema_tile")])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-def test_separable_extrema(gpu, oracle, dtype) -> None:
-    """Rectangular minima / maxima wider than 5 x 5 run the separable
-    (van Herk / Gil-Werman) kernel: bit-identical to direct selection under
-    every mode, origin and policy, with signed zeros, infinities and NaNs."""
+def test_separable_extrema(gpu, oracle, dtype, family, algorithm) -> None:
+    """Rectangular minima / maxima run the separable (van Herk / Gil-Werman)
+    kernels, the two column passes and the one-tile form: bit-identical to
+    direct selection under every mode, origin and policy, with signed zeros,
+    infinities, NaNs and NaN / infinite cval, on arrays that are not whole
+    numbers of strips and blocks."""
     from ndfiltrs_gb300 import _core
 
     values = _special_values((97, 130), dtype, seed=13, fraction=0.06)
+    tall = _special_values((301, 45), dtype, seed=15, fraction=0.02)
     line = _special_values((900,), dtype, seed=14, fraction=0.06)
-    for array, size, origin in ((values, (9, 9), (1, -2)), (values, (33, 17), (-5, 3)),
-                                (values, (65, 65), (0, 0)), (values, (1, 31), (0, 7)),
-                                (line, (41,), (-10,))):
-        for mode in MODES:
-            for kind in ("min", "max"):
-                for omit, ignore_inf, min_count in ((False, False, 1), (True, False, 1), (True, True, 9)):
-                    args = (kind, array, size, None, origin, (mode,) * array.ndim, -0.5, omit, ignore_inf,
-                            min_count)
-                    with _core.Plan(array.shape, dtype, kind, size, origin=origin, mode=[mode] * array.ndim,
-                                    cval=-0.5, omit_nan=omit, ignore_inf=ignore_inf,
-                                    min_count=min_count) as plan:
-                        assert plan.algorithm == "extrema_tile"
-                        actual = plan.run_host(array)
-                    _assert_bits(actual, _oracle(oracle, *args), (size, mode, kind, omit, ignore_inf))
+    _core.pin_kernel(family)
+    try:
+        for array, size, origin in ((values, (9, 9), (1, -2)), (values, (33, 17), (-5, 3)),
+                                    (values, (65, 65), (0, 0)), (values, (1, 31), (0, 7)),
+                                    (tall, (129, 3), (60, -1)), (values, (3, 3), (0, 1)),
+                                    (line, (41,), (-10,))):
+            for mode in MODES:
+                for kind in ("min", "max"):
+                    for omit, ignore_inf, min_count, cval in ((False, False, 1, -0.5), (True, False, 1, np.nan),
+                                                              (True, True, 9, np.inf), (False, False, 1, np.nan)):
+                        args = (kind, array, size, None, origin, (mode,) * array.ndim, cval, omit, ignore_inf,
+                                min_count)
+                        with _core.Plan(array.shape, dtype, kind, size, origin=origin,
+                                        mode=[mode] * array.ndim, cval=cval, omit_nan=omit,
+                                        ignore_inf=ignore_inf, min_count=min_count) as plan:
+                            assert plan.algorithm == algorithm
+                            actual = plan.run_host(array)
+                        _assert_bits(actual, _oracle(oracle, *args), (size, mode, kind, omit, ignore_inf, cval))
+    finally:
+        _core.pin_kernel(None)
