@@ -125,10 +125,11 @@ class Workload:
     """One benchmark configuration: an image generator and the filter."""
 
     def __init__(self, gen, kind, size, mode, omit=True, ignore_inf=False, min_count=1, parameter=0,
-                 q=50.0, footprint=None, origin=None):
+                 q=50.0, footprint=None, origin=None, robust=None):
         self.gen, self.kind, self.size, self.mode = gen, kind, size, mode
         self.omit, self.ignore_inf, self.min_count, self.parameter = omit, ignore_inf, min_count, parameter
         self.q, self.footprint_fn, self.origin = q, footprint, origin
+        self.robust = robust  # estimator options of the robust kinds
 
     def footprint(self):
         return self.footprint_fn() if self.footprint_fn is not None else None
@@ -175,7 +176,18 @@ WORKLOADS = {
     "nanmean_boxcar_129x129_8192_f32": Workload(lambda: sky_image(8192), "mean_rolling", (129, 129), "nearest"),
     "nanmean_boxcar_31x31_4096_f64": Workload(lambda: precision_image(4096, dtype=np.float64), "mean_rolling",
                                               (31, 31), "reflect", ignore_inf=True, min_count=5),
+    # Robust family (per-window float64 estimators).
+    "nanmad_5x5_4096_f32": Workload(lambda: robust_image(4096), "mad", (5, 5), "reflect",
+                                    robust=dict(parameter=1.0)),
+    "sigma_clip_mode_7x7_2048_f32": Workload(lambda: robust_image(2048), "sigma_mode", (7, 7), "reflect",
+                                             robust=dict(sigma_lower=3.0, sigma_upper=3.0, maxiters=None,
+                                                         center="median", spread="std", estimator="sex",
+                                                         pearson=2.5)),
+    "biweight_location_7x7_2048_f32": Workload(lambda: robust_image(2048), "biweight_location", (7, 7),
+                                               "reflect", robust=dict(parameter=6.0)),
 }
+ROBUST_KINDS = ("mad", "mode", "biweight_location", "biweight_scale", "sigma_mean", "sigma_median",
+                "sigma_mode")
 DEFAULT_WORKLOAD = "nanmedian_sortnet_5x5_4096_f32"
 
 # DRAM bytes (read + write) per launch of the workload's kernel, from one ncu
@@ -384,6 +396,12 @@ def cpu_baseline(image: np.ndarray, spec, budget_s: float = 3.0, threads: int | 
 
 
 def oracle_filter(oracle, spec, array, threads=None):
+    if spec.kind in ROBUST_KINDS:
+        clip = spec.kind.startswith("sigma")
+        return oracle.robust_filter(array, spec.kind, spec.window(), footprint=spec.footprint(),
+                                    origin=spec.origin if spec.origin is not None else 0, mode=spec.mode,
+                                    omit_nan=spec.omit or clip, ignore_inf=spec.ignore_inf or clip,
+                                    min_count=spec.min_count, threads=threads, **(spec.robust or {}))
     return oracle.window_filter(array, spec.kind, spec.window(), footprint=spec.footprint(),
                                 origin=spec.origin if spec.origin is not None else 0, mode=spec.mode, omit_nan=spec.omit,
                                 ignore_inf=spec.ignore_inf, min_count=spec.min_count,
@@ -690,7 +708,7 @@ def main() -> None:
         return nf.Plan(shape_, image.dtype, kind, spec.window(), footprint=spec.footprint(),
                        origin=spec.origin, mode=[mode] * image.ndim, omit_nan=spec.omit,
                        ignore_inf=spec.ignore_inf, min_count=spec.min_count, parameter=spec.parameter,
-                       percentile=spec.q)
+                       percentile=spec.q, robust=spec.robust)
 
     plan = make_plan(shape)
     device = torch.device("cuda", local_rank)

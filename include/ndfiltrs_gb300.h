@@ -64,6 +64,26 @@ extern "C" {
 #define NDF_KIND_RANK 9
 #define NDF_KIND_RANK_HISTOGRAM 10
 #define NDF_KIND_PERCENTILE 11
+/* The other robust kinds of src/pyapi/robust.rs:117-154 ("mad", "mode",
+ * "biweight_location", "biweight_scale", "sigma_mean", "sigma_median",
+ * "sigma_mode"); their parameters travel in ndf_robust_params. */
+#define NDF_KIND_MAD 12
+#define NDF_KIND_MODE 13
+#define NDF_KIND_BIWEIGHT_LOCATION 14
+#define NDF_KIND_BIWEIGHT_SCALE 15
+#define NDF_KIND_SIGMA_MEAN 16
+#define NDF_KIND_SIGMA_MEDIAN 17
+#define NDF_KIND_SIGMA_MODE 18
+
+/* ClipCenter, ClipSpread (src/robust.rs:16-35) and ModeEstimator
+ * (src/location.rs:13-25). */
+#define NDF_CLIP_CENTER_MEAN 0
+#define NDF_CLIP_CENTER_MEDIAN 1
+#define NDF_CLIP_SPREAD_STD 0
+#define NDF_CLIP_SPREAD_MAD 1
+#define NDF_MODE_ESTIMATOR_SEX 0
+#define NDF_MODE_ESTIMATOR_MMM 1
+#define NDF_MODE_ESTIMATOR_IRAF 2
 
 /* Boundary modes, src/boundary.rs:16-27. */
 #define NDF_MODE_REFLECT 0
@@ -90,15 +110,23 @@ int ndf_window_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim
                       int32_t ignore_inf, uint64_t min_count, uint64_t parameter);
 
 /* Replaces `_core.robust_filter(array, size, footprint, origin, mode, cval,
- * kind, parameter, omit_nan, ignore_inf, min_count, ...)` for
- * kind = "percentile", src/pyapi/robust.rs:78-171 (plan:
- * src/robust_plan.rs:55-67, run: src/robust.rs:765-785). `parameter` is the
- * percentile q in [0, 100]. Other robust kinds return NDF_ERR_UNSUPPORTED. */
+ * kind, parameter, omit_nan, ignore_inf, min_count, sigma_lower,
+ * sigma_upper, maxiters, center, spread, estimator, modify_sample_size,
+ * pearson)`, src/pyapi/robust.rs:78-171 (plan: src/robust_plan.rs:55-67,
+ * run: src/robust.rs:725-785). `kind` is one of "percentile", "mad", "mode",
+ * "biweight_location", "biweight_scale", "sigma_mean", "sigma_median",
+ * "sigma_mode"; `parameter` is the percentile q, the MAD scale or the
+ * biweight c; `maxiters` < 0 stands for None (clip until stable); `center`
+ * is "mean" or "median", `spread` "std" or "mad", `estimator` "sex", "mmm"
+ * or "iraf". */
 int ndf_robust_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim,
                       const uint64_t* shape, const uint64_t* size, const uint8_t* footprint,
                       const int64_t* origin, const char* const* modes, double cval,
                       const char* kind, double parameter, int32_t omit_nan,
-                      int32_t ignore_inf, uint64_t min_count);
+                      int32_t ignore_inf, uint64_t min_count, double sigma_lower,
+                      double sigma_upper, int64_t maxiters, const char* center,
+                      const char* spread, const char* estimator, int32_t modify_sample_size,
+                      double pearson);
 
 /* Replaces `_core.get_num_threads()`, src/pyapi/filter.rs:378-380. Returns
  * the number of streaming multiprocessors of the current device (the
@@ -113,6 +141,20 @@ const char* ndf_last_error(void);
  * to any number of arrays of its shape. */
 
 typedef struct ndf_plan ndf_plan;
+
+/* Parameters of the robust kinds other than the percentile (RobustReduction
+ * and ClipConfig, src/robust.rs:52-185). */
+typedef struct ndf_robust_params {
+  double parameter;           /* MAD scale (>= 0) or biweight c (> 0) */
+  double sigma_lower;         /* clipping multipliers (>= 0) */
+  double sigma_upper;
+  int64_t maxiters;           /* clipping passes; < 0: until stable */
+  int32_t center;             /* NDF_CLIP_CENTER_* */
+  int32_t spread;             /* NDF_CLIP_SPREAD_* */
+  int32_t estimator;          /* NDF_MODE_ESTIMATOR_* */
+  int32_t modify_sample_size; /* biweight scale: count only |u| < 1 */
+  double pearson;             /* mode rule factor (>= 1) */
+} ndf_robust_params;
 
 typedef struct ndf_filter_desc {
   int32_t dtype;             /* NDF_FLOAT32 / NDF_FLOAT64 */
@@ -130,6 +172,7 @@ typedef struct ndf_filter_desc {
   uint64_t parameter;        /* rank or ddof */
   double percentile;         /* q for NDF_KIND_PERCENTILE */
   int32_t moments;           /* NDF_MOMENTS_* for mean/var/std */
+  const ndf_robust_params* robust; /* NDF_KIND_MAD .. NDF_KIND_SIGMA_MODE; else NULL */
 } ndf_filter_desc;
 
 int ndf_plan_create(const ndf_filter_desc* desc, ndf_plan** plan);

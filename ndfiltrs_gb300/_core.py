@@ -56,9 +56,35 @@ KINDS = {
     "rank": 9,
     "rank_histogram": 10,
     "percentile": 11,
+    "mad": 12,
+    "mode": 13,
+    "biweight_location": 14,
+    "biweight_scale": 15,
+    "sigma_mean": 16,
+    "sigma_median": 17,
+    "sigma_mode": 18,
 }
+ROBUST_KINDS = ("mad", "mode", "biweight_location", "biweight_scale", "sigma_mean", "sigma_median",
+                "sigma_mode")
+CENTERS = {"mean": 0, "median": 1}
+SPREADS = {"std": 0, "mad": 1}
+ESTIMATORS = {"sex": 0, "mmm": 1, "iraf": 2}
 MODES = {"reflect": 0, "constant": 1, "nearest": 2, "mirror": 3, "wrap": 4}
 MOMENTS = {"fp32c": 0, "fp64": 1}
+
+
+class RobustParams(ctypes.Structure):
+    _fields_ = [
+        ("parameter", ctypes.c_double),
+        ("sigma_lower", ctypes.c_double),
+        ("sigma_upper", ctypes.c_double),
+        ("maxiters", ctypes.c_int64),
+        ("center", ctypes.c_int32),
+        ("spread", ctypes.c_int32),
+        ("estimator", ctypes.c_int32),
+        ("modify_sample_size", ctypes.c_int32),
+        ("pearson", ctypes.c_double),
+    ]
 
 
 class FilterDesc(ctypes.Structure):
@@ -80,6 +106,7 @@ class FilterDesc(ctypes.Structure):
         ("parameter", ctypes.c_uint64),
         ("percentile", ctypes.c_double),
         ("moments", ctypes.c_int32),
+        ("robust", ctypes.POINTER(RobustParams)),
     ]
 
 
@@ -209,6 +236,7 @@ class Plan:
         parameter: int = 0,
         percentile: float = 50.0,
         moments: str | None = None,
+        robust: dict | None = None,
     ) -> None:
         lib, _ = _load()
         shape = tuple(int(v) for v in shape)
@@ -263,7 +291,24 @@ class Plan:
             int(parameter),
             float(percentile),
             MOMENTS[moments],
+            None,
         )
+        if kind in ROBUST_KINDS:
+            options = dict(robust or {})
+            maxiters = options.get("maxiters", 5)
+            params = RobustParams(
+                float(options.get("parameter", 0.0)),
+                float(options.get("sigma_lower", 3.0)),
+                float(options.get("sigma_upper", 3.0)),
+                -1 if maxiters is None else int(maxiters),
+                CENTERS[options.get("center", "median")],
+                SPREADS[options.get("spread", "std")],
+                ESTIMATORS[options.get("estimator", "sex")],
+                int(bool(options.get("modify_sample_size", False))),
+                float(options.get("pearson", 2.5)),
+            )
+            self._keep.append(params)
+            desc.robust = ctypes.pointer(params)
         handle = ctypes.c_void_p()
         _check(lib.ndf_plan_create(ctypes.byref(desc), ctypes.byref(handle)), lib)
         self._handle = handle
@@ -461,17 +506,6 @@ def window_filter(
         return plan.run_host(array)
 
 
-_ROBUST_OUT_OF_SCOPE = (
-    "mad",
-    "mode",
-    "biweight_location",
-    "biweight_scale",
-    "sigma_mean",
-    "sigma_median",
-    "sigma_mode",
-)
-
-
 def robust_filter(
     array,
     size,
@@ -493,34 +527,44 @@ def robust_filter(
     modify_sample_size=False,
     pearson=2.5,
 ):
-    """Apply one robust window statistic (``_core.robust_filter``).
-
-    Only ``kind="percentile"`` runs on this library; the other robust kinds
-    of the reference (MAD, sigma clipping, mode, biweight) raise
-    NotImplementedError.
-    """
-    if kind in _ROBUST_OUT_OF_SCOPE:
-        raise NotImplementedError(f"robust kind {kind!r} is outside this library's scope")
-    if kind != "percentile":
+    """Apply one robust window statistic (``_core.robust_filter``,
+    src/pyapi/robust.rs:78-171): the percentile, the MAD, iterative sigma
+    clipping (``sigma_mean`` / ``sigma_median`` / ``sigma_mode``), the mode
+    estimators and the biweight location / scale."""
+    clip = kind in ("sigma_mean", "sigma_median", "sigma_mode")
+    if kind not in ("percentile",) + ROBUST_KINDS:
         raise ValueError("unsupported robust filter kind")
-    if not omit_nan and (ignore_inf or min_count != 1):
+    if not clip and not omit_nan and (ignore_inf or min_count != 1):
         raise ValueError("ignore_inf and min_count require NaN omission")
+    if kind in ("mode", "sigma_mode") and estimator not in ESTIMATORS:
+        raise ValueError("mode estimator must be 'sex', 'mmm', or 'iraf'")
+    if clip:
+        if center not in CENTERS:
+            raise ValueError("center must be 'mean' or 'median'")
+        if spread not in SPREADS:
+            raise ValueError("spread must be 'std' or 'mad'")
     array = _typed_array(array)
     if not array.flags.c_contiguous or not array.flags.aligned:
         raise ValueError("native input must be aligned and C-contiguous")
+    options = dict(parameter=parameter, sigma_lower=sigma_lower, sigma_upper=sigma_upper,
+                   maxiters=maxiters, center=center if clip else "median",
+                   spread=spread if clip else "std",
+                   estimator=estimator if kind in ("mode", "sigma_mode") else "sex",
+                   modify_sample_size=modify_sample_size, pearson=pearson)
     with Plan(
         array.shape,
         array.dtype,
-        "percentile",
+        kind,
         size,
         footprint=footprint,
         origin=origin,
         mode=mode,
         cval=float(cval),
-        omit_nan=omit_nan,
-        ignore_inf=ignore_inf,
+        omit_nan=True if clip else omit_nan,
+        ignore_inf=True if clip else ignore_inf,
         min_count=min_count,
         percentile=float(parameter),
+        robust=options,
     ) as plan:
         return plan.run_host(array)
 

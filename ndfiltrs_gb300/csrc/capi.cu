@@ -61,6 +61,8 @@ const char* algo_name(Algo a) {
       return "boxcar_band";
     case Algo::kExtremaPasses:
       return "extrema_passes";
+    case Algo::kRobust:
+      return "robust";
     case Algo::kMomentsSlide:
       return "moments_slide";
     case Algo::kExtremaTile:
@@ -153,6 +155,52 @@ bool is_selection(int kind) {
 }
 
 bool is_moment(int kind) { return kind == kMean || kind == kVar || kind == kStd; }
+
+bool is_robust(int kind) { return kind >= kMad && kind <= kSigmaMode; }
+
+// RobustReduction::validate (src/robust.rs:187-240) for the robust kinds,
+// then their parameters as the kernels read them.
+int validate_robust(const ndf_filter_desc* d, size_t count, Plan& p) {
+  const ndf_robust_params* rp = d->robust;
+  if (!rp) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing robust filter parameters");
+  const int kind = d->kind;
+  const bool clip = kind >= kSigmaMean;
+  auto pearson_ok = [&]() { return std::isfinite(rp->pearson) && rp->pearson >= 1.0; };
+  if (kind == kMad && (!std::isfinite(rp->parameter) || rp->parameter < 0.0))
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "MAD scale must be finite and nonnegative");
+  if (kind == kMode && !pearson_ok())
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "pearson must be finite and at least one");
+  if ((kind == kBiweightLocation || kind == kBiweightScale) &&
+      (!std::isfinite(rp->parameter) || rp->parameter <= 0.0))
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "biweight tuning constant must be finite and positive");
+  if (clip) {
+    if (!std::isfinite(rp->sigma_lower) || !std::isfinite(rp->sigma_upper) || rp->sigma_lower < 0.0 ||
+        rp->sigma_upper < 0.0)
+      return fail(NDF_ERR_INVALID_CONFIGURATION, "clipping limits must be finite and nonnegative");
+    if (kind == kSigmaMode && !pearson_ok())
+      return fail(NDF_ERR_INVALID_CONFIGURATION, "pearson must be finite and at least one");
+  }
+  const uint64_t min_count = clip || d->omit_nan ? d->min_count : 1;
+  if (min_count == 0 || min_count > count)
+    return fail(NDF_ERR_INVALID_CONFIGURATION,
+                "min_count must be between one and the number of window elements");
+  if ((rp->center != 0 && rp->center != 1) || (rp->spread != 0 && rp->spread != 1) || rp->estimator < 0 ||
+      rp->estimator > 2)
+    return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported clipping or mode option");
+  RobustArgs& a = p.robust;
+  a.kind = kind - kPercentile;
+  a.parameter = rp->parameter;
+  a.lower = rp->sigma_lower;
+  a.upper = rp->sigma_upper;
+  a.maxiters = rp->maxiters < 0 ? -1 : rp->maxiters;
+  a.center = rp->center;
+  a.spread = rp->spread;
+  a.estimator = rp->estimator;
+  a.modify_sample_size = rp->modify_sample_size != 0;
+  a.pearson = rp->pearson;
+  a.clip_min_count = (long long)min_count;
+  return NDF_OK;
+}
 
 // Canonical 3-D tile geometry for rank 1-3 arrays.
 void setup_tile(Plan& p) {
@@ -342,7 +390,7 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
   }
   if (count == 0)
     return fail(NDF_ERR_INVALID_CONFIGURATION, "footprint must select at least one element");
-  if (!is_selection(kind) && !is_moment(kind) && kind != kMeanRolling)
+  if (!is_selection(kind) && !is_moment(kind) && kind != kMeanRolling && !is_robust(kind))
     return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported window filter kind");
   Reduce& r = p.r;
   r.kind = kind;
@@ -357,7 +405,16 @@ int build_plan(const ndf_filter_desc* d, Plan& p) {
   r.pct = nullptr;
   r.cval = d->dtype == NDF_FLOAT32 ? (double)(float)d->cval : d->cval;
   r.moments = d->moments == NDF_MOMENTS_FP64 ? 1 : 0;
-  if (kind == kPercentile) {
+  if (is_robust(kind)) {
+    int rc = validate_robust(d, count, p);
+    if (rc != NDF_OK) return rc;
+    if (kind >= kSigmaMean) {
+      // Clipping always drops NaN and infinite samples (src/robust.rs:260-263).
+      r.omit = 1;
+      r.drop_inf = 1;
+    }
+    r.min_count = p.robust.clip_min_count;
+  } else if (kind == kPercentile) {
     if (!std::isfinite(r.q) || r.q < 0.0 || r.q > 100.0)
       return fail(NDF_ERR_INVALID_CONFIGURATION,
                   "percentile must be finite and between zero and 100");
@@ -586,6 +643,17 @@ int choose_algorithm(Plan& p, int smem_limit) {
     if (rc != NDF_OK) return rc;
   }
   const bool tileable = p.ndim <= 3 && p.r.count <= (1 << 24);
+  if (is_robust(p.r.kind)) {
+    int rc = setup_generic(p);
+    if (rc != NDF_OK) return rc;
+    if (!robust_configure(p)) {
+      cudaGetLastError();
+      p.d_scratch = nullptr;
+      return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
+    }
+    p.algo = Algo::kRobust;
+    return NDF_OK;
+  }
   if (p.r.kind == kMeanRolling) {
     // Exact rolling mean: the band or tiled kernel when one fits, with the
     // direct kernel for spans too wide for them (or for the whole array).
@@ -652,6 +720,9 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
     case Algo::kExtremaTile:
     case Algo::kExtremaPasses:
       e = launch_extrema(p, in, out, s);
+      break;
+    case Algo::kRobust:
+      e = launch_robust(p, in, out, s);
       break;
   }
   if (e != cudaSuccess) return cuda_fail(e, algo_name(p.algo));
@@ -920,20 +991,60 @@ int ndf_robust_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim
                       const uint64_t* shape, const uint64_t* size, const uint8_t* footprint,
                       const int64_t* origin, const char* const* modes, double cval,
                       const char* kind, double parameter, int32_t omit_nan,
-                      int32_t ignore_inf, uint64_t min_count) {
-  static const char* other_kinds[] = {"mad",        "mode",         "biweight_location",
-                                      "biweight_scale", "sigma_mean", "sigma_median",
-                                      "sigma_mode"};
-  if (!kind) return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported robust filter kind");
-  if (std::strcmp(kind, "percentile") != 0) {
-    for (const char* other : other_kinds)
-      if (std::strcmp(kind, other) == 0)
-        return fail(NDF_ERR_UNSUPPORTED,
-                    std::string("robust kind '") + kind + "' is outside this library's scope");
-    return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported robust filter kind");
-  }
-  if (!omit_nan && (ignore_inf || min_count != 1))
+                      int32_t ignore_inf, uint64_t min_count, double sigma_lower,
+                      double sigma_upper, int64_t maxiters, const char* center,
+                      const char* spread, const char* estimator, int32_t modify_sample_size,
+                      double pearson) {
+  static const std::pair<const char*, int> kinds[] = {
+      {"percentile", kPercentile},      {"mad", kMad},
+      {"mode", kMode},                  {"biweight_location", kBiweightLocation},
+      {"biweight_scale", kBiweightScale}, {"sigma_mean", kSigmaMean},
+      {"sigma_median", kSigmaMedian},   {"sigma_mode", kSigmaMode}};
+  int k = -1;
+  for (const auto& entry : kinds)
+    if (kind && std::strcmp(kind, entry.first) == 0) k = entry.second;
+  if (k < 0) return fail(NDF_ERR_INVALID_CONFIGURATION, "unsupported robust filter kind");
+  const bool clip = k >= kSigmaMean;
+  // src/pyapi/robust.rs:104-116 (non-clipping kinds), then the clipping and
+  // mode options in the order the reference parses them.
+  if (!clip && !omit_nan && (ignore_inf || min_count != 1))
     return fail(NDF_ERR_INVALID_CONFIGURATION, "ignore_inf and min_count require NaN omission");
+  ndf_robust_params rp{};
+  rp.parameter = parameter;
+  rp.sigma_lower = sigma_lower;
+  rp.sigma_upper = sigma_upper;
+  rp.maxiters = maxiters;
+  rp.modify_sample_size = modify_sample_size;
+  rp.pearson = pearson;
+  rp.center = NDF_CLIP_CENTER_MEDIAN;
+  rp.spread = NDF_CLIP_SPREAD_STD;
+  rp.estimator = NDF_MODE_ESTIMATOR_SEX;
+  auto parse_estimator = [&]() {
+    const char* e = estimator ? estimator : "sex";
+    if (std::strcmp(e, "sex") == 0) rp.estimator = NDF_MODE_ESTIMATOR_SEX;
+    else if (std::strcmp(e, "mmm") == 0) rp.estimator = NDF_MODE_ESTIMATOR_MMM;
+    else if (std::strcmp(e, "iraf") == 0) rp.estimator = NDF_MODE_ESTIMATOR_IRAF;
+    else return fail(NDF_ERR_INVALID_CONFIGURATION, "mode estimator must be 'sex', 'mmm', or 'iraf'");
+    return NDF_OK;
+  };
+  if (k == kMode) {
+    int rc = parse_estimator();
+    if (rc != NDF_OK) return rc;
+  }
+  if (clip) {
+    const char* c = center ? center : "median";
+    if (std::strcmp(c, "mean") == 0) rp.center = NDF_CLIP_CENTER_MEAN;
+    else if (std::strcmp(c, "median") == 0) rp.center = NDF_CLIP_CENTER_MEDIAN;
+    else return fail(NDF_ERR_INVALID_CONFIGURATION, "center must be 'mean' or 'median'");
+    const char* sp = spread ? spread : "std";
+    if (std::strcmp(sp, "std") == 0) rp.spread = NDF_CLIP_SPREAD_STD;
+    else if (std::strcmp(sp, "mad") == 0) rp.spread = NDF_CLIP_SPREAD_MAD;
+    else return fail(NDF_ERR_INVALID_CONFIGURATION, "spread must be 'std' or 'mad'");
+    if (k == kSigmaMode) {
+      int rc = parse_estimator();
+      if (rc != NDF_OK) return rc;
+    }
+  }
   if (ndim <= 0) return fail(NDF_ERR_INVALID_CONFIGURATION, "filtering requires at least one dimension");
   std::vector<int32_t> m(ndim);
   for (int a = 0; a < ndim; ++a) {
@@ -949,12 +1060,13 @@ int ndf_robust_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim
   d.origin = origin;
   d.modes = m.data();
   d.cval = cval;
-  d.kind = kPercentile;
-  d.omit_nan = omit_nan;
-  d.ignore_inf = ignore_inf;
+  d.kind = k;
+  d.omit_nan = clip ? 1 : omit_nan;
+  d.ignore_inf = clip ? 1 : ignore_inf;
   d.min_count = min_count;
   d.percentile = parameter;
   d.moments = NDF_MOMENTS_FP32C;
+  d.robust = k == kPercentile ? nullptr : &rp;
   return one_shot(d, h_in, h_out);
 }
 

@@ -29,6 +29,14 @@ enum Kind : int32_t {
   kRank = 9,
   kRankHistogram = 10,
   kPercentile = 11,
+  // Robust reductions (src/robust.rs:137-185).
+  kMad = 12,
+  kMode = 13,
+  kBiweightLocation = 14,
+  kBiweightScale = 15,
+  kSigmaMean = 16,
+  kSigmaMedian = 17,
+  kSigmaMode = 18,
 };
 
 // Error flags a kernel can raise in the plan's device status word.

@@ -51,6 +51,34 @@ struct Reduce {
   const PctEntry* pct; // device table indexed by n (count + 1 entries), or nullptr
 };
 
+// Robust reductions: estimator kinds as the kernels number them (kind - 11
+// of the C-ABI kinds) and their parameters (RobustReduction and ClipConfig,
+// src/robust.rs:52-185; ModeEstimator, src/location.rs:13-25).
+enum RobustKind {
+  kRobustPercentile = 0,
+  kRobustMad = 1,
+  kRobustMode = 2,
+  kRobustBiweightLocation = 3,
+  kRobustBiweightScale = 4,
+  kRobustSigmaMean = 5,
+  kRobustSigmaMedian = 6,
+  kRobustSigmaMode = 7,
+};
+enum ModeRule { kModeSex = 0, kModeMmm = 1, kModeIraf = 2 };
+
+struct RobustArgs {
+  int kind;                  // RobustKind
+  double parameter;          // MAD scale or biweight c
+  double lower, upper;       // clipping multipliers
+  long long maxiters;        // < 0: clip until stable
+  int center;                // 0 mean, 1 median
+  int spread;                // 0 std, 1 MAD
+  int estimator;             // ModeRule
+  int modify_sample_size;    // biweight scale
+  double pearson;            // mode rule factor
+  long long clip_min_count;  // ClipConfig::min_count
+};
+
 // Halo tile of one thread block: TW x TH outputs of one z slice. The block
 // stages kd x SH x SW samples (SH = TH + kh - 1, SW = TW + kw - 1).
 struct Tile {
@@ -98,6 +126,7 @@ enum class Algo {
   kExtremaTile,   // separable min / max (van Herk / Gil-Werman) over boxes
   kBoxcarBand,    // exact rolling mean, column sums sliding down bands
   kExtremaPasses, // separable min / max, two transposing column passes
+  kRobust,        // MAD, sigma clipping, mode, biweight: per-window float64
 };
 
 struct Plan {
@@ -149,6 +178,8 @@ struct Plan {
   // Kernel choice: measure candidates not in the autotune cache (batches).
   bool may_tune = false;
   int ext_rows[2] = {0, 0};  // rows per block of the two extrema column passes
+  RobustArgs robust{};       // robust estimator parameters
+  long long robust_threads = 0;  // threads of the scratch-backed robust kernel
 };
 
 const char* algo_name(Algo a);
@@ -190,6 +221,8 @@ bool moments_slide_configure(Plan& p, int smem_limit);
 cudaError_t launch_extrema(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool extrema_configure(Plan& p, int smem_limit);
 bool extrema_passes_configure(Plan& p, int smem_limit);
+bool robust_configure(Plan& p);
+cudaError_t launch_robust(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool boxcar_configure(Plan& p, int smem_limit);
 bool boxcar_band_configure(Plan& p, int smem_limit);
 

@@ -1,0 +1,501 @@
+// Robust window statistics: the MAD, iterative sigma clipping, the mode
+// estimators and the biweight location / scale.
+//
+// Replaces RobustReduction::finish for those kinds (src/robust.rs:244-299,
+// 376-689) and the estimators of src/location.rs:36-240, applied per window
+// by robust_into (src/robust.rs:725-785). Every step keeps the reference's
+// float64 arithmetic, operation for operation (each operation correctly
+// rounded, no contraction), so the results equal the reference's bit for
+// bit; the one order the reference leaves unpublished (the sample order
+// after its in-place median, which the biweight sums follow) is ascending
+// order here, as in the oracle.
+//
+// GB300 design: one thread per output pixel (grid-stride). A thread gathers
+// its window through the per-axis boundary maps (flat offsets for interior
+// windows), keeps the retained samples twice, in tap order (the order of
+// the reference's sums) and sorted by total order (insertion sort on
+// order-preserving keys), and runs the estimator on those two arrays. The
+// arrays live in thread-local memory for windows up to 256 samples and in a
+// per-thread slice of a global scratch buffer beyond. The work is float64
+// and branchy, so it runs on the FP64 pipe at a fraction of the FP32 rate;
+// the windows the robust filters serve are small.
+#include <algorithm>
+
+#include "common.cuh"
+#include "moments.cuh"
+#include "plan.h"
+
+namespace ndf {
+namespace {
+
+constexpr int kRThreads = 128;
+// Phi^-1(0.75), src/robust.rs:11.
+constexpr double kNormalUpperQuartile = 0.6744897501960817;
+
+struct Scaled {
+  double value;
+  int exponent;
+};
+
+__device__ __forceinline__ unsigned long long total_key(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ int total_cmp(double a, double b) {
+  const unsigned long long ka = total_key(a), kb = total_key(b);
+  return ka < kb ? -1 : (ka > kb ? 1 : 0);
+}
+
+__device__ void sort_total(double* a, int n) {
+  for (int i = 1; i < n; ++i) {
+    const double v = a[i];
+    const unsigned long long k = total_key(v);
+    int j = i - 1;
+    while (j >= 0 && total_key(a[j]) > k) {
+      a[j + 1] = a[j];
+      --j;
+    }
+    a[j + 1] = v;
+  }
+}
+
+// 2^n by binary powering with a final reciprocal for negative n: exact
+// unless 2^|n| overflows, when the reciprocal is zero.
+__device__ double powi2(int n) {
+  unsigned int m = n < 0 ? (unsigned int)(-(long long)n) : (unsigned int)n;
+  double r = 1.0, a = 2.0;
+  while (m) {
+    if (m & 1) r = __dmul_rn(r, a);
+    a = __dmul_rn(a, a);
+    m >>= 1;
+  }
+  return n < 0 ? __ddiv_rn(1.0, r) : r;
+}
+
+// binary_parts, src/robust.rs:498-511 (positive finite values).
+__device__ __forceinline__ Scaled binary_parts(double value) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(value);
+  const int exponent = (int)((b >> 52) & 0x7ff);
+  const unsigned long long fraction = b & ((1ull << 52) - 1);
+  if (exponent == 0) {
+    const int leading = 63 - __clzll((long long)fraction);
+    return {__ddiv_rn((double)fraction, (double)(1ull << leading)), leading - 1074};
+  }
+  return {__longlong_as_double((long long)(fraction | (1023ull << 52))), exponent - 1023};
+}
+
+__device__ __forceinline__ double inf64() { return __longlong_as_double(0x7ff0000000000000ll); }
+
+// absolute_deviation, src/robust.rs:438-466.
+__device__ Scaled absolute_deviation(double value, Scaled center) {
+  if (center.exponent == -1 && isfinite(__dmul_rn(value, 2.0))) {
+    const double difference = __dsub_rn(__dmul_rn(value, 2.0), center.value);
+    if (isfinite(difference)) return {fabs(difference), -1};
+  }
+  const double midpoint = center.exponent == -1 ? __ddiv_rn(center.value, 2.0) : center.value;
+  const double difference = __dsub_rn(value, midpoint);
+  if (isfinite(difference) || isinf(value)) return {fabs(difference), 0};
+  return {fabs(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(midpoint, 2.0))), 1};
+}
+
+// compare_scaled, src/robust.rs:468-481.
+__device__ int compare_scaled(Scaled left, Scaled right) {
+  if (left.value == 0.0 || right.value == 0.0 || isinf(left.value) || isinf(right.value))
+    return total_cmp(left.value, right.value);
+  const Scaled l = binary_parts(left.value), r = binary_parts(right.value);
+  const int a = l.exponent + left.exponent, b = r.exponent + right.exponent;
+  if (a != b) return a < b ? -1 : 1;
+  return total_cmp(l.value, r.value);
+}
+
+// scaled_midpoint, src/robust.rs:483-496.
+__device__ Scaled scaled_midpoint(Scaled left, Scaled right) {
+  if (isinf(right.value) || right.value == 0.0) return right;
+  const Scaled r = binary_parts(right.value);
+  const int exponent = r.exponent + right.exponent;
+  double lv = 0.0;
+  if (left.value != 0.0) {
+    const Scaled l = binary_parts(left.value);
+    lv = __dmul_rn(l.value, powi2(l.exponent + left.exponent - exponent));
+  }
+  return {__dadd_rn(lv, r.value), exponent - 1};
+}
+
+// mad_parts, src/robust.rs:376-436, over samples sorted in total order.
+__device__ Scaled mad_parts(const double* s, int n) {
+  const double lower = s[(n - 1) / 2], upper = s[n / 2];
+  Scaled center;
+  if (!isfinite(lower) || !isfinite(upper))
+    center = {interpolate(lower, upper, 0.5), 0};
+  else if (isfinite(__dadd_rn(lower, upper)))
+    center = {__dadd_rn(lower, upper), -1};
+  else
+    center = {__dadd_rn(__ddiv_rn(lower, 2.0), __ddiv_rn(upper, 2.0)), 0};
+  if (!isfinite(center.value)) return {nan_of(0.0), 0};
+  int left = n / 2, right = left;
+  Scaled previous{0.0, 0}, selected = previous;
+  for (int step = 0; step <= n / 2; ++step) {
+    previous = selected;
+    const bool take_left = left > 0 && (right == n || compare_scaled(absolute_deviation(s[left - 1], center),
+                                                                      absolute_deviation(s[right], center)) <= 0);
+    if (take_left) {
+      --left;
+      selected = absolute_deviation(s[left], center);
+    } else {
+      selected = absolute_deviation(s[right], center);
+      ++right;
+    }
+  }
+  return n % 2 == 1 ? selected : scaled_midpoint(previous, selected);
+}
+
+// multiply_scaled, src/robust.rs:513-534.
+__device__ double multiply_scaled(Scaled value, double multiplier) {
+  if (!isfinite(value.value)) return __dmul_rn(value.value, multiplier);
+  if (value.value == 0.0 || multiplier == 0.0) return 0.0;
+  const Scaled l = binary_parts(value.value), r = binary_parts(multiplier);
+  const Scaled m = binary_parts(__dmul_rn(l.value, r.value));
+  const int exponent = l.exponent + r.exponent + m.exponent + value.exponent;
+  if (exponent > 1023) return inf64();
+  if (exponent < -1075) return 0.0;
+  if (exponent >= -1022) return __dmul_rn(m.value, __longlong_as_double((long long)(exponent + 1023) << 52));
+  const double scale = __longlong_as_double((long long)(exponent + 2045) << 52);
+  return __dmul_rn(__dmul_rn(m.value, 2.2250738585072014e-308), scale);
+}
+
+// within_limit, src/robust.rs:536-559.
+__device__ bool within_limit(double value, double center, Scaled spread, double sigma) {
+  if (value == center) return true;
+  if (spread.value == 0.0 || sigma == 0.0) return false;
+  const double difference = __dsub_rn(value, center);
+  Scaled d;
+  if (isfinite(difference)) {
+    d = binary_parts(fabs(difference));
+  } else {
+    d = binary_parts(fabs(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(center, 2.0))));
+    d.exponent += 1;
+  }
+  const Scaled sc = binary_parts(spread.value), mu = binary_parts(sigma);
+  const Scaled limit = binary_parts(__dmul_rn(sc.value, mu.value));
+  const int limit_exp = sc.exponent + mu.exponent + limit.exponent + spread.exponent;
+  return d.exponent < limit_exp || (d.exponent == limit_exp && d.value <= limit.value);
+}
+
+// percentile, src/robust.rs:343-352, over sorted samples.
+__device__ double percentile_sorted(const double* s, int n, double q) {
+  if (q == 100.0) return s[n - 1];
+  const double rank = __dmul_rn(__ddiv_rn(q, 100.0), (double)(n - 1));
+  const int lower = (int)floor(rank);
+  const int upper = min(lower + 1, n - 1);
+  return interpolate(s[lower], s[upper], __dsub_rn(rank, (double)lower));
+}
+
+// median_valid_in_place of the reducers crate over sorted samples: the
+// middle value, or the midpoint of the two middle values.
+__device__ __forceinline__ double median_sorted(const double* s, int n) {
+  return n % 2 == 1 ? s[n / 2] : midpoint(s[n / 2 - 1], s[n / 2]);
+}
+
+// finite_mean, src/robust.rs:572-592, in tap order.
+__device__ double finite_mean(const double* v, int n) {
+  Sum64 sum;
+  for (int i = 0; i < n; ++i) sum.add(v[i]);
+  const double total = sum.total();
+  if (isfinite(total)) return __ddiv_rn(total, (double)n);
+  const unsigned long long m = (unsigned long long)(n - 1);
+  const int exponent = (m == 0 ? 0 : 64 - __clzll((long long)m)) + 1;
+  const double scale = powi2(exponent);
+  Sum64 scaled;
+  double lower = inf64(), upper = -inf64();
+  for (int i = 0; i < n; ++i) {
+    scaled.add(__ddiv_rn(v[i], scale));
+    lower = fmin(lower, v[i]);
+    upper = fmax(upper, v[i]);
+  }
+  return clamp64(__ddiv_rn(scaled.total(), __ddiv_rn((double)n, scale)), lower, upper);
+}
+
+// std_parts, src/robust.rs:594-630, in tap order.
+__device__ Scaled std_parts(const double* v, int n) {
+  const double reference = v[0];
+  bool halve = false;
+  for (int i = 0; i < n; ++i) halve = halve || !isfinite(__dsub_rn(v[i], reference));
+  auto delta = [&](double x) {
+    return halve ? __dsub_rn(__ddiv_rn(x, 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(x, reference);
+  };
+  double scale = 0.0;
+  for (int i = 0; i < n; ++i) scale = fmax(scale, fabs(delta(v[i])));
+  if (scale == 0.0) return {0.0, 0};
+  Sum64 sum;
+  for (int i = 0; i < n; ++i) sum.add(__ddiv_rn(delta(v[i]), scale));
+  const double center = __ddiv_rn(sum.total(), (double)n);
+  Sum64 squares;
+  for (int i = 0; i < n; ++i) {
+    const double residual = __dsub_rn(__ddiv_rn(delta(v[i]), scale), center);
+    squares.add(__dmul_rn(residual, residual));
+  }
+  const Scaled parts = binary_parts(scale);
+  return {__dmul_rn(parts.value, __dsqrt_rn(__ddiv_rn(squares.total(), (double)n))),
+          parts.exponent + (halve ? 1 : 0)};
+}
+
+// mode_from_moments, src/location.rs:56-84.
+__device__ double mode_from_moments(double mean, double median, double std_dev, int estimator, double pearson) {
+  const double difference = __dsub_rn(median, mean);
+  const double pearson_mode = __dadd_rn(median, __dmul_rn(__dsub_rn(pearson, 1.0), difference));
+  if (estimator == kModeMmm) return pearson_mode;
+  if (estimator == kModeIraf) return mean < median ? mean : pearson_mode;
+  if (std_dev == 0.0) return mean;
+  if (__ddiv_rn(fabs(difference), std_dev) >= 0.3) return median;
+  return pearson_mode;
+}
+
+// mode_estimate, src/location.rs:36-54: mean and std in tap order (`v`),
+// the median from the sorted samples (`s`).
+__device__ double mode_estimate(const double* v, const double* s, int n, int estimator, double pearson) {
+  if (n == 0) return nan_of(0.0);
+  Reduce r{};
+  r.count = n;
+  auto fetch = [&](int i) { return v[i]; };
+  const double mean = mom::mean_exact(fetch, r);
+  const double std_dev = estimator == kModeSex ? mom::dispersion_exact(fetch, r, true) : nan_of(0.0);
+  return mode_from_moments(mean, median_sorted(s, n), std_dev, estimator, pearson);
+}
+
+// standardize + biweight_location / biweight_scale, src/location.rs:104-240,
+// over samples sorted in total order; `dev` receives the standardized
+// deviations in that order.
+__device__ double biweight(const double* s, int n, double* dev, const RobustArgs& ra, bool location) {
+  const double median = median_sorted(s, n);
+  double factor = 1.0;
+  bool overflow = false;
+  for (int i = 0; i < n; ++i) {
+    dev[i] = __dsub_rn(s[i], median);
+    overflow = overflow || !isfinite(dev[i]);
+  }
+  if (overflow) {
+    factor = 2.0;
+    for (int i = 0; i < n; ++i) dev[i] = __dsub_rn(__ddiv_rn(s[i], 2.0), __ddiv_rn(median, 2.0));
+  }
+  // Median of |dev|: the deviations ascend, so their magnitudes ascend
+  // outwards from the smallest; merge both sides up to the middle ranks.
+  int right = 0;
+  while (right < n && dev[right] < 0.0) ++right;
+  int left = right;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k <= n / 2; ++k) {
+    double next;
+    if (left > 0 && (right == n || fabs(dev[left - 1]) <= fabs(dev[right]))) {
+      next = fabs(dev[--left]);
+    } else {
+      next = fabs(dev[right++]);
+    }
+    if (k == (n - 1) / 2) a = next;
+    if (k == n / 2) b = next;
+  }
+  double mad = n % 2 == 1 ? b : midpoint(a, b);
+  if (mad == 0.0) return location ? median : 0.0;
+  const double c = ra.parameter;
+  double extra = 1.0;
+  while (!isfinite(__dmul_rn(c, mad))) {
+    mad = __ddiv_rn(mad, 2.0);
+    extra = __dmul_rn(extra, 2.0);
+  }
+  const double width = __dmul_rn(c, mad);
+  factor = __dmul_rn(factor, extra);
+  if (location) {
+    Sum64 weighted, weights;
+    for (int i = 0; i < n; ++i) {
+      const double u = __ddiv_rn(__ddiv_rn(dev[i], extra), width);
+      if (!(fabs(u) < 1.0)) continue;
+      const double t = __dsub_rn(1.0, __dmul_rn(u, u));
+      const double weight = __dmul_rn(t, t);
+      weighted.add(__dmul_rn(u, weight));
+      weights.add(weight);
+    }
+    const double correction = __dmul_rn(width, __ddiv_rn(weighted.total(), weights.total()));
+    const double unscaled = __dmul_rn(correction, factor);
+    if (isfinite(unscaled)) return __dadd_rn(median, unscaled);
+    return __dmul_rn(__dadd_rn(__ddiv_rn(median, factor), correction), factor);
+  }
+  Sum64 numerator, denominator;
+  int kept = 0;
+  for (int i = 0; i < n; ++i) {
+    const double u = __ddiv_rn(__ddiv_rn(dev[i], extra), width);
+    if (!(fabs(u) < 1.0)) continue;
+    const double u2 = __dmul_rn(u, u);
+    const double w = __dsub_rn(1.0, u2);
+    const double taper = __dmul_rn(w, w);
+    numerator.add(__dmul_rn(__dmul_rn(u2, taper), taper));
+    denominator.add(__dmul_rn(w, __dsub_rn(1.0, __dmul_rn(5.0, u2))));
+    ++kept;
+  }
+  const double count = (double)(ra.modify_sample_size ? kept : n);
+  const double ratio = __ddiv_rn(__dsqrt_rn(__dmul_rn(count, numerator.total())), fabs(denominator.total()));
+  return __dmul_rn(__dmul_rn(width, ratio), factor);
+}
+
+// clipped, src/robust.rs:632-689: `v` holds the finite samples in tap
+// order and `s` the same samples sorted; both shrink together.
+__device__ double clipped(double* v, double* s, int n, const RobustArgs& ra, int kind) {
+  long long iteration = 0;
+  while (n >= ra.clip_min_count && (ra.maxiters < 0 || iteration < ra.maxiters)) {
+    const double center = ra.center == 0 ? finite_mean(v, n) : percentile_sorted(s, n, 50.0);
+    Scaled spread;
+    if (ra.spread == 1) {
+      const Scaled deviation = mad_parts(s, n);
+      if (deviation.value > 0.0 && isfinite(deviation.value)) {
+        const Scaled parts = binary_parts(deviation.value);
+        spread = {__ddiv_rn(parts.value, kNormalUpperQuartile), parts.exponent + deviation.exponent};
+      } else {
+        spread = deviation;
+      }
+    } else {
+      spread = std_parts(v, n);
+    }
+    int kept = 0, kept_sorted = 0;
+    for (int i = 0; i < n; ++i) {
+      const double x = v[i];
+      if (within_limit(x, center, spread, x < center ? ra.lower : ra.upper)) v[kept++] = x;
+      const double y = s[i];
+      if (within_limit(y, center, spread, y < center ? ra.lower : ra.upper)) s[kept_sorted++] = y;
+    }
+    ++iteration;
+    const bool stable = kept == n;
+    n = kept;
+    if (stable) break;
+  }
+  if (n < ra.clip_min_count) return nan_of(0.0);
+  if (kind == kRobustSigmaMean) return finite_mean(v, n);
+  if (kind == kRobustSigmaMedian) return percentile_sorted(s, n, 50.0);
+  return mode_estimate(v, s, n, ra.estimator, ra.pearson);
+}
+
+// One window: gather, the sample policy, the estimator.
+template <typename Fetch>
+__device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const RobustArgs& ra, double* v,
+                                double* s) {
+  const bool clip = ra.kind >= kRobustSigmaMean;
+  int n = 0;
+  bool nan = false, inf = false;
+  for (int i = 0; i < V; ++i) {
+    const double x = fetch(i);
+    if (clip) {
+      if (isfinite(x)) v[n++] = x;
+      continue;
+    }
+    if (isnan(x)) {
+      nan = nan || !r.omit;
+      continue;
+    }
+    if (r.drop_inf && isinf(x)) continue;
+    inf = inf || isinf(x);
+    v[n++] = x;
+  }
+  if (!clip) {
+    if (nan || (r.omit && n < r.min_count) || n == 0) return nan_of(0.0);
+  }
+  for (int i = 0; i < n; ++i) s[i] = v[i];
+  sort_total(s, n);
+  switch (ra.kind) {
+    case kRobustMad:
+      return multiply_scaled(mad_parts(s, n), ra.parameter);
+    case kRobustMode:
+      return inf ? nan_of(0.0) : mode_estimate(v, s, n, ra.estimator, ra.pearson);
+    case kRobustBiweightLocation:
+    case kRobustBiweightScale:
+      return inf ? nan_of(0.0) : biweight(s, n, v, ra, ra.kind == kRobustBiweightLocation);
+    default:
+      return clipped(v, s, n, ra, ra.kind);
+  }
+}
+
+// MAXV > 0: thread-local arrays; MAXV == 0: per-thread slices of `scratch`.
+template <typename T, int MAXV>
+__global__ void __launch_bounds__(kRThreads)
+    robust_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ GenericArgs a,
+                  const long long* __restrict__ taps, const __grid_constant__ RobustArgs ra,
+                  double* __restrict__ scratch) {
+  const int rank = a.rank;
+  const int V = a.r.count;
+  const long long* flat = taps + (long long)V * rank;
+  const T cval = (T)a.r.cval;
+  double local_v[MAXV > 0 ? MAXV : 1], local_s[MAXV > 0 ? MAXV : 1];
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double* v = MAXV > 0 ? local_v : scratch + tid * 2ll * V;
+  double* s = MAXV > 0 ? local_s : v + V;
+  for (long long o = tid; o < a.n_out; o += (long long)gridDim.x * blockDim.x) {
+    long long coord[kMaxGenericRank];
+    long long rem = o;
+    bool interior = true;
+    for (int d = 0; d < rank; ++d) {
+      coord[d] = rem / a.stride[d];
+      rem -= coord[d] * a.stride[d];
+      interior = interior && coord[d] + a.low[d] >= 0 && coord[d] + a.high[d] < a.shape[d];
+    }
+    auto fetch = [&](int i) -> double {
+      if (interior) return (double)__ldg(in + o + flat[i]);
+      const long long* tap = taps + (long long)i * rank;
+      long long src = 0;
+      for (int d = 0; d < rank; ++d) {
+        long long m;
+        if (!map_index(coord[d] + tap[d], a.shape[d], a.mode[d], &m)) return (double)cval;
+        src += m * a.stride[d];
+      }
+      return (double)__ldg(in + src);
+    };
+    const double result = robust_window(fetch, V, a.r, ra, v, s);
+    T value;
+    if constexpr (sizeof(T) == 4)
+      value = isnan(result) ? nan_of(0.0f) : __double2float_rn(result);
+    else
+      value = isnan(result) ? nan_of(0.0) : result;
+    out[o] = value;
+  }
+}
+
+template <typename T, int MAXV>
+cudaError_t launch_robust_v(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  const long long blocks = MAXV > 0 ? std::max(1ll, std::min((p.n_out + kRThreads - 1) / kRThreads,
+                                                             (long long)std::max(1, p.sm_count) * 16))
+                                    : p.robust_threads / kRThreads;
+  robust_kernel<T, MAXV><<<(unsigned)blocks, kRThreads, 0, s>>>(in, out, p.generic, p.d_gen_taps, p.robust,
+                                                                 reinterpret_cast<double*>(p.d_scratch));
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_robust_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
+  const int V = p.r.count;
+  if (V <= 32) return launch_robust_v<T, 32>(p, in, out, s);
+  if (V <= 64) return launch_robust_v<T, 64>(p, in, out, s);
+  if (V <= 128) return launch_robust_v<T, 128>(p, in, out, s);
+  if (V <= 256) return launch_robust_v<T, 256>(p, in, out, s);
+  return launch_robust_v<T, 0>(p, in, out, s);
+}
+
+}  // namespace
+
+// Windows beyond 256 samples take per-thread slices of a scratch buffer of
+// at most 1 GiB (two float64 arrays per thread): the thread count is the
+// largest multiple of the block size within that, capped at 16 blocks per
+// SM. Returns false when the scratch cannot be allocated.
+bool robust_configure(Plan& p) {
+  p.robust_threads = 0;
+  if (p.r.count <= 256) return true;
+  const size_t per_thread = (size_t)p.r.count * 2 * sizeof(double);
+  long long threads = (long long)((1ull << 30) / per_thread) / kRThreads * kRThreads;
+  threads = std::min(threads, (long long)std::max(1, p.sm_count) * 16 * kRThreads);
+  if (threads < kRThreads) threads = kRThreads;
+  p.robust_threads = threads;
+  p.scratch_bytes = (size_t)threads * per_thread;
+  return cudaMalloc(&p.d_scratch, p.scratch_bytes) == cudaSuccess;
+}
+
+cudaError_t launch_robust(const Plan& p, const void* in, void* out, cudaStream_t s) {
+  if (p.dtype == 0) return launch_robust_t<float>(p, (const float*)in, (float*)out, s);
+  return launch_robust_t<double>(p, (const double*)in, (double*)out, s);
+}
+
+}  // namespace ndf
