@@ -197,7 +197,9 @@ MEASURED_TRAFFIC = {
     "nanmedian_sortnet_5x5_4096_f32": (67.154688e6 + 30.220032e6, "profiles/tile_box_kernel_nanmedian_sortnet_5x5_4096_f32.md"),
     "nanmedian_hist_65x65_4096_f32": (172.860160e6 + 1.108634e9, "profiles/histogram_kernel_nanmedian_hist_65x65_4096_f32.md"),
     "nanmedian_ring_4_6_4096_f32": (67.187968e6 + 32.040704e6, "profiles/tile_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
-    "nanstd_31x31_4096_f32": (69.093376e6 + 34.978048e6, "profiles/tile_moments_kernel_nanstd_31x31_4096_f32.md"),
+    "nanstd_31x31_4096_f32": (67.205120e6 + 31.025152e6, "profiles/moments_slide_kernel_nanstd_31x31_4096_f32.md"),
+    "nanmin_31x31_4096_f32": (67.144192e6 + 21.329152e6, "profiles/extrema_pass_kernel_nanmin_31x31_4096_f32.md"),
+    "nanmad_5x5_4096_f32": (108.382208e6 + 2.929056e9, "profiles/robust_kernel_nanmad_5x5_4096_f32.md"),
 }
 
 

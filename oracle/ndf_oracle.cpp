@@ -2066,6 +2066,523 @@ double robust_finish(const RobustSpec& spec, std::vector<double>& values) {
   return biweight_scale(values, spec.parameter, spec.modify_sample_size);
 }
 
+// ---------------------------------------------------------------------------
+// Mesh background: MeshBackground::new / estimate / interpolate_into
+// (src/background.rs:417-923), the per-mesh statistics (:924-1152), the
+// natural spline (:1154-1212) and the SExtractor-compatible interpolation
+// (src/background/sep_interpolation.rs).
+
+struct MeshSpec {
+  int estimator = 0;  // 0 SExtractor, 1 sigma clip
+  double pearson = 2.5;
+  double lower = 3.0, upper = 3.0;
+  int64_t maxiters = 10;  // < 0: until stable
+  int center = 1, spread = 0;
+  int statistic = 2;  // 0 mean, 1 median, 2 mode
+  int mode_estimator = kModeSex;
+  int rms = 0;        // 0 std, 1 MAD std
+  double min_valid_fraction = 0.5;
+  int valid_count = 0;  // 0 finite, 1 retained
+  int valid_base = 0;   // 0 mesh, 1 box
+  int fill = 0;         // 0 nearest, 1 inverse distance
+  uint64_t idw_neighbors = 10;
+  double idw_power = 1.0;
+  int filter_edge = 0;     // 0 shrink, 1 truncate
+  int threshold_kind = 0;  // 0 all, 1 deviation, 2 above
+  double threshold = 0.0;
+  int interpolation = 0;   // 0 spline, 1 SExtractor
+};
+
+// median_sorted / median_of, src/background.rs:940-963.
+double mesh_median_sorted(const double* v, size_t n) {
+  if (n % 2 == 1) return v[n / 2];
+  const double a = v[n / 2 - 1], b = v[n / 2];
+  const double mid = (a + b) / 2.0;
+  return std::isfinite(mid) ? mid : a / 2.0 + b / 2.0;
+}
+
+double mesh_median_of(std::vector<double> v) {
+  if (v.empty()) return kNaN64;
+  for (double x : v)
+    if (std::isnan(x)) return kNaN64;
+  std::sort(v.begin(), v.end(), key_less);
+  return mesh_median_sorted(v.data(), v.size());
+}
+
+// mean_of, src/background.rs:965-978.
+double mesh_mean_of(const double* v, size_t n) {
+  Sum sum;
+  for (size_t i = 0; i < n; ++i) sum.add(v[i]);
+  const double total = sum.total();
+  if (std::isfinite(total)) return total / (double)n;
+  return mean_valid(v, n);
+}
+
+// std_about, src/background.rs:1000-1015.
+double mesh_std_about(const double* v, size_t n, double mean) {
+  if (n == 0) return kNaN64;
+  const double scale = std::fmax(std::fabs(v[0] - mean), std::fabs(v[n - 1] - mean));
+  if (scale == 0.0) return 0.0;
+  if (!std::isfinite(scale)) return kNaN64;
+  Sum squares;
+  for (size_t i = 0; i < n; ++i) {
+    const double deviation = (v[i] - mean) / scale;
+    squares.add(deviation * deviation);
+  }
+  return scale * std::sqrt(squares.total() / (double)n);
+}
+
+// mad_std, src/background.rs:1017-1022.
+double mesh_mad_std(const double* v, size_t n, double median) {
+  std::vector<double> scratch(n);
+  for (size_t i = 0; i < n; ++i) scratch[i] = std::fabs(v[i] - median);
+  return mesh_median_of(std::move(scratch)) / kNormalUpperQuartile;
+}
+
+// within, src/background.rs:1024-1032.
+std::pair<size_t, size_t> mesh_within(const std::vector<double>& v, std::pair<size_t, size_t> range,
+                                      double low, double high) {
+  const auto b = v.begin() + (ptrdiff_t)range.first, e = v.begin() + (ptrdiff_t)range.second;
+  const size_t lo = range.first + (size_t)(std::partition_point(b, e, [&](double x) { return x < low; }) - b);
+  const size_t hi = range.first + (size_t)(std::partition_point(b, e, [&](double x) { return x <= high; }) - b);
+  return {lo, std::max(hi, lo)};
+}
+
+// clip_sorted, src/background.rs:1034-1069.
+std::pair<size_t, size_t> mesh_clip_sorted(const std::vector<double>& v, std::pair<size_t, size_t> range,
+                                           double lower, double upper, int64_t maxiters, int center,
+                                           int spread, size_t min_count) {
+  int64_t iteration = 0;
+  while (range.second - range.first >= std::max<size_t>(min_count, 1) &&
+         (maxiters < 0 || iteration < maxiters)) {
+    const double* kept = v.data() + range.first;
+    const size_t n = range.second - range.first;
+    const double middle = center == 0 ? mesh_mean_of(kept, n) : mesh_median_sorted(kept, n);
+    const double width = spread == 0 ? mesh_std_about(kept, n, mesh_mean_of(kept, n))
+                                     : mesh_mad_std(kept, n, mesh_median_sorted(kept, n));
+    const auto next = mesh_within(v, range, middle - lower * width, middle + upper * width);
+    ++iteration;
+    if (next == range) break;
+    range = next;
+  }
+  return range;
+}
+
+struct MeshStat {
+  double background = kNaN64, rms = kNaN64;
+  uint64_t finite = 0, retained = 0;
+  bool valid = false;
+};
+
+// sextractor_stats / clipped_stats / finish_stats, src/background.rs:652-705,
+// 1071-1152, over the mesh's finite samples sorted in total order.
+MeshStat mesh_finish(std::vector<double>& v, uint64_t volume, uint64_t box_volume, const MeshSpec& spec) {
+  MeshStat st;
+  st.finite = v.size();
+  if (v.empty()) return st;
+  std::sort(v.begin(), v.end(), key_less);
+  const size_t n = v.size();
+  double background = kNaN64, rms = kNaN64;
+  size_t retained = 0;
+  if (spec.estimator == 0) {
+    const double mean = mesh_mean_of(v.data(), n);
+    const double sd = mesh_std_about(v.data(), n, mean);
+    const auto first = mesh_within(v, {0, n}, mean - 2.0 * sd, mean + 2.0 * sd);
+    if (first.first != first.second) {
+      const double* sub = v.data() + first.first;
+      const size_t m = first.second - first.first;
+      const double mean2 = mesh_mean_of(sub, m);
+      const double sd2 = mesh_std_about(sub, m, mean2);
+      const auto span = mesh_within(v, {0, n}, mean2 - 5.0 * sd2, mean2 + 5.0 * sd2);
+      const auto kept = mesh_clip_sorted(v, span, 3.0, 3.0, 100, 1, 0, 1);
+      if (kept.first != kept.second) {
+        const double* k = v.data() + kept.first;
+        const size_t c = kept.second - kept.first;
+        const double mean3 = mesh_mean_of(k, c);
+        const double sd3 = mesh_std_about(k, c, mean3);
+        background = mode_from_moments(mean3, mesh_median_sorted(k, c), sd3, kModeSex, spec.pearson);
+        rms = sd3;
+        retained = c;
+      }
+    }
+  } else {
+    const auto kept = mesh_clip_sorted(v, {0, n}, spec.lower, spec.upper, spec.maxiters, spec.center,
+                                       spec.spread, 1);
+    const size_t c = kept.second - kept.first;
+    retained = c;
+    if (c > 0) {
+      const double* k = v.data() + kept.first;
+      const double mean = mesh_mean_of(k, c);
+      const double median = mesh_median_sorted(k, c);
+      if (spec.statistic == 0)
+        background = mean;
+      else if (spec.statistic == 1)
+        background = median;
+      else
+        background = mode_from_moments(mean, median, mesh_std_about(k, c, mean), spec.mode_estimator,
+                                       spec.pearson);
+      rms = spec.rms == 0 ? mesh_std_about(k, c, mean) : mesh_mad_std(k, c, median);
+    }
+  }
+  st.retained = retained;
+  const uint64_t count = spec.valid_count == 0 ? st.finite : retained;
+  const uint64_t base = spec.valid_base == 0 ? volume : box_volume;
+  if (count > 0 && (double)count >= spec.min_valid_fraction * (double)base && std::isfinite(background) &&
+      std::isfinite(rms)) {
+    st.background = background;
+    st.rms = rms;
+    st.valid = true;
+  }
+  return st;
+}
+
+void mesh_index(size_t flat, const std::vector<size_t>& mesh_shape, size_t* index) {
+  for (size_t a = mesh_shape.size(); a-- > 0;) {
+    index[a] = flat % mesh_shape[a];
+    flat /= mesh_shape[a];
+  }
+}
+
+// fill_invalid / replacement, src/background.rs:715-798.
+void mesh_fill(std::vector<double>& bg, std::vector<double>& rms, const std::vector<bool>& valid,
+               const std::vector<size_t>& mesh_shape, const MeshSpec& spec) {
+  const size_t len = bg.size(), ndim = mesh_shape.size();
+  std::vector<size_t> good;
+  for (size_t i = 0; i < len; ++i)
+    if (valid[i]) good.push_back(i);
+  if (good.size() == len || good.empty()) return;
+  std::vector<size_t> gi(good.size() * ndim), idx(ndim);
+  for (size_t s = 0; s < good.size(); ++s) mesh_index(good[s], mesh_shape, &gi[s * ndim]);
+  std::vector<std::tuple<size_t, double, double>> out;
+  std::vector<std::pair<uint64_t, size_t>> d;
+  for (size_t flat = 0; flat < len; ++flat) {
+    if (valid[flat]) continue;
+    mesh_index(flat, mesh_shape, idx.data());
+    d.clear();
+    for (size_t s = 0; s < good.size(); ++s) {
+      uint64_t d2 = 0;
+      for (size_t a = 0; a < ndim; ++a) {
+        const uint64_t diff = idx[a] > gi[s * ndim + a] ? idx[a] - gi[s * ndim + a] : gi[s * ndim + a] - idx[a];
+        d2 += diff * diff;
+      }
+      d.push_back({d2, good[s]});
+    }
+    double value, spread;
+    if (spec.fill == 0) {
+      uint64_t nearest = UINT64_MAX;
+      for (auto& e : d) nearest = std::min(nearest, e.first);
+      Sum v, r;
+      size_t count = 0;
+      for (auto& e : d)
+        if (e.first == nearest) {
+          v.add(bg[e.second]);
+          r.add(rms[e.second]);
+          ++count;
+        }
+      value = v.total() / (double)count;
+      spread = r.total() / (double)count;
+    } else {
+      std::sort(d.begin(), d.end());
+      const uint64_t last = d[std::min<size_t>(spec.idw_neighbors, d.size()) - 1].first;
+      Sum weighted, weighted_rms, total;
+      for (auto& e : d) {
+        if (e.first > last) break;
+        const double weight = 1.0 / std::pow(std::sqrt((double)e.first), spec.idw_power);
+        weighted.add(weight * bg[e.second]);
+        weighted_rms.add(weight * rms[e.second]);
+        total.add(weight);
+      }
+      value = weighted.total() / total.total();
+      spread = weighted_rms.total() / total.total();
+    }
+    out.emplace_back(flat, value, spread);
+  }
+  for (auto& [flat, value, spread] : out) {
+    bg[flat] = value;
+    rms[flat] = spread;
+  }
+}
+
+// filter, src/background.rs:800-856.
+void mesh_filter(std::vector<double>& bg, std::vector<double>& rms, const std::vector<size_t>& mesh_shape,
+                 const std::vector<size_t>& filter_size, const MeshSpec& spec) {
+  bool off = bg.empty();
+  bool all_one = true;
+  for (size_t f : filter_size) all_one = all_one && f == 1;
+  if (off || all_one) return;
+  const size_t ndim = mesh_shape.size(), len = bg.size();
+  std::vector<double> ob(bg), orms(rms), wb, wr;
+  std::vector<size_t> idx(ndim), low(ndim), high(ndim);
+  for (size_t flat = 0; flat < len; ++flat) {
+    mesh_index(flat, mesh_shape, idx.data());
+    for (size_t a = 0; a < ndim; ++a) {
+      const size_t k = idx[a], n = mesh_shape[a], half = filter_size[a] / 2;
+      if (spec.filter_edge == 0) {
+        const size_t h = std::min(std::min(half, k), n - 1 - k);
+        low[a] = k - h;
+        high[a] = k + h;
+      } else {
+        low[a] = k >= half ? k - half : 0;
+        high[a] = std::min(k + half, n - 1);
+      }
+    }
+    wb.clear();
+    wr.clear();
+    size_t volume = 1;
+    for (size_t a = 0; a < ndim; ++a) volume *= high[a] - low[a] + 1;
+    for (size_t pos = 0; pos < volume; ++pos) {
+      size_t rest = pos, offset = 0, stride = 1;
+      for (size_t a = ndim; a-- > 0;) {
+        const size_t width = high[a] - low[a] + 1;
+        offset += (low[a] + rest % width) * stride;
+        rest /= width;
+        stride *= mesh_shape[a];
+      }
+      wb.push_back(bg[offset]);
+      wr.push_back(rms[offset]);
+    }
+    const double median = mesh_median_of(wb);
+    bool replace = true;
+    if (spec.threshold_kind == 1) replace = std::fabs(median - bg[flat]) >= spec.threshold;
+    if (spec.threshold_kind == 2) replace = bg[flat] > spec.threshold;
+    if (replace) {
+      ob[flat] = median;
+      orms[flat] = mesh_median_of(wr);
+    }
+  }
+  bg.swap(ob);
+  rms.swap(orms);
+}
+
+// Tap, src/background.rs:349-397.
+struct SplineTap {
+  size_t seg;
+  double a, b, c, d;
+};
+
+SplineTap spline_tap(double u, size_t nodes) {
+  if (nodes < 2) return {0, 1.0, 0.0, 0.0, 0.0};
+  const double fl = std::floor(u);
+  size_t seg = fl > 0.0 ? (size_t)fl : 0;
+  seg = std::min(seg, nodes - 2);
+  const double t = u - (double)seg;
+  const double a = 1.0 - t;
+  return {seg, a, t, (a * a * a - a) / 6.0, (t * t * t - t) / 6.0};
+}
+
+// natural_pivots / natural_second_derivatives / columns_second_derivatives,
+// src/background.rs:1154-1212.
+std::vector<double> natural_pivots(size_t nodes) {
+  std::vector<double> p(nodes, 0.0);
+  double previous = 0.0;
+  for (size_t i = 1; i + 1 < nodes; ++i) {
+    p[i] = 1.0 / (4.0 - previous);
+    previous = p[i];
+  }
+  return p;
+}
+
+void columns_second(const double* block, size_t nodes, size_t inner, const std::vector<double>& pivots,
+                    double* second) {
+  std::fill(second, second + nodes * inner, 0.0);
+  if (nodes < 3) return;
+  for (size_t i = 1; i + 1 < nodes; ++i)
+    for (size_t j = 0; j < inner; ++j) {
+      const double rhs = 6.0 * (block[(i - 1) * inner + j] - 2.0 * block[i * inner + j] + block[(i + 1) * inner + j]);
+      second[i * inner + j] = (rhs - second[(i - 1) * inner + j]) * pivots[i];
+    }
+  for (size_t i = nodes - 2; i-- > 1;)
+    for (size_t j = 0; j < inner; ++j) second[i * inner + j] -= pivots[i] * second[(i + 1) * inner + j];
+}
+
+// spline_into, src/background.rs:858-921.
+template <class T>
+void mesh_spline(const std::vector<double>& mesh, const std::vector<size_t>& shape,
+                 const std::vector<size_t>& mesh_shape, const std::vector<size_t>& box, T* out) {
+  const size_t ndim = shape.size();
+  std::vector<double> current(mesh);
+  for (size_t axis = 0; axis < ndim; ++axis) {
+    size_t outer = 1, inner = 1;
+    for (size_t a = 0; a < axis; ++a) outer *= shape[a];
+    for (size_t a = axis + 1; a < ndim; ++a) inner *= mesh_shape[a];
+    const size_t nodes = mesh_shape[axis], length = shape[axis];
+    std::vector<SplineTap> taps(length);
+    for (size_t p = 0; p < length; ++p) taps[p] = spline_tap(((double)p + 0.5) / (double)box[axis] - 0.5, nodes);
+    const std::vector<double> pivots = natural_pivots(nodes);
+    const size_t block = nodes * inner;
+    std::vector<double> second(current.size());
+    for (size_t o = 0; o < outer; ++o)
+      columns_second(&current[o * block], nodes, inner, pivots, &second[o * block]);
+    if (axis + 1 == ndim) {
+      for (size_t line = 0; line < outer; ++line) {
+        const double* y = &current[line * nodes];
+        const double* m = &second[line * nodes];
+        for (size_t p = 0; p < length; ++p) {
+          const SplineTap& t = taps[p];
+          double v;
+          if (nodes < 2)
+            v = y[0];
+          else
+            v = t.a * y[t.seg] + t.b * y[t.seg + 1] + t.c * m[t.seg] + t.d * m[t.seg + 1];
+          out[line * length + p] = (T)v;
+        }
+      }
+      return;
+    }
+    std::vector<double> next(outer * length * inner);
+    for (size_t row = 0; row < outer * length; ++row) {
+      const size_t o = row / length, p = row % length;
+      const SplineTap& t = taps[p];
+      const size_t base = o * block;
+      double* dst = &next[row * inner];
+      if (nodes < 2) {
+        std::copy(&current[base], &current[base] + inner, dst);
+        continue;
+      }
+      const size_t lo = base + t.seg * inner, hi = lo + inner;
+      for (size_t j = 0; j < inner; ++j)
+        dst[j] = t.a * current[lo + j] + t.b * current[hi + j] + t.c * second[lo + j] + t.d * second[hi + j];
+    }
+    current.swap(next);
+  }
+}
+
+// sep_interpolation.rs: SExtractor-compatible 2-D interpolation.
+inline double legacy_phase(double v) { return (double)(float)v; }
+
+std::vector<double> sep_pivots(size_t nodes) {
+  std::vector<double> p(nodes, 0.0);
+  for (size_t i = 1; i + 1 < nodes; ++i) p[i] = 1.0 / (2.0 - 0.25 * p[i - 1]);
+  return p;
+}
+
+void sep_coefficients(const double* values, const std::vector<double>& pivots, size_t lanes, double* coeff) {
+  const size_t n = pivots.size();
+  for (size_t i = 1; i + 1 < n; ++i)
+    for (size_t j = 0; j < lanes; ++j) {
+      const double left = values[(i - 1) * lanes + j], middle = values[i * lanes + j],
+                   right = values[(i + 1) * lanes + j];
+      const double difference = (right - middle) - (middle - left);
+      coeff[i * lanes + j] = std::fma(3.0, difference, -0.5 * coeff[(i - 1) * lanes + j]) * pivots[i];
+    }
+  for (size_t i = n - 1; i-- > 1;) {
+    const double multiplier = -0.5 * pivots[i];
+    for (size_t j = 0; j < lanes; ++j)
+      coeff[i * lanes + j] = std::fma(multiplier, coeff[(i + 1) * lanes + j], coeff[i * lanes + j]) / 6.0;
+  }
+}
+
+struct SepWeight {
+  double fraction, left_curve, right_curve;
+};
+
+template <class T>
+void mesh_sep(const std::vector<double>& mesh, size_t ny, size_t nx, size_t height, size_t width, T* out) {
+  const size_t rows = (ny + height - 1) / height, columns = (nx + width - 1) / width;
+  if (mesh.size() == 1) {
+    for (size_t i = 0; i < ny * nx; ++i) out[i] = (T)mesh[0];
+    return;
+  }
+  double peak = 0.0;
+  for (double v : mesh) peak = std::fmax(peak, std::fabs(v));
+  const double scale = std::fmax(from_bits64(bits64(peak) & 0x7ff0000000000000ull), 2.2250738585072014e-308);
+  const double inverse_scale = 1.0 / scale;
+  std::vector<double> values(mesh.size());
+  for (size_t i = 0; i < mesh.size(); ++i) values[i] = mesh[i] * inverse_scale;
+  // Horizontal::new
+  std::vector<size_t> lengths;
+  std::vector<SepWeight> first, later;
+  const bool have_x = columns > 1;
+  if (have_x) {
+    const double step = legacy_phase(1.0 / legacy_phase((double)width));
+    auto weights = [&](double b, size_t length) {
+      std::vector<SepWeight> w;
+      for (size_t i = 0; i < length; ++i) {
+        const double a = 1.0 - b;
+        w.push_back({b, a * std::fma(a, a, -1.0), b * std::fma(b, b, -1.0)});
+        b = legacy_phase(b + step);
+      }
+      return w;
+    };
+    const size_t intervals = width == 1 ? 1 : columns - 1;
+    size_t start = 0;
+    for (size_t i = 1; i <= intervals; ++i) {
+      const size_t end = i == intervals ? nx : i * width + width / 2;
+      lengths.push_back(end - start);
+      start = end;
+    }
+    first = weights(legacy_phase(0.5 * step - 0.5), lengths[0]);
+    size_t longest = 0;
+    for (size_t i = 1; i < lengths.size(); ++i) longest = std::max(longest, lengths[i]);
+    later = weights(width % 2 == 0 ? 0.5 * step : 0.0, longest);
+  }
+  auto row_out = [&](const double* vals, const double* coeff, auto&& store) {
+    size_t pos = 0;
+    for (size_t i = 0; i < lengths.size(); ++i) {
+      const std::vector<SepWeight>& w = i == 0 ? first : later;
+      const double left = vals[i], right = vals[i + 1], cl = coeff[i], cr = coeff[i + 1];
+      const double slope = right - left;
+      for (size_t k = 0; k < lengths[i]; ++k, ++pos) {
+        const double linear = std::fma(w[k].fraction, slope, left);
+        store(pos, std::fma(w[k].right_curve, cr, std::fma(w[k].left_curve, cl, linear)));
+      }
+    }
+  };
+  if (rows == 1 && have_x) {
+    std::vector<double> zeros(columns, 0.0), profile(nx);
+    row_out(values.data(), zeros.data(), [&](size_t p, double v) { profile[p] = v * scale; });
+    for (size_t y = 0; y < ny; ++y)
+      for (size_t x = 0; x < nx; ++x) out[y * nx + x] = (T)profile[x];
+    return;
+  }
+  std::vector<double> y_coeff(mesh.size(), 0.0);
+  sep_coefficients(values.data(), sep_pivots(rows), columns, y_coeff.data());
+  const std::vector<double> x_pivots = have_x ? sep_pivots(columns) : std::vector<double>();
+  const double phase_height = legacy_phase((double)height);
+  std::vector<double> line(columns), x_coeff(columns);
+  for (size_t y = 0; y < ny; ++y) {
+    const double box_coordinate = legacy_phase(legacy_phase((double)y) / phase_height);
+    const double z = legacy_phase(box_coordinate - 0.5);
+    const size_t i = std::min(z > 0.0 ? (size_t)z : (size_t)0, rows - 2);
+    const double b = z - (double)i, a = 1.0 - b;
+    const double ca = std::fma(a * a, a, -a), cb = std::fma(b * b, b, -b);
+    const double* top = &values[i * columns];
+    const double* bottom = &values[(i + 1) * columns];
+    const double* ct = &y_coeff[i * columns];
+    const double* cbot = &y_coeff[(i + 1) * columns];
+    for (size_t j = 0; j < columns; ++j) {
+      const double linear = std::fma(b, bottom[j] - top[j], top[j]);
+      line[j] = std::fma(cb, cbot[j], std::fma(ca, ct[j], linear));
+    }
+    if (have_x) {
+      std::fill(x_coeff.begin(), x_coeff.end(), 0.0);
+      sep_coefficients(line.data(), x_pivots, 1, x_coeff.data());
+      row_out(line.data(), x_coeff.data(), [&](size_t p, double v) { out[y * nx + p] = (T)(v * scale); });
+    } else {
+      for (size_t x = 0; x < nx; ++x) out[y * nx + x] = (T)(line[0] * scale);
+    }
+  }
+}
+
+template <class T>
+void mesh_interpolate(const std::vector<double>& mesh, const std::vector<size_t>& shape,
+                      const std::vector<size_t>& mesh_shape, const std::vector<size_t>& box, const MeshSpec& spec,
+                      T* out) {
+  size_t len = 1;
+  for (size_t v : shape) len *= v;
+  if (len == 0) return;
+  bool constant = true;
+  for (double v : mesh) constant = constant && v == mesh[0];
+  if (constant) {
+    for (size_t i = 0; i < len; ++i) out[i] = (T)mesh[0];
+    return;
+  }
+  if (spec.interpolation == 0)
+    mesh_spline(mesh, shape, mesh_shape, box, out);
+  else
+    mesh_sep(mesh, shape[0], shape[1], box[0], box[1], out);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -2290,6 +2807,125 @@ int ndfo_robust_filter(int32_t dtype, int32_t rank, const uint64_t* shape, const
     run(float());
   else
     run(double());
+  return kOk;
+}
+
+// MeshBackground::new + estimate + interpolate_into (background and RMS),
+// src/background.rs:445-560. Returns the reference's error classes; outputs
+// are the two full-resolution maps (dtype of the input), the mesh grids
+// (float64, int64 counts, uint8 validity) and the two global medians.
+int ndfo_mesh_background(int32_t dtype, int32_t ndim, const uint64_t* shape, const void* input,
+                         const uint8_t* mask, const uint64_t* box_size, const uint64_t* filter_size,
+                         int32_t estimator, double pearson, double lower, double upper, int64_t maxiters,
+                         int32_t center, int32_t spread, int32_t statistic, int32_t mode_estimator,
+                         int32_t rms_kind, double min_valid_fraction, int32_t valid_count, int32_t valid_base,
+                         int32_t fill, uint64_t idw_neighbors, double idw_power, int32_t filter_edge,
+                         int32_t threshold_kind, double threshold, int32_t interpolation, void* out_background,
+                         void* out_rms, double* mesh_background, double* mesh_rms, uint8_t* mesh_valid,
+                         int64_t* finite_count, int64_t* retained_count, double* globals) {
+  if (ndim <= 0) return fail(kInvalid, "shape must have at least one axis");
+  for (int a = 0; a < ndim; ++a)
+    if (box_size[a] == 0) return fail(kInvalid, "box sizes must be positive");
+  for (int a = 0; a < ndim; ++a)
+    if (filter_size[a] % 2 == 0) return fail(kInvalid, "filter sizes must be odd and positive");
+  MeshSpec spec;
+  spec.estimator = estimator;
+  spec.pearson = pearson;
+  spec.lower = lower;
+  spec.upper = upper;
+  spec.maxiters = maxiters;
+  spec.center = center;
+  spec.spread = spread;
+  spec.statistic = statistic;
+  spec.mode_estimator = mode_estimator;
+  spec.rms = rms_kind;
+  spec.min_valid_fraction = min_valid_fraction;
+  spec.valid_count = valid_count;
+  spec.valid_base = valid_base;
+  spec.fill = fill;
+  spec.idw_neighbors = idw_neighbors;
+  spec.idw_power = idw_power;
+  spec.filter_edge = filter_edge;
+  spec.threshold_kind = threshold_kind;
+  spec.threshold = threshold;
+  spec.interpolation = interpolation;
+  // MeshConfig::validate, src/background.rs:230-289.
+  if (!(std::isfinite(pearson) && pearson >= 1.0))
+    return fail(kInvalid, "pearson must be finite and at least one");
+  if (estimator == 1 && (!std::isfinite(lower) || !std::isfinite(upper) || lower < 0.0 || upper < 0.0))
+    return fail(kInvalid, "clipping limits must be finite and nonnegative");
+  if (!(min_valid_fraction >= 0.0 && min_valid_fraction <= 1.0))
+    return fail(kInvalid, "minimum valid fraction must be between zero and one");
+  if (fill == 1 && (idw_neighbors == 0 || !std::isfinite(idw_power) || idw_power < 0.0))
+    return fail(kInvalid,
+                "inverse-distance fill needs at least one neighbor and a finite nonnegative power");
+  if (threshold_kind != 0 && !std::isfinite(threshold)) return fail(kInvalid, "filter threshold must be finite");
+  if (interpolation == 1 && ndim != 2) return fail(kInvalid, "SExtractor interpolation needs a 2-D shape");
+  std::vector<size_t> sh(shape, shape + ndim), box(box_size, box_size + ndim), filt(filter_size, filter_size + ndim),
+      mesh_shape(ndim);
+  size_t len = 1, mesh_len = 1;
+  uint64_t box_volume = 1;
+  for (int a = 0; a < ndim; ++a) {
+    mesh_shape[a] = (sh[a] + box[a] - 1) / box[a];
+    len *= sh[a];
+    mesh_len *= mesh_shape[a];
+    if (box[a] != 0 && box_volume > UINT64_MAX / box[a]) return fail(kOverflow, "box volume overflowed");
+    box_volume *= box[a];
+  }
+  std::vector<MeshStat> stats(mesh_len);
+  std::vector<size_t> idx(ndim);
+  for (size_t mesh = 0; mesh < mesh_len; ++mesh) {
+    mesh_index(mesh, mesh_shape, idx.data());
+    std::vector<size_t> start(ndim), stop(ndim);
+    uint64_t volume = 1;
+    for (int a = 0; a < ndim; ++a) {
+      start[a] = idx[a] * box[a];
+      stop[a] = std::min(start[a] + box[a], sh[a]);
+      volume *= stop[a] - start[a];
+    }
+    std::vector<double> values;
+    std::vector<size_t> pos(start);
+    if (volume > 0) {
+      while (true) {
+        size_t offset = 0;
+        for (int a = 0; a < ndim; ++a) offset = offset * sh[a] + pos[a];
+        const double v = dtype == 0 ? (double)((const float*)input)[offset] : ((const double*)input)[offset];
+        if (std::isfinite(v) && !(mask && mask[offset])) values.push_back(v);
+        int a = ndim - 1;
+        for (; a >= 0; --a) {
+          if (++pos[a] < stop[a]) break;
+          pos[a] = start[a];
+        }
+        if (a < 0) break;
+      }
+    }
+    stats[mesh] = mesh_finish(values, volume, box_volume, spec);
+  }
+  std::vector<double> bg(mesh_len), rms(mesh_len);
+  std::vector<bool> valid(mesh_len);
+  for (size_t i = 0; i < mesh_len; ++i) {
+    bg[i] = stats[i].background;
+    rms[i] = stats[i].rms;
+    valid[i] = stats[i].valid;
+  }
+  mesh_fill(bg, rms, valid, mesh_shape, spec);
+  mesh_filter(bg, rms, mesh_shape, filt, spec);
+  for (size_t i = 0; i < mesh_len; ++i) {
+    mesh_background[i] = bg[i];
+    mesh_rms[i] = rms[i];
+    mesh_valid[i] = valid[i] ? 1 : 0;
+    finite_count[i] = (int64_t)stats[i].finite;
+    retained_count[i] = (int64_t)stats[i].retained;
+  }
+  globals[0] = mesh_median_of(bg);
+  globals[1] = mesh_median_of(rms);
+  if (dtype == 0) {
+    mesh_interpolate(bg, sh, mesh_shape, box, spec, (float*)out_background);
+    mesh_interpolate(rms, sh, mesh_shape, box, spec, (float*)out_rms);
+  } else {
+    mesh_interpolate(bg, sh, mesh_shape, box, spec, (double*)out_background);
+    mesh_interpolate(rms, sh, mesh_shape, box, spec, (double*)out_rms);
+  }
   return kOk;
 }
 
