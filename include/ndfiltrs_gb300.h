@@ -128,6 +128,75 @@ int ndf_robust_filter(const void* h_in, void* h_out, int32_t dtype, int32_t ndim
                       const char* spread, const char* estimator, int32_t modify_sample_size,
                       double pearson);
 
+/* ---- Mesh background: MeshBackground (src/background.rs:31-923) and
+ * `_core.mesh_background` (src/pyapi/background.rs:225-280). The rule set of
+ * MeshConfig (src/background.rs:144-289), numbered as below. */
+#define NDF_MESH_ESTIMATOR_SEXTRACTOR 0
+#define NDF_MESH_ESTIMATOR_SIGMA_CLIP 1
+#define NDF_MESH_STATISTIC_MEAN 0
+#define NDF_MESH_STATISTIC_MEDIAN 1
+#define NDF_MESH_STATISTIC_MODE 2
+#define NDF_MESH_RMS_STD 0
+#define NDF_MESH_RMS_MAD_STD 1
+#define NDF_MESH_VALID_FINITE 0
+#define NDF_MESH_VALID_RETAINED 1
+#define NDF_MESH_BASE_MESH 0
+#define NDF_MESH_BASE_BOX 1
+#define NDF_MESH_FILL_NEAREST 0
+#define NDF_MESH_FILL_IDW 1
+#define NDF_MESH_EDGE_SHRINK 0
+#define NDF_MESH_EDGE_TRUNCATE 1
+#define NDF_MESH_THRESHOLD_ALL 0
+#define NDF_MESH_THRESHOLD_DEVIATION 1
+#define NDF_MESH_THRESHOLD_ABOVE 2
+#define NDF_MESH_INTERP_SPLINE 0
+#define NDF_MESH_INTERP_SEXTRACTOR 1
+
+typedef struct ndf_mesh_config {
+  int32_t estimator;          /* NDF_MESH_ESTIMATOR_* */
+  double pearson;             /* mode rule factor (>= 1) */
+  double sigma_lower;         /* sigma clip: multipliers (>= 0) */
+  double sigma_upper;
+  int64_t maxiters;           /* sigma clip: passes; < 0: until stable */
+  int32_t center;             /* NDF_CLIP_CENTER_* */
+  int32_t spread;             /* NDF_CLIP_SPREAD_* */
+  int32_t statistic;          /* NDF_MESH_STATISTIC_* */
+  int32_t mode_estimator;     /* NDF_MODE_ESTIMATOR_* */
+  int32_t rms;                /* NDF_MESH_RMS_* */
+  double min_valid_fraction;  /* [0, 1] */
+  int32_t valid_count;        /* NDF_MESH_VALID_* */
+  int32_t valid_base;         /* NDF_MESH_BASE_* */
+  int32_t fill;               /* NDF_MESH_FILL_* */
+  uint64_t idw_neighbors;     /* >= 1 */
+  double idw_power;           /* finite, >= 0 */
+  int32_t filter_edge;        /* NDF_MESH_EDGE_* */
+  int32_t threshold_kind;     /* NDF_MESH_THRESHOLD_* */
+  double threshold;           /* finite unless NDF_MESH_THRESHOLD_ALL */
+  int32_t interpolation;      /* NDF_MESH_INTERP_* */
+} ndf_mesh_config;
+
+/* Replaces `_core.mesh_background(array, mask, box_size, filter_size, ...)`:
+ * per-mesh statistics on the GPU, fill and median filter of the mesh grid,
+ * and the full-resolution background and RMS maps (dtype of the input) on the
+ * GPU. `h_mask` is NULL or prod(shape) bytes (nonzero excludes the sample).
+ * Mesh outputs have prod(ceil(shape / box_size)) entries; `globals` receives
+ * the global background and RMS. */
+int ndf_mesh_background(const void* h_in, const uint8_t* h_mask, int32_t dtype, int32_t ndim,
+                        const uint64_t* shape, const uint64_t* box_size, const uint64_t* filter_size,
+                        const ndf_mesh_config* config, void* h_background, void* h_rms,
+                        double* mesh_background, double* mesh_rms, uint8_t* mesh_valid,
+                        int64_t* mesh_finite_count, int64_t* mesh_retained_count, double* globals);
+
+/* The same pipeline over device buffers (`d_mask` may be NULL), enqueued on
+ * `stream`; the call synchronizes once between the mesh statistics and the
+ * host-side fill / filter and returns after enqueuing the interpolation. */
+int ndf_mesh_background_device(const void* d_in, const uint8_t* d_mask, int32_t dtype, int32_t ndim,
+                               const uint64_t* shape, const uint64_t* box_size,
+                               const uint64_t* filter_size, const ndf_mesh_config* config,
+                               void* d_background, void* d_rms, double* mesh_background,
+                               double* mesh_rms, uint8_t* mesh_valid, int64_t* mesh_finite_count,
+                               int64_t* mesh_retained_count, double* globals, void* stream);
+
 /* Replaces `_core.get_num_threads()`, src/pyapi/filter.rs:378-380. Returns
  * the number of streaming multiprocessors of the current device (the
  * library's unit of parallelism), or 0 without a device. */

@@ -4,10 +4,10 @@ A drop-in for the windowed-statistics path of ndfiltrs (ysBach/ndfiltrs
 v0.2.0): NaN-aware median, rank and percentile filters (direct, sortnet and
 histogram methods), the mean/var/std footprint reductions, exact rolling
 means, separable min/max and the robust family (MAD, sigma clipping, mode,
-biweight), for every footprint, origin and boundary mode. The public
-functions keep the reference's signatures and NaN/inf/min_count semantics;
-all computation runs on the GPU through the C-ABI library
-``libndfiltrs_gb300.so``.
+biweight), for every footprint, origin and boundary mode, and the mesh
+background built on them. The public functions keep the reference's
+signatures and NaN/inf/min_count semantics; all computation runs on the GPU
+through the C-ABI library ``libndfiltrs_gb300.so``.
 """
 
 from . import kernels
@@ -27,6 +27,7 @@ from ._api import (
     std_filter,
     var_filter,
 )
+from ._background import MeshBackground, mesh_background
 from ._core import Batch, Plan, autotune_entries, device_info, set_autotune
 from ._robust import (
     biweight_location_filter,
@@ -52,6 +53,8 @@ __all__ = [
     "get_num_threads",
     "kernels",
     "mad_filter",
+    "mesh_background",
+    "MeshBackground",
     "max_filter",
     "mean_filter",
     "median_filter",

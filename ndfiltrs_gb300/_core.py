@@ -87,6 +87,31 @@ class RobustParams(ctypes.Structure):
     ]
 
 
+class MeshConfig(ctypes.Structure):
+    _fields_ = [
+        ("estimator", ctypes.c_int32),
+        ("pearson", ctypes.c_double),
+        ("sigma_lower", ctypes.c_double),
+        ("sigma_upper", ctypes.c_double),
+        ("maxiters", ctypes.c_int64),
+        ("center", ctypes.c_int32),
+        ("spread", ctypes.c_int32),
+        ("statistic", ctypes.c_int32),
+        ("mode_estimator", ctypes.c_int32),
+        ("rms", ctypes.c_int32),
+        ("min_valid_fraction", ctypes.c_double),
+        ("valid_count", ctypes.c_int32),
+        ("valid_base", ctypes.c_int32),
+        ("fill", ctypes.c_int32),
+        ("idw_neighbors", ctypes.c_uint64),
+        ("idw_power", ctypes.c_double),
+        ("filter_edge", ctypes.c_int32),
+        ("threshold_kind", ctypes.c_int32),
+        ("threshold", ctypes.c_double),
+        ("interpolation", ctypes.c_int32),
+    ]
+
+
 class FilterDesc(ctypes.Structure):
     """``ndf_filter_desc`` of include/ndfiltrs_gb300.h."""
 
@@ -179,6 +204,17 @@ def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
                 handle.ndf_autotune_entries.restype = ctypes.c_int32
                 handle.ndf_pin_kernel.argtypes = [ctypes.c_char_p]
                 handle.ndf_pin_kernel.restype = ctypes.c_int
+                dp = ctypes.POINTER(ctypes.c_double)
+                i64p = ctypes.POINTER(ctypes.c_int64)
+                u8p = ctypes.POINTER(ctypes.c_uint8)
+                u64p = ctypes.POINTER(ctypes.c_uint64)
+                mesh_tail = [ctypes.POINTER(MeshConfig), vp, vp, dp, dp, u8p, i64p, i64p, dp]
+                handle.ndf_mesh_background.argtypes = [vp, u8p, ctypes.c_int32, ctypes.c_int32, u64p, u64p,
+                                                       u64p] + mesh_tail
+                handle.ndf_mesh_background.restype = ctypes.c_int
+                handle.ndf_mesh_background_device.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, u64p,
+                                                              u64p, u64p] + mesh_tail + [vp]
+                handle.ndf_mesh_background_device.restype = ctypes.c_int
                 handle.ndf_set_tma.argtypes = [ctypes.c_int32]
                 handle.ndf_set_tma.restype = ctypes.c_int
                 handle.ndf_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
@@ -567,6 +603,98 @@ def robust_filter(
         robust=options,
     ) as plan:
         return plan.run_host(array)
+
+
+def _unsupported(name: str) -> ValueError:
+    return ValueError(f"unsupported {name}")
+
+
+def mesh_config(estimator, sigma_lower, sigma_upper, maxiters, center, spread, statistic, mode_estimator,
+                pearson, rms, min_valid_fraction, valid_count, valid_base, fill, idw_neighbors, idw_power,
+                filter_edge, filter_threshold, threshold_kind, interpolation) -> MeshConfig:
+    """The MeshConfig of src/pyapi/background.rs:42-123 (string options parsed
+    in the same order, with the same messages)."""
+    choices = {
+        "estimator": {"sextractor": 0, "sigma_clip": 1},
+        "valid_count": {"finite": 0, "retained": 1},
+        "valid_base": {"mesh": 0, "box": 1},
+        "fill": {"nearest": 0, "idw": 1},
+        "filter_edge": {"shrink": 0, "truncate": 1},
+        "interpolation": {"spline": 0, "sextractor": 1},
+    }
+
+    def pick(name, value, table):
+        if value not in table:
+            raise _unsupported(name)
+        return table[value]
+
+    est = pick("estimator", estimator, choices["estimator"])
+    mode_code, center_code, spread_code, statistic_code, rms_code = 0, 1, 0, 2, 0
+    if est == 1:
+        mode_code = pick("mode_estimator", mode_estimator, ESTIMATORS)
+        center_code = pick("center", center, CENTERS)
+        spread_code = pick("spread", spread, SPREADS)
+        statistic_code = pick("statistic", statistic, {"mean": 0, "median": 1, "mode": 2})
+        rms_code = pick("rms", rms, {"std": 0, "mad": 1})
+    count = pick("valid_count", valid_count, choices["valid_count"])
+    base = pick("valid_base", valid_base, choices["valid_base"])
+    fill_code = pick("fill", fill, choices["fill"])
+    edge = pick("filter_edge", filter_edge, choices["filter_edge"])
+    if threshold_kind not in ("deviation", "above"):
+        raise _unsupported("threshold_kind")
+    kind = 0 if filter_threshold is None else (1 if threshold_kind == "deviation" else 2)
+    interp = pick("interpolation", interpolation, choices["interpolation"])
+    return MeshConfig(est, float(pearson), float(sigma_lower), float(sigma_upper),
+                      -1 if maxiters is None else int(maxiters), center_code, spread_code, statistic_code,
+                      mode_code, rms_code, float(min_valid_fraction), count, base, fill_code, int(idw_neighbors),
+                      float(idw_power), edge, kind, 0.0 if filter_threshold is None else float(filter_threshold),
+                      interp)
+
+
+def mesh_background(array, mask, box_size, filter_size, estimator, sigma_lower, sigma_upper, maxiters, center,
+                    spread, statistic, mode_estimator, pearson, rms, min_valid_fraction, valid_count, valid_base,
+                    fill, idw_neighbors, idw_power, filter_edge, filter_threshold, threshold_kind, interpolation):
+    """``_core.mesh_background`` (src/pyapi/background.rs:225-280): returns
+    (background, rms, mesh_background, mesh_rms, mesh_valid,
+    mesh_finite_count, mesh_retained_count, global_background, global_rms)."""
+    lib, _ = _load()
+    config = mesh_config(estimator, sigma_lower, sigma_upper, maxiters, center, spread, statistic, mode_estimator,
+                         pearson, rms, min_valid_fraction, valid_count, valid_base, fill, idw_neighbors, idw_power,
+                         filter_edge, filter_threshold, threshold_kind, interpolation)
+    array = _typed_array(array)
+    if not array.flags.c_contiguous or not array.flags.aligned:
+        raise ValueError("native input must be aligned and C-contiguous")
+    shape = array.shape
+    ndim = len(shape)
+    boxes, filters = list(box_size), list(filter_size)
+    if len(boxes) != ndim or len(filters) != ndim:
+        raise ValueError("box and filter sizes need one entry per axis")
+    if any(int(b) == 0 for b in boxes):
+        raise ValueError("box sizes must be positive")
+    mesh_shape = tuple(-(-int(n) // int(b)) for n, b in zip(shape, boxes))
+    flags = None
+    if mask is not None:
+        flags = np.ascontiguousarray(mask, dtype=np.uint8)
+        if flags.shape != shape:
+            raise ValueError("mask must have the same shape as data")
+    background = np.zeros(shape, dtype=array.dtype)
+    rms_map = np.zeros(shape, dtype=array.dtype)
+    mesh_bg = np.zeros(mesh_shape, np.float64)
+    mesh_rms = np.zeros(mesh_shape, np.float64)
+    valid = np.zeros(mesh_shape, np.uint8)
+    finite = np.zeros(mesh_shape, np.int64)
+    retained = np.zeros(mesh_shape, np.int64)
+    globals_ = np.zeros(2, np.float64)
+    ptr = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    _check(lib.ndf_mesh_background(
+        array.ctypes.data_as(ctypes.c_void_p), None if flags is None else ptr(flags, ctypes.c_uint8),
+        0 if array.dtype == np.float32 else 1, ndim, _u64(shape), _u64(boxes), _u64(filters),
+        ctypes.byref(config), background.ctypes.data_as(ctypes.c_void_p),
+        rms_map.ctypes.data_as(ctypes.c_void_p), ptr(mesh_bg, ctypes.c_double), ptr(mesh_rms, ctypes.c_double),
+        ptr(valid, ctypes.c_uint8), ptr(finite, ctypes.c_int64), ptr(retained, ctypes.c_int64),
+        ptr(globals_, ctypes.c_double)), lib)
+    return (background, rms_map, mesh_bg, mesh_rms, valid.astype(bool), finite, retained, float(globals_[0]),
+            float(globals_[1]))
 
 
 def get_num_threads() -> int:

@@ -814,6 +814,9 @@ int one_shot(const ndf_filter_desc& d, const void* h_in, void* h_out) {
 
 }  // namespace
 
+// Device check for translation units without plans (mesh.cu).
+int device_ready(int* device, int* sm_count, int* smem_optin) { return ensure_device(device, sm_count, smem_optin); }
+
 // Plan construction for the batched path (batch.cu).
 int batch_build_plan(const ndf_filter_desc* d, Plan& p, int* smem_limit) {
   int rc = build_plan(d, p);

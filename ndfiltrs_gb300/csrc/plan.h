@@ -222,6 +222,9 @@ cudaError_t launch_extrema(const Plan& p, const void* in, void* out, cudaStream_
 bool extrema_configure(Plan& p, int smem_limit);
 bool extrema_passes_configure(Plan& p, int smem_limit);
 bool robust_configure(Plan& p);
+int device_ready(int* device, int* sm_count, int* smem_optin);
+int fail(int code, const std::string& message);
+int cuda_fail(cudaError_t e, const char* what);
 cudaError_t launch_robust(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool boxcar_configure(Plan& p, int smem_limit);
 bool boxcar_band_configure(Plan& p, int smem_limit);

@@ -2822,7 +2822,7 @@ int ndfo_mesh_background(int32_t dtype, int32_t ndim, const uint64_t* shape, con
                          int32_t fill, uint64_t idw_neighbors, double idw_power, int32_t filter_edge,
                          int32_t threshold_kind, double threshold, int32_t interpolation, void* out_background,
                          void* out_rms, double* mesh_background, double* mesh_rms, uint8_t* mesh_valid,
-                         int64_t* finite_count, int64_t* retained_count, double* globals) {
+                         int64_t* finite_count, int64_t* retained_count, double* globals, int32_t threads) {
   if (ndim <= 0) return fail(kInvalid, "shape must have at least one axis");
   for (int a = 0; a < ndim; ++a)
     if (box_size[a] == 0) return fail(kInvalid, "box sizes must be positive");
@@ -2873,8 +2873,10 @@ int ndfo_mesh_background(int32_t dtype, int32_t ndim, const uint64_t* shape, con
     box_volume *= box[a];
   }
   std::vector<MeshStat> stats(mesh_len);
+  // Meshes in parallel, as the reference's estimate (src/background.rs:533-541).
+  run_parallel(mesh_len, threads, [&](size_t first_mesh, size_t end_mesh) {
   std::vector<size_t> idx(ndim);
-  for (size_t mesh = 0; mesh < mesh_len; ++mesh) {
+  for (size_t mesh = first_mesh; mesh < end_mesh; ++mesh) {
     mesh_index(mesh, mesh_shape, idx.data());
     std::vector<size_t> start(ndim), stop(ndim);
     uint64_t volume = 1;
@@ -2901,6 +2903,7 @@ int ndfo_mesh_background(int32_t dtype, int32_t ndim, const uint64_t* shape, con
     }
     stats[mesh] = mesh_finish(values, volume, box_volume, spec);
   }
+  });
   std::vector<double> bg(mesh_len), rms(mesh_len);
   std::vector<bool> valid(mesh_len);
   for (size_t i = 0; i < mesh_len; ++i) {

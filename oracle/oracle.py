@@ -127,6 +127,16 @@ def lib() -> ctypes.CDLL:
             ctypes.c_double, ctypes.c_int32,
         ] + robust_args + [ctypes.c_int32]
         handle.ndfo_robust_filter.restype = ctypes.c_int
+        handle.ndfo_mesh_background.argtypes = [
+            ctypes.c_int32, ctypes.c_int32, u64p, vp, u8p, u64p, u64p,
+            ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+            ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
+            ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+            vp, vp, dptr, dptr, u8p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), dptr,
+            ctypes.c_int32,
+        ]
+        handle.ndfo_mesh_background.restype = ctypes.c_int
         _lib = handle
     return _lib
 
@@ -282,6 +292,61 @@ def robust_filter(array: np.ndarray, kind: str, size=3, *, footprint=None, origi
     if rc != 0:
         raise OracleError(rc, lib().ndfo_last_error().decode())
     return out
+
+
+MESH_DEFAULTS = dict(
+    estimator="sextractor", sigma_lower=3.0, sigma_upper=3.0, maxiters=10, center="median", spread="std",
+    statistic="mode", mode_estimator="sex", pearson=2.5, rms="std", min_valid_fraction=0.5,
+    valid_count="finite", valid_base="mesh", fill="nearest", idw_neighbors=10, idw_power=1.0,
+    filter_edge="shrink", filter_threshold=None, threshold_kind="deviation", interpolation="spline",
+)
+
+
+def mesh_background(data: np.ndarray, box_size, filter_size=3, mask=None, threads: int | None = None, **options):
+    """MeshBackground::new + estimate + interpolate_into (src/background.rs).
+
+    Returns (background, rms, mesh_background, mesh_rms, mesh_valid,
+    mesh_finite_count, mesh_retained_count, global_background, global_rms)
+    like the reference's ``_core.mesh_background``.
+    """
+    o = dict(MESH_DEFAULTS, **options)
+    data = np.ascontiguousarray(data)
+    ndim = data.ndim
+    boxes = (int(box_size),) * ndim if np.ndim(box_size) == 0 else tuple(int(b) for b in box_size)
+    filters = (int(filter_size),) * ndim if np.ndim(filter_size) == 0 else tuple(int(f) for f in filter_size)
+    mesh_shape = tuple(-(-n // b) for n, b in zip(data.shape, boxes)) if all(b > 0 for b in boxes) else data.shape
+    background = np.empty_like(data)
+    rms = np.empty_like(data)
+    mb = np.empty(mesh_shape, np.float64)
+    mr = np.empty(mesh_shape, np.float64)
+    mv = np.empty(mesh_shape, np.uint8)
+    fc = np.empty(mesh_shape, np.int64)
+    rc_ = np.empty(mesh_shape, np.int64)
+    globals_ = np.empty(2, np.float64)
+    flags = None if mask is None else np.ascontiguousarray(np.asarray(mask) != 0, dtype=np.uint8)
+    threshold = o["filter_threshold"]
+    kind = 0 if threshold is None else {"deviation": 1, "above": 2}[o["threshold_kind"]]
+    pointer = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    rc = lib().ndfo_mesh_background(
+        0 if data.dtype == np.float32 else 1, ndim, _arr([int(v) for v in data.shape], ctypes.c_uint64),
+        data.ctypes.data_as(ctypes.c_void_p), None if flags is None else pointer(flags, ctypes.c_uint8),
+        _arr(list(boxes), ctypes.c_uint64), _arr(list(filters), ctypes.c_uint64),
+        {"sextractor": 0, "sigma_clip": 1}[o["estimator"]], float(o["pearson"]), float(o["sigma_lower"]),
+        float(o["sigma_upper"]), -1 if o["maxiters"] is None else int(o["maxiters"]),
+        {"mean": 0, "median": 1}[o["center"]], {"std": 0, "mad": 1}[o["spread"]],
+        {"mean": 0, "median": 1, "mode": 2}[o["statistic"]], ESTIMATORS[o["mode_estimator"]],
+        {"std": 0, "mad": 1}[o["rms"]], float(o["min_valid_fraction"]),
+        {"finite": 0, "retained": 1}[o["valid_count"]], {"mesh": 0, "box": 1}[o["valid_base"]],
+        {"nearest": 0, "idw": 1}[o["fill"]], int(o["idw_neighbors"]), float(o["idw_power"]),
+        {"shrink": 0, "truncate": 1}[o["filter_edge"]], kind, 0.0 if threshold is None else float(threshold),
+        {"spline": 0, "sextractor": 1}[o["interpolation"]],
+        background.ctypes.data_as(ctypes.c_void_p), rms.ctypes.data_as(ctypes.c_void_p),
+        pointer(mb, ctypes.c_double), pointer(mr, ctypes.c_double), pointer(mv, ctypes.c_uint8),
+        pointer(fc, ctypes.c_int64), pointer(rc_, ctypes.c_int64), pointer(globals_, ctypes.c_double),
+        int(threads or default_threads()))
+    if rc != 0:
+        raise OracleError(rc, lib().ndfo_last_error().decode())
+    return (background, rms, mb, mr, mv.astype(bool), fc, rc_, float(globals_[0]), float(globals_[1]))
 
 
 def exact_moments(
