@@ -203,6 +203,12 @@ MEASURED_TRAFFIC = {
 }
 
 
+# Kernels of this library one filter call launches, per algorithm (the band
+# and tiled exact means add a wider pass and the direct pass for bands or
+# tiles their words cannot hold; the separable extrema run two passes).
+LAUNCHES_PER_CALL = {"boxcar_band": 3, "boxcar_tile": 2, "extrema_passes": 2}
+
+
 def oracle_kind(kind: str) -> str:
     return kind
 
@@ -1003,7 +1009,7 @@ def main() -> None:
             },
             "cpu_baseline": base,
             "clocks": clocks.summary(),
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * LAUNCHES_PER_CALL.get(plan.algorithm, 1),
             "nanstd_precision": precision,
             "parity_check_rows64": check,
         }

@@ -10,14 +10,17 @@
 // reference writes mul_add), so results equal the reference bit for bit.
 //
 // GB300 design:
-//  * mesh_stats_kernel: one 128-thread block per mesh (grid-stride over
-//    meshes). The block gathers the mesh's finite, unmasked samples as
-//    order-preserving 64-bit keys into shared memory (global scratch for
-//    meshes beyond 8192 samples), bitonic-sorts them, and one thread runs the
-//    SExtractor or sigma-clip sequence over the sorted samples: the reference
-//    accumulates Neumaier sums in sorted order, an order a parallel reduction
-//    would not keep, so the per-mesh statistics are one sequential chain and
-//    the GPU's parallelism is across meshes;
+//  * mesh_sort_kernel: one 128-thread block per mesh (grid-stride over
+//    meshes) gathers the mesh's finite, unmasked samples as order-preserving
+//    64-bit keys into shared memory (global scratch for meshes beyond 8192
+//    samples), bitonic-sorts them and stores the sorted float64 samples,
+//    32 meshes interleaved;
+//  * mesh_finish_kernel: one thread per mesh runs the SExtractor or
+//    sigma-clip sequence over its sorted samples. The reference accumulates
+//    Neumaier sums in sorted order, an order a parallel reduction would not
+//    keep, so each mesh is one sequential float64 chain; giving every mesh
+//    its own lane keeps all 32 lanes of each FP64 instruction busy (the GB300
+//    FP64 pipe is narrow, and a one-lane chain would waste 31 of them);
 //  * fill, median filter and the global medians run on the host over the
 //    small mesh grid;
 //  * the maps: the natural spline is a tensor product, one axis per pass
@@ -49,6 +52,7 @@ struct MeshArgs {
   long long shape[kMaxMeshRank], box[kMaxMeshRank], mesh_shape[kMaxMeshRank];
   long long mesh_len;
   long long capacity;  // keys per block in `scratch` (0: shared memory)
+  long long cap;       // samples per mesh in the sorted buffer (largest mesh volume)
   long long box_volume;
   int estimator, center, spread, statistic, mode_estimator, rms, valid_count, valid_base;
   long long maxiters;
@@ -71,8 +75,17 @@ __device__ __forceinline__ double mval(unsigned long long k) {
   return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
 }
 
+// A mesh's sorted samples: element i at p[i * stride] (meshes of one warp
+// interleave, so the lanes of a warp read neighbouring addresses).
+struct SV {
+  const double* p;
+  long long stride;
+  __device__ __forceinline__ double operator[](long long i) const { return p[i * stride]; }
+  __device__ __forceinline__ SV at(long long k) const { return {p + k * stride, stride}; }
+};
+
 // median_sorted, src/background.rs:950-963.
-__device__ double m_median(const double* v, long long n) {
+__device__ double m_median(SV v, long long n) {
   if (n % 2 == 1) return v[n / 2];
   const double a = v[n / 2 - 1], b = v[n / 2];
   const double mid = __ddiv_rn(__dadd_rn(a, b), 2.0);
@@ -80,7 +93,7 @@ __device__ double m_median(const double* v, long long n) {
 }
 
 // mean_of, src/background.rs:965-978 (mean_valid on overflow).
-__device__ double m_mean(const double* v, long long n) {
+__device__ double m_mean(SV v, long long n) {
   Sum64 sum;
   for (long long i = 0; i < n; ++i) sum.add(v[i]);
   const double total = sum.total();
@@ -91,7 +104,7 @@ __device__ double m_mean(const double* v, long long n) {
 }
 
 // std_about, src/background.rs:1000-1015.
-__device__ double m_std(const double* v, long long n, double mean) {
+__device__ double m_std(SV v, long long n, double mean) {
   if (n == 0) return nan_of(0.0);
   const double scale = fmax(fabs(__dsub_rn(v[0], mean)), fabs(__dsub_rn(v[n - 1], mean)));
   if (scale == 0.0) return 0.0;
@@ -107,7 +120,7 @@ __device__ double m_std(const double* v, long long n, double mean) {
 // mad_std, src/background.rs:1017-1022: the median of |v - median| over
 // sorted v, merged outwards from the smallest deviation (they ascend on both
 // sides), divided by Phi^-1(0.75).
-__device__ double m_mad_std(const double* v, long long n, double median) {
+__device__ double m_mad_std(SV v, long long n, double median) {
   long long right = 0;
   while (right < n && __dsub_rn(v[right], median) < 0.0) ++right;
   long long left = right;
@@ -128,7 +141,7 @@ __device__ double m_mad_std(const double* v, long long n, double median) {
 }
 
 // within, src/background.rs:1024-1032 (two binary searches).
-__device__ void m_within(const double* v, long long r0, long long r1, double low, double high, long long& lo,
+__device__ void m_within(SV v, long long r0, long long r1, double low, double high, long long& lo,
                          long long& hi) {
   long long a = r0, b = r1;
   while (a < b) {
@@ -146,11 +159,11 @@ __device__ void m_within(const double* v, long long r0, long long r1, double low
 }
 
 // clip_sorted, src/background.rs:1034-1069.
-__device__ void m_clip(const double* v, long long& r0, long long& r1, double lower, double upper,
+__device__ void m_clip(SV v, long long& r0, long long& r1, double lower, double upper,
                        long long maxiters, int center, int spread) {
   long long iteration = 0;
   while (r1 - r0 >= 1 && (maxiters < 0 || iteration < maxiters)) {
-    const double* kept = v + r0;
+    const SV kept = v.at(r0);
     const long long n = r1 - r0;
     const double middle = center == 0 ? m_mean(kept, n) : m_median(kept, n);
     const double width = spread == 0 ? m_std(kept, n, m_mean(kept, n)) : m_mad_std(kept, n, m_median(kept, n));
@@ -175,7 +188,7 @@ __device__ double m_mode(double mean, double median, double sd, int estimator, d
 }
 
 // finish_stats with sextractor_stats / clipped_stats, src/background.rs:652-705, 1071-1152.
-__device__ void m_finish(const double* v, long long n, long long volume, const MeshArgs& a, const MeshOut& o,
+__device__ void m_finish(SV v, long long n, long long volume, const MeshArgs& a, const MeshOut& o,
                          long long mesh) {
   double background = nan_of(0.0), rms = nan_of(0.0);
   long long retained = 0;
@@ -186,13 +199,13 @@ __device__ void m_finish(const double* v, long long n, long long volume, const M
       long long f0, f1;
       m_within(v, 0, n, __dsub_rn(mean, __dmul_rn(2.0, sd)), __dadd_rn(mean, __dmul_rn(2.0, sd)), f0, f1);
       if (f0 != f1) {
-        const double mean2 = m_mean(v + f0, f1 - f0);
-        const double sd2 = m_std(v + f0, f1 - f0, mean2);
+        const double mean2 = m_mean(v.at(f0), f1 - f0);
+        const double sd2 = m_std(v.at(f0), f1 - f0, mean2);
         long long s0, s1;
         m_within(v, 0, n, __dsub_rn(mean2, __dmul_rn(5.0, sd2)), __dadd_rn(mean2, __dmul_rn(5.0, sd2)), s0, s1);
         m_clip(v, s0, s1, 3.0, 3.0, 100, 1, 0);
         if (s0 != s1) {
-          const double* k = v + s0;
+          const SV k = v.at(s0);
           const long long c = s1 - s0;
           const double mean3 = m_mean(k, c);
           const double sd3 = m_std(k, c, mean3);
@@ -206,7 +219,7 @@ __device__ void m_finish(const double* v, long long n, long long volume, const M
       m_clip(v, r0, r1, a.lower, a.upper, a.maxiters, a.center, a.spread);
       retained = r1 - r0;
       if (retained > 0) {
-        const double* k = v + r0;
+        const SV k = v.at(r0);
         const double mean = m_mean(k, retained);
         const double median = m_median(k, retained);
         if (a.statistic == 0)
@@ -230,10 +243,14 @@ __device__ void m_finish(const double* v, long long n, long long volume, const M
   o.valid[mesh] = valid ? 1 : 0;
 }
 
+// Gather and sort: one block per mesh; the sorted samples go to `sorted`
+// (meshes of one warp interleaved: mesh m's sample i at
+// (m / 32) * 32 * cap + i * 32 + m % 32) and their count to `counts`.
 template <typename T>
 __global__ void __launch_bounds__(kMThreads)
-    mesh_stats_kernel(const T* __restrict__ in, const unsigned char* __restrict__ mask,
-                      const __grid_constant__ MeshArgs a, MeshOut o, unsigned long long* __restrict__ scratch) {
+    mesh_sort_kernel(const T* __restrict__ in, const unsigned char* __restrict__ mask,
+                     const __grid_constant__ MeshArgs a, unsigned long long* __restrict__ scratch,
+                     double* __restrict__ sorted, long long* __restrict__ counts) {
   extern __shared__ __align__(16) unsigned long long skeys[];
   __shared__ unsigned int count;
   unsigned long long* keys = a.capacity > 0 ? scratch + blockIdx.x * a.capacity : skeys;
@@ -282,12 +299,27 @@ __global__ void __launch_bounds__(kMThreads)
         __syncthreads();
       }
     }
-    double* values = reinterpret_cast<double*>(keys);
-    for (unsigned int i = threadIdx.x; i < n; i += blockDim.x) values[i] = mval(keys[i]);
-    __syncthreads();
-    if (threadIdx.x == 0) m_finish(values, n, volume, a, o, mesh);
+    double* dst = sorted + (mesh / 32) * 32 * a.cap + mesh % 32;
+    for (unsigned int i = threadIdx.x; i < n; i += blockDim.x) dst[(long long)i * 32] = mval(keys[i]);
+    if (threadIdx.x == 0) counts[mesh] = n;
     __syncthreads();
   }
+}
+
+// The statistics: one thread per mesh, so the float64 chain of every mesh
+// runs in its own lane (a warp's lanes hold 32 meshes).
+__global__ void mesh_finish_kernel(const __grid_constant__ MeshArgs a, const double* __restrict__ sorted,
+                                   const long long* __restrict__ counts, MeshOut o) {
+  const long long mesh = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (mesh >= a.mesh_len) return;
+  long long rest = mesh, volume = 1;
+  for (int d = a.ndim - 1; d >= 0; --d) {
+    const long long k = rest % a.mesh_shape[d];
+    rest /= a.mesh_shape[d];
+    volume *= min(k * a.box[d] + a.box[d], a.shape[d]) - k * a.box[d];
+  }
+  const SV v{sorted + (mesh / 32) * 32 * a.cap + mesh % 32, 32};
+  m_finish(v, counts[mesh], volume, a, o, mesh);
 }
 
 // ---------------------------------------------------------------------------
@@ -950,17 +982,28 @@ int run_device(const T* d_in, const uint8_t* d_mask, const Rules& r, T* d_bg, T*
       cudaError_t e = buf.alloc(&scratch, (size_t)(blocks * padded) * 8);
       if (e != cudaSuccess) return fail(NDF_ERR_MEMORY, "unable to allocate mesh workspace");
     }
+    a.cap = largest;
+    double* sorted = nullptr;
+    long long* counts = nullptr;
+    const long long groups = (m + 31) / 32;
     MeshOut o;
-    cudaError_t e = buf.alloc(&o.background, (size_t)m * 8);
+    cudaError_t e = buf.alloc(&sorted, (size_t)(groups * 32 * largest) * 8);
+    if (e == cudaSuccess) e = buf.alloc(&counts, (size_t)m * 8);
+    if (e == cudaSuccess) e = buf.alloc(&o.background, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.rms, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.finite, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.retained, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.valid, (size_t)m);
     if (e != cudaSuccess) return fail(NDF_ERR_MEMORY, "unable to allocate mesh workspace");
-    auto k = mesh_stats_kernel<T>;
+    auto k = mesh_sort_kernel<T>;
     if ((e = allow_max_smem((const void*)k)) != cudaSuccess) return cuda_fail(e, "mesh statistics");
-    k<<<(unsigned)blocks, kMThreads, smem, s>>>(d_in, d_mask, a, o, scratch);
+    k<<<(unsigned)blocks, kMThreads, smem, s>>>(d_in, d_mask, a, scratch, sorted, counts);
     e = cudaGetLastError();
+    if (e == cudaSuccess) {
+      // One warp per block spreads the meshes' warps over the most SMs.
+      mesh_finish_kernel<<<(unsigned)groups, 32, 0, s>>>(a, sorted, counts, o);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(bg.data(), o.background, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rms.data(), o.rms, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fin.data(), o.finite, (size_t)m * 8, cudaMemcpyDeviceToHost, s);

@@ -133,18 +133,23 @@ __device__ Scaled mad_parts(const double* s, int n) {
   else
     center = {__dadd_rn(__ddiv_rn(lower, 2.0), __ddiv_rn(upper, 2.0)), 0};
   if (!isfinite(center.value)) return {nan_of(0.0), 0};
+  // The merge keeps the two candidate deviations (left and right of the
+  // consumed middle run) and recomputes only the side it consumed.
   int left = n / 2, right = left;
   Scaled previous{0.0, 0}, selected = previous;
+  Scaled dl = left > 0 ? absolute_deviation(s[left - 1], center) : selected;
+  Scaled dr = right < n ? absolute_deviation(s[right], center) : selected;
   for (int step = 0; step <= n / 2; ++step) {
     previous = selected;
-    const bool take_left = left > 0 && (right == n || compare_scaled(absolute_deviation(s[left - 1], center),
-                                                                      absolute_deviation(s[right], center)) <= 0);
+    const bool take_left = left > 0 && (right == n || compare_scaled(dl, dr) <= 0);
     if (take_left) {
       --left;
-      selected = absolute_deviation(s[left], center);
+      selected = dl;
+      if (left > 0) dl = absolute_deviation(s[left - 1], center);
     } else {
-      selected = absolute_deviation(s[right], center);
+      selected = dr;
       ++right;
+      if (right < n) dr = absolute_deviation(s[right], center);
     }
   }
   return n % 2 == 1 ? selected : scaled_midpoint(previous, selected);
@@ -164,10 +169,28 @@ __device__ double multiply_scaled(Scaled value, double multiplier) {
   return __dmul_rn(__dmul_rn(m.value, 2.2250738585072014e-308), scale);
 }
 
-// within_limit, src/robust.rs:536-559.
-__device__ bool within_limit(double value, double center, Scaled spread, double sigma) {
+// within_limit, src/robust.rs:536-559, with the spread and the multiplier
+// split once per clipping pass (make_limit) and only the distance per sample
+// (inside): the same comparisons, in the same arithmetic.
+struct Limit {
+  bool zero;  // spread or sigma zero: only samples equal to the center pass
+  Scaled limit;
+  int exponent;
+};
+
+__device__ Limit make_limit(Scaled spread, double sigma) {
+  Limit l;
+  l.zero = spread.value == 0.0 || sigma == 0.0;
+  if (l.zero) return l;
+  const Scaled sc = binary_parts(spread.value), mu = binary_parts(sigma);
+  l.limit = binary_parts(__dmul_rn(sc.value, mu.value));
+  l.exponent = sc.exponent + mu.exponent + l.limit.exponent + spread.exponent;
+  return l;
+}
+
+__device__ __forceinline__ bool inside(double value, double center, const Limit& l) {
   if (value == center) return true;
-  if (spread.value == 0.0 || sigma == 0.0) return false;
+  if (l.zero) return false;
   const double difference = __dsub_rn(value, center);
   Scaled d;
   if (isfinite(difference)) {
@@ -176,10 +199,7 @@ __device__ bool within_limit(double value, double center, Scaled spread, double 
     d = binary_parts(fabs(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(center, 2.0))));
     d.exponent += 1;
   }
-  const Scaled sc = binary_parts(spread.value), mu = binary_parts(sigma);
-  const Scaled limit = binary_parts(__dmul_rn(sc.value, mu.value));
-  const int limit_exp = sc.exponent + mu.exponent + limit.exponent + spread.exponent;
-  return d.exponent < limit_exp || (d.exponent == limit_exp && d.value <= limit.value);
+  return d.exponent < l.exponent || (d.exponent == l.exponent && d.value <= l.limit.value);
 }
 
 // percentile, src/robust.rs:343-352, over sorted samples.
@@ -216,8 +236,9 @@ __device__ double finite_mean(const double* v, int n) {
   return clamp64(__ddiv_rn(scaled.total(), __ddiv_rn((double)n, scale)), lower, upper);
 }
 
-// std_parts, src/robust.rs:594-630, in tap order.
-__device__ Scaled std_parts(const double* v, int n) {
+// std_parts, src/robust.rs:594-630, in tap order. `w` keeps each sample's
+// delta / scale between the two sums (the same quotient both times).
+__device__ Scaled std_parts(const double* v, int n, double* w) {
   const double reference = v[0];
   bool halve = false;
   for (int i = 0; i < n; ++i) halve = halve || !isfinite(__dsub_rn(v[i], reference));
@@ -225,14 +246,20 @@ __device__ Scaled std_parts(const double* v, int n) {
     return halve ? __dsub_rn(__ddiv_rn(x, 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(x, reference);
   };
   double scale = 0.0;
-  for (int i = 0; i < n; ++i) scale = fmax(scale, fabs(delta(v[i])));
+  for (int i = 0; i < n; ++i) {
+    w[i] = delta(v[i]);
+    scale = fmax(scale, fabs(w[i]));
+  }
   if (scale == 0.0) return {0.0, 0};
   Sum64 sum;
-  for (int i = 0; i < n; ++i) sum.add(__ddiv_rn(delta(v[i]), scale));
+  for (int i = 0; i < n; ++i) {
+    w[i] = __ddiv_rn(w[i], scale);
+    sum.add(w[i]);
+  }
   const double center = __ddiv_rn(sum.total(), (double)n);
   Sum64 squares;
   for (int i = 0; i < n; ++i) {
-    const double residual = __dsub_rn(__ddiv_rn(delta(v[i]), scale), center);
+    const double residual = __dsub_rn(w[i], center);
     squares.add(__dmul_rn(residual, residual));
   }
   const Scaled parts = binary_parts(scale);
@@ -251,15 +278,42 @@ __device__ double mode_from_moments(double mean, double median, double std_dev, 
   return pearson_mode;
 }
 
+// dispersion_valid(values, 0, true), src/dispersion.rs:5-61, for finite
+// samples in tap order; `w` keeps each delta / scale between the two sums.
+__device__ double population_std(const double* v, int n, double* w) {
+  const double reference = v[0];
+  bool halve = false;
+  for (int i = 0; i < n; ++i) halve = halve || !isfinite(__dsub_rn(v[i], reference));
+  double scale = 0.0;
+  for (int i = 0; i < n; ++i) {
+    w[i] = halve ? __dsub_rn(__ddiv_rn(v[i], 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(v[i], reference);
+    scale = fmax(scale, fabs(w[i]));
+  }
+  if (scale == 0.0) return 0.0;
+  Sum64 sum;
+  for (int i = 0; i < n; ++i) {
+    w[i] = __ddiv_rn(w[i], scale);
+    sum.add(w[i]);
+  }
+  const double center = __ddiv_rn(sum.total(), (double)n);
+  Sum64 squares;
+  for (int i = 0; i < n; ++i) {
+    const double residual = __dsub_rn(w[i], center);
+    squares.add(__dmul_rn(residual, residual));
+  }
+  const double result = __dmul_rn(scale, __dsqrt_rn(__ddiv_rn(squares.total(), (double)n)));
+  return halve ? __dmul_rn(result, 2.0) : result;
+}
+
 // mode_estimate, src/location.rs:36-54: mean and std in tap order (`v`),
 // the median from the sorted samples (`s`).
-__device__ double mode_estimate(const double* v, const double* s, int n, int estimator, double pearson) {
+__device__ double mode_estimate(const double* v, const double* s, int n, int estimator, double pearson,
+                                double* w) {
   if (n == 0) return nan_of(0.0);
   Reduce r{};
   r.count = n;
-  auto fetch = [&](int i) { return v[i]; };
-  const double mean = mom::mean_exact(fetch, r);
-  const double std_dev = estimator == kModeSex ? mom::dispersion_exact(fetch, r, true) : nan_of(0.0);
+  const double mean = mom::mean_exact([&](int i) { return v[i]; }, r);
+  const double std_dev = estimator == kModeSex ? population_std(v, n, w) : nan_of(0.0);
   return mode_from_moments(mean, median_sorted(s, n), std_dev, estimator, pearson);
 }
 
@@ -337,8 +391,9 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
 }
 
 // clipped, src/robust.rs:632-689: `v` holds the finite samples in tap
-// order and `s` the same samples sorted; both shrink together.
-__device__ double clipped(double* v, double* s, int n, const RobustArgs& ra, int kind) {
+// order and `s` the same samples sorted; both shrink together (`w` is
+// scratch).
+__device__ double clipped(double* v, double* s, double* w, int n, const RobustArgs& ra, int kind) {
   long long iteration = 0;
   while (n >= ra.clip_min_count && (ra.maxiters < 0 || iteration < ra.maxiters)) {
     const double center = ra.center == 0 ? finite_mean(v, n) : percentile_sorted(s, n, 50.0);
@@ -352,14 +407,15 @@ __device__ double clipped(double* v, double* s, int n, const RobustArgs& ra, int
         spread = deviation;
       }
     } else {
-      spread = std_parts(v, n);
+      spread = std_parts(v, n, w);
     }
+    const Limit below = make_limit(spread, ra.lower), above = make_limit(spread, ra.upper);
     int kept = 0, kept_sorted = 0;
     for (int i = 0; i < n; ++i) {
       const double x = v[i];
-      if (within_limit(x, center, spread, x < center ? ra.lower : ra.upper)) v[kept++] = x;
+      if (inside(x, center, x < center ? below : above)) v[kept++] = x;
       const double y = s[i];
-      if (within_limit(y, center, spread, y < center ? ra.lower : ra.upper)) s[kept_sorted++] = y;
+      if (inside(y, center, y < center ? below : above)) s[kept_sorted++] = y;
     }
     ++iteration;
     const bool stable = kept == n;
@@ -369,13 +425,13 @@ __device__ double clipped(double* v, double* s, int n, const RobustArgs& ra, int
   if (n < ra.clip_min_count) return nan_of(0.0);
   if (kind == kRobustSigmaMean) return finite_mean(v, n);
   if (kind == kRobustSigmaMedian) return percentile_sorted(s, n, 50.0);
-  return mode_estimate(v, s, n, ra.estimator, ra.pearson);
+  return mode_estimate(v, s, n, ra.estimator, ra.pearson, w);
 }
 
 // One window: gather, the sample policy, the estimator.
 template <typename Fetch>
 __device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const RobustArgs& ra, double* v,
-                                double* s) {
+                                double* s, double* w) {
   const bool clip = ra.kind >= kRobustSigmaMean;
   int n = 0;
   bool nan = false, inf = false;
@@ -402,12 +458,12 @@ __device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const Rob
     case kRobustMad:
       return multiply_scaled(mad_parts(s, n), ra.parameter);
     case kRobustMode:
-      return inf ? nan_of(0.0) : mode_estimate(v, s, n, ra.estimator, ra.pearson);
+      return inf ? nan_of(0.0) : mode_estimate(v, s, n, ra.estimator, ra.pearson, w);
     case kRobustBiweightLocation:
     case kRobustBiweightScale:
       return inf ? nan_of(0.0) : biweight(s, n, v, ra, ra.kind == kRobustBiweightLocation);
     default:
-      return clipped(v, s, n, ra, ra.kind);
+      return clipped(v, s, w, n, ra, ra.kind);
   }
 }
 
@@ -421,10 +477,11 @@ __global__ void __launch_bounds__(kRThreads)
   const int V = a.r.count;
   const long long* flat = taps + (long long)V * rank;
   const T cval = (T)a.r.cval;
-  double local_v[MAXV > 0 ? MAXV : 1], local_s[MAXV > 0 ? MAXV : 1];
+  double local_v[MAXV > 0 ? MAXV : 1], local_s[MAXV > 0 ? MAXV : 1], local_w[MAXV > 0 ? MAXV : 1];
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  double* v = MAXV > 0 ? local_v : scratch + tid * 2ll * V;
+  double* v = MAXV > 0 ? local_v : scratch + tid * 3ll * V;
   double* s = MAXV > 0 ? local_s : v + V;
+  double* w = MAXV > 0 ? local_w : s + V;
   for (long long o = tid; o < a.n_out; o += (long long)gridDim.x * blockDim.x) {
     long long coord[kMaxGenericRank];
     long long rem = o;
@@ -445,7 +502,7 @@ __global__ void __launch_bounds__(kRThreads)
       }
       return (double)__ldg(in + src);
     };
-    const double result = robust_window(fetch, V, a.r, ra, v, s);
+    const double result = robust_window(fetch, V, a.r, ra, v, s, w);
     T value;
     if constexpr (sizeof(T) == 4)
       value = isnan(result) ? nan_of(0.0f) : __double2float_rn(result);
@@ -478,13 +535,13 @@ cudaError_t launch_robust_t(const Plan& p, const T* in, T* out, cudaStream_t s) 
 }  // namespace
 
 // Windows beyond 256 samples take per-thread slices of a scratch buffer of
-// at most 1 GiB (two float64 arrays per thread): the thread count is the
+// at most 1 GiB (three float64 arrays per thread): the thread count is the
 // largest multiple of the block size within that, capped at 16 blocks per
 // SM. Returns false when the scratch cannot be allocated.
 bool robust_configure(Plan& p) {
   p.robust_threads = 0;
   if (p.r.count <= 256) return true;
-  const size_t per_thread = (size_t)p.r.count * 2 * sizeof(double);
+  const size_t per_thread = (size_t)p.r.count * 3 * sizeof(double);
   long long threads = (long long)((1ull << 30) / per_thread) / kRThreads * kRThreads;
   threads = std::min(threads, (long long)std::max(1, p.sm_count) * 16 * kRThreads);
   if (threads < kRThreads) threads = kRThreads;
