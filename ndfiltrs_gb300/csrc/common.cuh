@@ -205,12 +205,25 @@ __device__ __forceinline__ float midpoint_f32(float lower, float upper) {
   return __double2float_rn(midpoint((double)lower, (double)upper));
 }
 
-// Neumaier float64 sum, src/mean.rs:7-26.
+// Float64 classification and magnitude on the integer pipes (GB300's FP64
+// pipe is narrow; these are exact bit tests, the same answers as isfinite /
+// isnan / fabs and a magnitude comparison).
+__device__ __forceinline__ unsigned long long mag_bits64(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ bool finite64(double x) { return mag_bits64(x) < 0x7FF0000000000000ull; }
+__device__ __forceinline__ bool nan64(double x) { return mag_bits64(x) > 0x7FF0000000000000ull; }
+__device__ __forceinline__ bool inf64_test(double x) { return mag_bits64(x) == 0x7FF0000000000000ull; }
+__device__ __forceinline__ double abs64(double x) { return __longlong_as_double((long long)mag_bits64(x)); }
+
+// Neumaier float64 sum, src/mean.rs:7-26. The |value| >= |x| test compares
+// magnitude bits (the same order for every non-NaN pair; with a NaN operand
+// the sum is NaN on either branch).
 struct Sum64 {
   double value = 0.0, correction = 0.0;
   __device__ __forceinline__ void add(double x) {
     double next = __dadd_rn(value, x);
-    if (fabs(value) >= fabs(x))
+    if (mag_bits64(value) >= mag_bits64(x))
       correction = __dadd_rn(correction, __dadd_rn(__dsub_rn(value, next), x));
     else
       correction = __dadd_rn(correction, __dadd_rn(__dsub_rn(x, next), value));

@@ -89,7 +89,7 @@ __device__ double m_median(SV v, long long n) {
   if (n % 2 == 1) return v[n / 2];
   const double a = v[n / 2 - 1], b = v[n / 2];
   const double mid = __ddiv_rn(__dadd_rn(a, b), 2.0);
-  return isfinite(mid) ? mid : __dadd_rn(__ddiv_rn(a, 2.0), __ddiv_rn(b, 2.0));
+  return finite64(mid) ? mid : __dadd_rn(__ddiv_rn(a, 2.0), __ddiv_rn(b, 2.0));
 }
 
 // mean_of, src/background.rs:965-978 (mean_valid on overflow).
@@ -97,7 +97,7 @@ __device__ double m_mean(SV v, long long n) {
   Sum64 sum;
   for (long long i = 0; i < n; ++i) sum.add(v[i]);
   const double total = sum.total();
-  if (isfinite(total)) return __ddiv_rn(total, (double)n);
+  if (finite64(total)) return __ddiv_rn(total, (double)n);
   Reduce r{};
   r.count = (int)n;
   return mom::mean_exact([&](int i) { return v[i]; }, r);
@@ -106,9 +106,9 @@ __device__ double m_mean(SV v, long long n) {
 // std_about, src/background.rs:1000-1015.
 __device__ double m_std(SV v, long long n, double mean) {
   if (n == 0) return nan_of(0.0);
-  const double scale = fmax(fabs(__dsub_rn(v[0], mean)), fabs(__dsub_rn(v[n - 1], mean)));
+  const double scale = fmax(abs64(__dsub_rn(v[0], mean)), abs64(__dsub_rn(v[n - 1], mean)));
   if (scale == 0.0) return 0.0;
-  if (!isfinite(scale)) return nan_of(0.0);
+  if (!finite64(scale)) return nan_of(0.0);
   Sum64 squares;
   for (long long i = 0; i < n; ++i) {
     const double d = __ddiv_rn(__dsub_rn(v[i], mean), scale);
@@ -127,14 +127,14 @@ __device__ double m_mad_std(SV v, long long n, double median) {
   double a = 0.0, b = 0.0;
   for (long long k = 0; k <= n / 2; ++k) {
     double next;
-    if (left > 0 && (right == n || fabs(__dsub_rn(v[left - 1], median)) <= fabs(__dsub_rn(v[right], median))))
-      next = fabs(__dsub_rn(v[--left], median));
+    if (left > 0 && (right == n || abs64(__dsub_rn(v[left - 1], median)) <= abs64(__dsub_rn(v[right], median))))
+      next = abs64(__dsub_rn(v[--left], median));
     else
-      next = fabs(__dsub_rn(v[right++], median));
+      next = abs64(__dsub_rn(v[right++], median));
     if (k == (n - 1) / 2) a = next;
     if (k == n / 2) b = next;
   }
-  const double mad = n % 2 == 1 ? b : (isfinite(__ddiv_rn(__dadd_rn(a, b), 2.0))
+  const double mad = n % 2 == 1 ? b : (finite64(__ddiv_rn(__dadd_rn(a, b), 2.0))
                                            ? __ddiv_rn(__dadd_rn(a, b), 2.0)
                                            : __dadd_rn(__ddiv_rn(a, 2.0), __ddiv_rn(b, 2.0)));
   return __ddiv_rn(mad, kNuq);
@@ -183,7 +183,7 @@ __device__ double m_mode(double mean, double median, double sd, int estimator, d
   if (estimator == kModeMmm) return pearson_mode;
   if (estimator == kModeIraf) return mean < median ? mean : pearson_mode;
   if (sd == 0.0) return mean;
-  if (__ddiv_rn(fabs(difference), sd) >= 0.3) return median;
+  if (__ddiv_rn(abs64(difference), sd) >= 0.3) return median;
   return pearson_mode;
 }
 
@@ -235,7 +235,7 @@ __device__ void m_finish(SV v, long long n, long long volume, const MeshArgs& a,
   const long long count = a.valid_count == 0 ? n : retained;
   const long long base = a.valid_base == 0 ? volume : a.box_volume;
   const bool valid = count > 0 && (double)count >= __dmul_rn(a.min_valid_fraction, (double)base) &&
-                     isfinite(background) && isfinite(rms);
+                     finite64(background) && finite64(rms);
   o.background[mesh] = valid ? background : nan_of(0.0);
   o.rms[mesh] = valid ? rms : nan_of(0.0);
   o.finite[mesh] = n;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kMThreads)
         stride *= a.shape[d];
       }
       const double v = (double)__ldg(in + offset);
-      if (isfinite(v) && !(mask && mask[offset])) keys[atomicAdd(&count, 1u)] = mkey(v);
+      if (finite64(v) && !(mask && mask[offset])) keys[atomicAdd(&count, 1u)] = mkey(v);
     }
     __syncthreads();
     const unsigned int n = count;

@@ -89,19 +89,19 @@ __device__ __forceinline__ double inf64() { return __longlong_as_double(0x7ff000
 
 // absolute_deviation, src/robust.rs:438-466.
 __device__ Scaled absolute_deviation(double value, Scaled center) {
-  if (center.exponent == -1 && isfinite(__dmul_rn(value, 2.0))) {
+  if (center.exponent == -1 && finite64(__dmul_rn(value, 2.0))) {
     const double difference = __dsub_rn(__dmul_rn(value, 2.0), center.value);
-    if (isfinite(difference)) return {fabs(difference), -1};
+    if (finite64(difference)) return {abs64(difference), -1};
   }
   const double midpoint = center.exponent == -1 ? __ddiv_rn(center.value, 2.0) : center.value;
   const double difference = __dsub_rn(value, midpoint);
-  if (isfinite(difference) || isinf(value)) return {fabs(difference), 0};
-  return {fabs(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(midpoint, 2.0))), 1};
+  if (finite64(difference) || inf64_test(value)) return {abs64(difference), 0};
+  return {abs64(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(midpoint, 2.0))), 1};
 }
 
 // compare_scaled, src/robust.rs:468-481.
 __device__ int compare_scaled(Scaled left, Scaled right) {
-  if (left.value == 0.0 || right.value == 0.0 || isinf(left.value) || isinf(right.value))
+  if (left.value == 0.0 || right.value == 0.0 || inf64_test(left.value) || inf64_test(right.value))
     return total_cmp(left.value, right.value);
   const Scaled l = binary_parts(left.value), r = binary_parts(right.value);
   const int a = l.exponent + left.exponent, b = r.exponent + right.exponent;
@@ -111,7 +111,7 @@ __device__ int compare_scaled(Scaled left, Scaled right) {
 
 // scaled_midpoint, src/robust.rs:483-496.
 __device__ Scaled scaled_midpoint(Scaled left, Scaled right) {
-  if (isinf(right.value) || right.value == 0.0) return right;
+  if (inf64_test(right.value) || right.value == 0.0) return right;
   const Scaled r = binary_parts(right.value);
   const int exponent = r.exponent + right.exponent;
   double lv = 0.0;
@@ -126,13 +126,13 @@ __device__ Scaled scaled_midpoint(Scaled left, Scaled right) {
 __device__ Scaled mad_parts(const double* s, int n) {
   const double lower = s[(n - 1) / 2], upper = s[n / 2];
   Scaled center;
-  if (!isfinite(lower) || !isfinite(upper))
+  if (!finite64(lower) || !finite64(upper))
     center = {interpolate(lower, upper, 0.5), 0};
-  else if (isfinite(__dadd_rn(lower, upper)))
+  else if (finite64(__dadd_rn(lower, upper)))
     center = {__dadd_rn(lower, upper), -1};
   else
     center = {__dadd_rn(__ddiv_rn(lower, 2.0), __ddiv_rn(upper, 2.0)), 0};
-  if (!isfinite(center.value)) return {nan_of(0.0), 0};
+  if (!finite64(center.value)) return {nan_of(0.0), 0};
   // The merge keeps the two candidate deviations (left and right of the
   // consumed middle run) and recomputes only the side it consumed.
   int left = n / 2, right = left;
@@ -157,7 +157,7 @@ __device__ Scaled mad_parts(const double* s, int n) {
 
 // multiply_scaled, src/robust.rs:513-534.
 __device__ double multiply_scaled(Scaled value, double multiplier) {
-  if (!isfinite(value.value)) return __dmul_rn(value.value, multiplier);
+  if (!finite64(value.value)) return __dmul_rn(value.value, multiplier);
   if (value.value == 0.0 || multiplier == 0.0) return 0.0;
   const Scaled l = binary_parts(value.value), r = binary_parts(multiplier);
   const Scaled m = binary_parts(__dmul_rn(l.value, r.value));
@@ -193,10 +193,10 @@ __device__ __forceinline__ bool inside(double value, double center, const Limit&
   if (l.zero) return false;
   const double difference = __dsub_rn(value, center);
   Scaled d;
-  if (isfinite(difference)) {
-    d = binary_parts(fabs(difference));
+  if (finite64(difference)) {
+    d = binary_parts(abs64(difference));
   } else {
-    d = binary_parts(fabs(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(center, 2.0))));
+    d = binary_parts(abs64(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(center, 2.0))));
     d.exponent += 1;
   }
   return d.exponent < l.exponent || (d.exponent == l.exponent && d.value <= l.limit.value);
@@ -222,7 +222,7 @@ __device__ double finite_mean(const double* v, int n) {
   Sum64 sum;
   for (int i = 0; i < n; ++i) sum.add(v[i]);
   const double total = sum.total();
-  if (isfinite(total)) return __ddiv_rn(total, (double)n);
+  if (finite64(total)) return __ddiv_rn(total, (double)n);
   const unsigned long long m = (unsigned long long)(n - 1);
   const int exponent = (m == 0 ? 0 : 64 - __clzll((long long)m)) + 1;
   const double scale = powi2(exponent);
@@ -241,14 +241,14 @@ __device__ double finite_mean(const double* v, int n) {
 __device__ Scaled std_parts(const double* v, int n, double* w) {
   const double reference = v[0];
   bool halve = false;
-  for (int i = 0; i < n; ++i) halve = halve || !isfinite(__dsub_rn(v[i], reference));
+  for (int i = 0; i < n; ++i) halve = halve || !finite64(__dsub_rn(v[i], reference));
   auto delta = [&](double x) {
     return halve ? __dsub_rn(__ddiv_rn(x, 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(x, reference);
   };
   double scale = 0.0;
   for (int i = 0; i < n; ++i) {
     w[i] = delta(v[i]);
-    scale = fmax(scale, fabs(w[i]));
+    scale = fmax(scale, abs64(w[i]));
   }
   if (scale == 0.0) return {0.0, 0};
   Sum64 sum;
@@ -274,7 +274,7 @@ __device__ double mode_from_moments(double mean, double median, double std_dev, 
   if (estimator == kModeMmm) return pearson_mode;
   if (estimator == kModeIraf) return mean < median ? mean : pearson_mode;
   if (std_dev == 0.0) return mean;
-  if (__ddiv_rn(fabs(difference), std_dev) >= 0.3) return median;
+  if (__ddiv_rn(abs64(difference), std_dev) >= 0.3) return median;
   return pearson_mode;
 }
 
@@ -283,11 +283,11 @@ __device__ double mode_from_moments(double mean, double median, double std_dev, 
 __device__ double population_std(const double* v, int n, double* w) {
   const double reference = v[0];
   bool halve = false;
-  for (int i = 0; i < n; ++i) halve = halve || !isfinite(__dsub_rn(v[i], reference));
+  for (int i = 0; i < n; ++i) halve = halve || !finite64(__dsub_rn(v[i], reference));
   double scale = 0.0;
   for (int i = 0; i < n; ++i) {
     w[i] = halve ? __dsub_rn(__ddiv_rn(v[i], 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(v[i], reference);
-    scale = fmax(scale, fabs(w[i]));
+    scale = fmax(scale, abs64(w[i]));
   }
   if (scale == 0.0) return 0.0;
   Sum64 sum;
@@ -326,7 +326,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   bool overflow = false;
   for (int i = 0; i < n; ++i) {
     dev[i] = __dsub_rn(s[i], median);
-    overflow = overflow || !isfinite(dev[i]);
+    overflow = overflow || !finite64(dev[i]);
   }
   if (overflow) {
     factor = 2.0;
@@ -340,10 +340,10 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   double a = 0.0, b = 0.0;
   for (int k = 0; k <= n / 2; ++k) {
     double next;
-    if (left > 0 && (right == n || fabs(dev[left - 1]) <= fabs(dev[right]))) {
-      next = fabs(dev[--left]);
+    if (left > 0 && (right == n || abs64(dev[left - 1]) <= abs64(dev[right]))) {
+      next = abs64(dev[--left]);
     } else {
-      next = fabs(dev[right++]);
+      next = abs64(dev[right++]);
     }
     if (k == (n - 1) / 2) a = next;
     if (k == n / 2) b = next;
@@ -352,7 +352,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   if (mad == 0.0) return location ? median : 0.0;
   const double c = ra.parameter;
   double extra = 1.0;
-  while (!isfinite(__dmul_rn(c, mad))) {
+  while (!finite64(__dmul_rn(c, mad))) {
     mad = __ddiv_rn(mad, 2.0);
     extra = __dmul_rn(extra, 2.0);
   }
@@ -362,7 +362,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
     Sum64 weighted, weights;
     for (int i = 0; i < n; ++i) {
       const double u = __ddiv_rn(__ddiv_rn(dev[i], extra), width);
-      if (!(fabs(u) < 1.0)) continue;
+      if (!(abs64(u) < 1.0)) continue;
       const double t = __dsub_rn(1.0, __dmul_rn(u, u));
       const double weight = __dmul_rn(t, t);
       weighted.add(__dmul_rn(u, weight));
@@ -370,14 +370,14 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
     }
     const double correction = __dmul_rn(width, __ddiv_rn(weighted.total(), weights.total()));
     const double unscaled = __dmul_rn(correction, factor);
-    if (isfinite(unscaled)) return __dadd_rn(median, unscaled);
+    if (finite64(unscaled)) return __dadd_rn(median, unscaled);
     return __dmul_rn(__dadd_rn(__ddiv_rn(median, factor), correction), factor);
   }
   Sum64 numerator, denominator;
   int kept = 0;
   for (int i = 0; i < n; ++i) {
     const double u = __ddiv_rn(__ddiv_rn(dev[i], extra), width);
-    if (!(fabs(u) < 1.0)) continue;
+    if (!(abs64(u) < 1.0)) continue;
     const double u2 = __dmul_rn(u, u);
     const double w = __dsub_rn(1.0, u2);
     const double taper = __dmul_rn(w, w);
@@ -386,7 +386,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
     ++kept;
   }
   const double count = (double)(ra.modify_sample_size ? kept : n);
-  const double ratio = __ddiv_rn(__dsqrt_rn(__dmul_rn(count, numerator.total())), fabs(denominator.total()));
+  const double ratio = __ddiv_rn(__dsqrt_rn(__dmul_rn(count, numerator.total())), abs64(denominator.total()));
   return __dmul_rn(__dmul_rn(width, ratio), factor);
 }
 
@@ -400,7 +400,7 @@ __device__ double clipped(double* v, double* s, double* w, int n, const RobustAr
     Scaled spread;
     if (ra.spread == 1) {
       const Scaled deviation = mad_parts(s, n);
-      if (deviation.value > 0.0 && isfinite(deviation.value)) {
+      if (deviation.value > 0.0 && finite64(deviation.value)) {
         const Scaled parts = binary_parts(deviation.value);
         spread = {__ddiv_rn(parts.value, kNormalUpperQuartile), parts.exponent + deviation.exponent};
       } else {
@@ -438,15 +438,15 @@ __device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const Rob
   for (int i = 0; i < V; ++i) {
     const double x = fetch(i);
     if (clip) {
-      if (isfinite(x)) v[n++] = x;
+      if (finite64(x)) v[n++] = x;
       continue;
     }
-    if (isnan(x)) {
+    if (nan64(x)) {
       nan = nan || !r.omit;
       continue;
     }
-    if (r.drop_inf && isinf(x)) continue;
-    inf = inf || isinf(x);
+    if (r.drop_inf && inf64_test(x)) continue;
+    inf = inf || inf64_test(x);
     v[n++] = x;
   }
   if (!clip) {
@@ -505,9 +505,9 @@ __global__ void __launch_bounds__(kRThreads)
     const double result = robust_window(fetch, V, a.r, ra, v, s, w);
     T value;
     if constexpr (sizeof(T) == 4)
-      value = isnan(result) ? nan_of(0.0f) : __double2float_rn(result);
+      value = nan64(result) ? nan_of(0.0f) : __double2float_rn(result);
     else
-      value = isnan(result) ? nan_of(0.0) : result;
+      value = nan64(result) ? nan_of(0.0) : result;
     out[o] = value;
   }
 }
