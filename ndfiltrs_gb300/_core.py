@@ -249,6 +249,24 @@ def _i32(values) -> ctypes.Array:
     return (ctypes.c_int32 * max(len(values), 1))(*[int(v) for v in values])
 
 
+def _robust_params(robust: dict | None) -> RobustParams:
+    """The ndf_robust_params of a robust kind's options (defaults as the
+    reference's ClipConfig::new(3.0) and the estimators' defaults)."""
+    options = dict(robust or {})
+    maxiters = options.get("maxiters", 5)
+    return RobustParams(
+        float(options.get("parameter", 0.0)),
+        float(options.get("sigma_lower", 3.0)),
+        float(options.get("sigma_upper", 3.0)),
+        -1 if maxiters is None else int(maxiters),
+        CENTERS[options.get("center", "median")],
+        SPREADS[options.get("spread", "std")],
+        ESTIMATORS[options.get("estimator", "sex")],
+        int(bool(options.get("modify_sample_size", False))),
+        float(options.get("pearson", 2.5)),
+    )
+
+
 class Plan:
     """A validated filter plan (``WindowFilter::new``, src/plan.rs:260-324).
 
@@ -330,19 +348,7 @@ class Plan:
             None,
         )
         if kind in ROBUST_KINDS:
-            options = dict(robust or {})
-            maxiters = options.get("maxiters", 5)
-            params = RobustParams(
-                float(options.get("parameter", 0.0)),
-                float(options.get("sigma_lower", 3.0)),
-                float(options.get("sigma_upper", 3.0)),
-                -1 if maxiters is None else int(maxiters),
-                CENTERS[options.get("center", "median")],
-                SPREADS[options.get("spread", "std")],
-                ESTIMATORS[options.get("estimator", "sex")],
-                int(bool(options.get("modify_sample_size", False))),
-                float(options.get("pearson", 2.5)),
-            )
+            params = _robust_params(robust)
             self._keep.append(params)
             desc.robust = ctypes.pointer(params)
         handle = ctypes.c_void_p()
@@ -414,7 +420,8 @@ class Batch:
     ``specs`` is a list of dicts with the Plan keyword arguments (``shape``,
     ``kind``, ``size``, ``footprint``, ``origin``, ``mode``, ``cval``,
     ``omit_nan``, ``ignore_inf``, ``min_count``, ``parameter``,
-    ``percentile``, ``moments``). ``run_device`` takes device pointers of
+    ``percentile``, ``moments``, and ``robust`` for the robust kinds).
+    ``run_device`` takes device pointers of
     every image and enqueues the captured CUDA graph on ``stream``.
     """
 
@@ -445,6 +452,10 @@ class Batch:
                 int(spec.get("min_count", 1)), int(spec.get("parameter", 0)),
                 float(spec.get("percentile", 50.0)), MOMENTS[spec.get("moments", "fp32c")],
             )
+            if spec["kind"] in ROBUST_KINDS:
+                params = _robust_params(spec.get("robust"))
+                self._keep.append(params)
+                descs[i].robust = ctypes.pointer(params)
         handle = ctypes.c_void_p()
         _check(lib.ndf_batch_create(descs, len(specs), ctypes.byref(handle)), lib)
         self._handle = handle

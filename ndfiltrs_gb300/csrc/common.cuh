@@ -216,6 +216,48 @@ __device__ __forceinline__ bool nan64(double x) { return mag_bits64(x) > 0x7FF00
 __device__ __forceinline__ bool inf64_test(double x) { return mag_bits64(x) == 0x7FF0000000000000ull; }
 __device__ __forceinline__ double abs64(double x) { return __longlong_as_double((long long)mag_bits64(x)); }
 
+// Division of many dividends by one divisor s, correctly rounded (the same
+// result as d / s): with r = RN(1/s), q = RN(d r) is corrected once by its
+// exact residual (Markstein's method), and the corrected quotient is kept
+// only when its own residual proves it is the nearest float: |d - q s| <
+// ulp(q) |s| / 2, which holds exactly when q = RN(d / s) and no tie occurs
+// (the residual is exact for q within one ulp; a wrong q has a residual of
+// at least that bound, and rounding cannot bring it below a representable
+// bound). Anything else (ties, powers of two, subnormal, zero or non-finite
+// operands or results) takes the division.
+struct Divisor {
+  double s, r;
+  bool fast;  // s normal and finite
+};
+
+__device__ __forceinline__ Divisor make_divisor(double s) {
+  const unsigned long long m = (unsigned long long)__double_as_longlong(s) & 0x7FFFFFFFFFFFFFFFull;
+  Divisor d;
+  d.s = s;
+  d.fast = m >= 0x0010000000000000ull && m < 0x7FF0000000000000ull;
+  d.r = d.fast ? __drcp_rn(s) : 0.0;
+  return d;
+}
+
+__device__ __forceinline__ double div_by(double x, const Divisor& d) {
+  if (d.fast) {
+    const double q0 = __dmul_rn(x, d.r);
+    const double q = __fma_rn(__fma_rn(-q0, d.s, x), d.r, q0);
+    const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+    const int qe = (int)((qb >> 52) & 0x7FF);
+    const int se = (int)(((unsigned long long)__double_as_longlong(d.s) >> 52) & 0x7FF);
+    // q normal, not a power of two, and the bound |s| 2^(E(q) - 53) normal.
+    const int he = se + qe - 1023 - 53;
+    if (qe >= 1 && qe < 0x7FF && (qb & 0x000FFFFFFFFFFFFFull) != 0 && he >= 1 && he <= 2046) {
+      const double e = __fma_rn(-q, d.s, x);
+      const unsigned long long hb =
+          ((unsigned long long)__double_as_longlong(d.s) & 0x000FFFFFFFFFFFFFull) | ((unsigned long long)he << 52);
+      if (((unsigned long long)__double_as_longlong(e) & 0x7FFFFFFFFFFFFFFFull) < hb) return q;
+    }
+  }
+  return __ddiv_rn(x, d.s);
+}
+
 // Neumaier float64 sum, src/mean.rs:7-26. The |value| >= |x| test compares
 // magnitude bits (the same order for every non-NaN pair; with a NaN operand
 // the sum is NaN on either branch).

@@ -92,16 +92,17 @@ __device__ double dispersion_exact(Fetch&& fetch, const Reduce& r, bool want_std
   }
   if (scale == 0.0) return 0.0;
   Sum64 sum;
+  const Divisor by = make_divisor(scale);
   for (int i = 0; i < V; ++i) {
     double v = fetch(i);
-    if (kept(v)) sum.add(__ddiv_rn(delta(v), scale));
+    if (kept(v)) sum.add(div_by(delta(v), by));
   }
   double center = __ddiv_rn(sum.total(), (double)n);
   Sum64 squares;
   for (int i = 0; i < V; ++i) {
     double v = fetch(i);
     if (!kept(v)) continue;
-    double residual = __dsub_rn(__ddiv_rn(delta(v), scale), center);
+    double residual = __dsub_rn(div_by(delta(v), by), center);
     squares.add(__dmul_rn(residual, residual));
   }
   double normalized = __ddiv_rn(squares.total(), (double)(n - r.param));

@@ -93,10 +93,10 @@ __device__ Scaled absolute_deviation(double value, Scaled center) {
     const double difference = __dsub_rn(__dmul_rn(value, 2.0), center.value);
     if (finite64(difference)) return {abs64(difference), -1};
   }
-  const double midpoint = center.exponent == -1 ? __ddiv_rn(center.value, 2.0) : center.value;
+  const double midpoint = center.exponent == -1 ? __dmul_rn(center.value, 0.5) : center.value;
   const double difference = __dsub_rn(value, midpoint);
   if (finite64(difference) || inf64_test(value)) return {abs64(difference), 0};
-  return {abs64(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(midpoint, 2.0))), 1};
+  return {abs64(__dsub_rn(__dmul_rn(value, 0.5), __dmul_rn(midpoint, 0.5))), 1};
 }
 
 // compare_scaled, src/robust.rs:468-481.
@@ -131,7 +131,7 @@ __device__ Scaled mad_parts(const double* s, int n) {
   else if (finite64(__dadd_rn(lower, upper)))
     center = {__dadd_rn(lower, upper), -1};
   else
-    center = {__dadd_rn(__ddiv_rn(lower, 2.0), __ddiv_rn(upper, 2.0)), 0};
+    center = {__dadd_rn(__dmul_rn(lower, 0.5), __dmul_rn(upper, 0.5)), 0};
   if (!finite64(center.value)) return {nan_of(0.0), 0};
   // The merge keeps the two candidate deviations (left and right of the
   // consumed middle run) and recomputes only the side it consumed.
@@ -196,7 +196,7 @@ __device__ __forceinline__ bool inside(double value, double center, const Limit&
   if (finite64(difference)) {
     d = binary_parts(abs64(difference));
   } else {
-    d = binary_parts(abs64(__dsub_rn(__ddiv_rn(value, 2.0), __ddiv_rn(center, 2.0))));
+    d = binary_parts(abs64(__dsub_rn(__dmul_rn(value, 0.5), __dmul_rn(center, 0.5))));
     d.exponent += 1;
   }
   return d.exponent < l.exponent || (d.exponent == l.exponent && d.value <= l.limit.value);
@@ -243,7 +243,7 @@ __device__ Scaled std_parts(const double* v, int n, double* w) {
   bool halve = false;
   for (int i = 0; i < n; ++i) halve = halve || !finite64(__dsub_rn(v[i], reference));
   auto delta = [&](double x) {
-    return halve ? __dsub_rn(__ddiv_rn(x, 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(x, reference);
+    return halve ? __dsub_rn(__dmul_rn(x, 0.5), __dmul_rn(reference, 0.5)) : __dsub_rn(x, reference);
   };
   double scale = 0.0;
   for (int i = 0; i < n; ++i) {
@@ -252,8 +252,9 @@ __device__ Scaled std_parts(const double* v, int n, double* w) {
   }
   if (scale == 0.0) return {0.0, 0};
   Sum64 sum;
+  const Divisor by = make_divisor(scale);
   for (int i = 0; i < n; ++i) {
-    w[i] = __ddiv_rn(w[i], scale);
+    w[i] = div_by(w[i], by);
     sum.add(w[i]);
   }
   const double center = __ddiv_rn(sum.total(), (double)n);
@@ -286,13 +287,14 @@ __device__ double population_std(const double* v, int n, double* w) {
   for (int i = 0; i < n; ++i) halve = halve || !finite64(__dsub_rn(v[i], reference));
   double scale = 0.0;
   for (int i = 0; i < n; ++i) {
-    w[i] = halve ? __dsub_rn(__ddiv_rn(v[i], 2.0), __ddiv_rn(reference, 2.0)) : __dsub_rn(v[i], reference);
+    w[i] = halve ? __dsub_rn(__dmul_rn(v[i], 0.5), __dmul_rn(reference, 0.5)) : __dsub_rn(v[i], reference);
     scale = fmax(scale, abs64(w[i]));
   }
   if (scale == 0.0) return 0.0;
   Sum64 sum;
+  const Divisor by = make_divisor(scale);
   for (int i = 0; i < n; ++i) {
-    w[i] = __ddiv_rn(w[i], scale);
+    w[i] = div_by(w[i], by);
     sum.add(w[i]);
   }
   const double center = __ddiv_rn(sum.total(), (double)n);
@@ -330,7 +332,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   }
   if (overflow) {
     factor = 2.0;
-    for (int i = 0; i < n; ++i) dev[i] = __dsub_rn(__ddiv_rn(s[i], 2.0), __ddiv_rn(median, 2.0));
+    for (int i = 0; i < n; ++i) dev[i] = __dsub_rn(__dmul_rn(s[i], 0.5), __dmul_rn(median, 0.5));
   }
   // Median of |dev|: the deviations ascend, so their magnitudes ascend
   // outwards from the smallest; merge both sides up to the middle ranks.
@@ -353,15 +355,16 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   const double c = ra.parameter;
   double extra = 1.0;
   while (!finite64(__dmul_rn(c, mad))) {
-    mad = __ddiv_rn(mad, 2.0);
+    mad = __dmul_rn(mad, 0.5);
     extra = __dmul_rn(extra, 2.0);
   }
   const double width = __dmul_rn(c, mad);
   factor = __dmul_rn(factor, extra);
+  const Divisor by_extra = make_divisor(extra), by_width = make_divisor(width);
   if (location) {
     Sum64 weighted, weights;
     for (int i = 0; i < n; ++i) {
-      const double u = __ddiv_rn(__ddiv_rn(dev[i], extra), width);
+      const double u = div_by(div_by(dev[i], by_extra), by_width);
       if (!(abs64(u) < 1.0)) continue;
       const double t = __dsub_rn(1.0, __dmul_rn(u, u));
       const double weight = __dmul_rn(t, t);
@@ -376,7 +379,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   Sum64 numerator, denominator;
   int kept = 0;
   for (int i = 0; i < n; ++i) {
-    const double u = __ddiv_rn(__ddiv_rn(dev[i], extra), width);
+    const double u = div_by(div_by(dev[i], by_extra), by_width);
     if (!(abs64(u) < 1.0)) continue;
     const double u2 = __dmul_rn(u, u);
     const double w = __dsub_rn(1.0, u2);

@@ -109,3 +109,45 @@ def test_batch_host_pipeline_matches_device_run(gpu) -> None:
     for want, have in zip(expected, outputs):
         np.testing.assert_array_equal(bits(have), bits(want))
     batch.close()
+
+
+def test_batch_with_rolling_means_extrema_and_robust_kinds(gpu) -> None:
+    """Images whose plans use the band rolling mean, the two-pass extrema or
+    the robust kernel run their own launches inside the batch's graph; the
+    results equal per-image plans, on device buffers and through the host
+    pipeline."""
+    import torch
+
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(17)
+    kinds = [("mean_rolling", (31, 31), {}), ("min", (9, 9), {}), ("max", (1, 15), {}),
+             ("mad", (5, 5), {"parameter": 1.4826}),
+             ("sigma_median", (7, 7), {"sigma_lower": 2.0, "sigma_upper": 2.0, "maxiters": None}),
+             ("biweight_location", (5, 5), {"parameter": 6.0}), ("median", (5, 5), {})]
+    specs, images = [], []
+    for i in range(21):
+        kind, size, robust = kinds[i % len(kinds)]
+        image = rng.normal(1000, 10, size=(int(rng.integers(30, 200)), int(rng.integers(30, 200))))
+        image = image.astype(np.float32)
+        image[rng.random(image.shape) < 0.02] = np.nan
+        specs.append(dict(shape=image.shape, kind=kind, size=size, footprint=None, omit_nan=True,
+                          ignore_inf=False, min_count=1, parameter=0, percentile=50.0,
+                          mode=["reflect", "nearest", "wrap"][i % 3], robust=robust))
+        images.append(image)
+    batch = _core.Batch(specs)
+    device = torch.device("cuda")
+    d_in = [torch.from_numpy(im).to(device) for im in images]
+    d_out = [torch.full_like(t, 7.0) for t in d_in]
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):
+        batch.run_device([t.data_ptr() for t in d_in], [t.data_ptr() for t in d_out], stream)
+    torch.cuda.synchronize()
+    hosted = batch.run_host(images)
+    for spec, image, out, host in zip(specs, images, d_out, hosted):
+        with _core.Plan(image.shape, np.float32, spec["kind"], spec["size"], mode=[spec["mode"]] * 2,
+                        omit_nan=True, robust=spec["robust"]) as plan:
+            want = plan.run_host(image)
+        np.testing.assert_array_equal(bits(out.cpu().numpy()), bits(want), err_msg=spec["kind"])
+        np.testing.assert_array_equal(bits(host), bits(want), err_msg=spec["kind"])
+    batch.close()
