@@ -17,6 +17,62 @@ using namespace net;
 constexpr int kBoxTW = 32;
 constexpr int kBoxPairs = 2;  // pairs per thread: tile height 16 * kBoxPairs
 
+// The key of rank R (0-based) in the union of two sorted runs `a` and `b`,
+// NB of b's keys in play: R + 1 smallest keys split as p from a and q from
+// b, and the rank-R key is the smallest over splits of the larger last
+// element, min over q of max(a[R - q], b[q - 1]) (q = 0: a[R]). Dropped
+// samples sit at the runs' ends as the largest key and never win for
+// R below the retained count. 2 NB + 1 operations instead of a merge.
+template <int R, int NB, int P, typename K>
+__device__ __forceinline__ K union_rank(const K (&a)[P], const K (&b)[P]) {
+  static_assert(R < P, "rank beyond the first run");
+  K best = a[R];
+#pragma unroll
+  for (int q = 1; q <= NB; ++q) {
+    if (q > R + 1) break;
+    const K t = (R - q >= 0) ? (a[R - q > 0 ? R - q : 0] > b[q - 1] ? a[R - q > 0 ? R - q : 0] : b[q - 1])
+                             : b[q - 1];
+    best = t < best ? t : best;
+  }
+  return best;
+}
+
+// The window median (Reduction::finish for the median kinds,
+// src/reduction.rs:78-130) from the shared and private sorted runs: the
+// reducers midpoint for even counts, NaN when the window has too few
+// retained samples (omit) or any dropped one (propagate). With at most four
+// dropped samples the middle ranks lie in [V/2 - 2, V/2]; otherwise the runs
+// are merged.
+template <typename T, int V, int NB, int P, typename K>
+__device__ __forceinline__ T box_median(const K (&sh)[P], const K (&pv)[P], int nv, const Reduce& r) {
+  using KO = KeyOf<T>;
+  const bool missing = r.omit ? (nv < r.min_count) : (nv != V);
+  if (missing || nv == 0) return nan_of(T());
+  if (!r.omit) {
+    if constexpr (V & 1) return KO::value(union_rank<V / 2, NB>(sh, pv));
+    else return median_of_two(KO::value(union_rank<V / 2 - 1, NB>(sh, pv)), KO::value(union_rank<V / 2, NB>(sh, pv)));
+  }
+  if constexpr (V >= 9 && (V & 1)) {
+    constexpr int L = V / 2 - 2;
+    if (nv >= V - 4) {
+      const K c0 = union_rank<L, NB>(sh, pv), c1 = union_rank<L + 1, NB>(sh, pv), c2 = union_rank<L + 2, NB>(sh, pv);
+      const int hi = nv / 2 - L;  // 0, 1 or 2
+      const K a_hi = hi == 0 ? c0 : (hi == 1 ? c1 : c2);
+      if (nv & 1) return KO::value(a_hi);
+      const K a_lo = hi == 1 ? c0 : c1;  // even nv: hi is 1 or 2
+      return median_of_two(KO::value(a_lo), KO::value(a_hi));
+    }
+  }
+  K m[2 * P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    m[i] = sh[i];
+    m[P + i] = pv[i];
+  }
+  batcher_merge<2 * P>(m);
+  return network_finish<T, 2 * P, V, 1>(m, nv, r);
+}
+
 template <typename T, int KH, int KW, int MODE>
 __global__ void __launch_bounds__(kThreads)
     tile_box_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
@@ -65,6 +121,12 @@ __global__ void __launch_bounds__(kThreads)
     batcher_sort<P>(sh);
     batcher_sort<P>(pa);
     batcher_sort<P>(pb);
+    if constexpr (MODE == 1) {
+      out[(z * g.H + y) * g.W + x] = canonical(box_median<T, V, KW>(sh, pa, n_sh + n_a, a.r));
+      if (y + 1 < g.H)
+        out[(z * g.H + y + 1) * g.W + x] = canonical(box_median<T, V, KW>(sh, pb, n_sh + n_b, a.r));
+      continue;
+    }
     {
       K m[2 * P];
 #pragma unroll
