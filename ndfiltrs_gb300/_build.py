@@ -84,7 +84,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
     with ThreadPoolExecutor(max_workers=workers) as pool:
         list(pool.map(compile_one, zip(units, objects)))
     tmp = LIBRARY.with_suffix(f".so.{os.getpid()}.tmp")
-    link = [compiler, "-shared", ARCH, "-o", str(tmp), *map(str, objects)]
+    link = [compiler, "-shared", ARCH, "-o", str(tmp), *map(str, objects), "-lpthread"]
     result = subprocess.run(link, capture_output=True, text=True)
     if result.returncode != 0:
         raise RuntimeError(f"link failed:\n{result.stderr}")

@@ -10,17 +10,17 @@
 // reference writes mul_add), so results equal the reference bit for bit.
 //
 // GB300 design:
-//  * mesh_sort_kernel: one 128-thread block per mesh (grid-stride over
-//    meshes) gathers the mesh's finite, unmasked samples as order-preserving
-//    64-bit keys into shared memory (global scratch for meshes beyond 8192
-//    samples), bitonic-sorts them and stores the sorted float64 samples,
-//    32 meshes interleaved;
-//  * mesh_finish_kernel: one thread per mesh runs the SExtractor or
-//    sigma-clip sequence over its sorted samples. The reference accumulates
-//    Neumaier sums in sorted order, an order a parallel reduction would not
-//    keep, so each mesh is one sequential float64 chain; giving every mesh
-//    its own lane keeps all 32 lanes of each FP64 instruction busy (the GB300
-//    FP64 pipe is narrow, and a one-lane chain would waste 31 of them);
+//  * mesh_stats_kernel: one 128-thread block per mesh gathers the mesh's
+//    finite, unmasked samples as order-preserving 64-bit keys into shared
+//    memory (global scratch for meshes beyond 8192 samples), bitonic-sorts
+//    them and runs the SExtractor or sigma-clip sequence with the whole
+//    block. The reference accumulates Neumaier sums in sorted order; the
+//    block sums the terms exactly in fixed point, in parallel, and proves
+//    from the exact sum and a bound on the compensation's rounding that the
+//    sequential sum rounds to the same double (thread 0 runs the sequential
+//    sum in the rare case it cannot), so the float64 chains of one mesh no
+//    longer run one sample at a time; medians, MADs and clipping bounds are
+//    binary searches over the sorted samples;
 //  * fill, median filter and the global medians run on the host over the
 //    small mesh grid;
 //  * the maps: the natural spline is a tensor product, one axis per pass
@@ -29,8 +29,11 @@
 //    one block per output line. The SExtractor form runs one block per output
 //    row. Both are a handful of float64 operations per output pixel.
 #include <algorithm>
+#include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -52,7 +55,6 @@ struct MeshArgs {
   long long shape[kMaxMeshRank], box[kMaxMeshRank], mesh_shape[kMaxMeshRank];
   long long mesh_len;
   long long capacity;  // keys per block in `scratch` (0: shared memory)
-  long long cap;       // samples per mesh in the sorted buffer (largest mesh volume)
   long long box_volume;
   int estimator, center, spread, statistic, mode_estimator, rms, valid_count, valid_base;
   long long maxiters;
@@ -75,14 +77,32 @@ __device__ __forceinline__ double mval(unsigned long long k) {
   return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
 }
 
-// A mesh's sorted samples: element i at p[i * stride] (meshes of one warp
-// interleave, so the lanes of a warp read neighbouring addresses).
+// A mesh's sorted samples: element i is p[i] (float64 bits).
 struct SV {
-  const double* p;
-  long long stride;
-  __device__ __forceinline__ double operator[](long long i) const { return p[i * stride]; }
-  __device__ __forceinline__ SV at(long long k) const { return {p + k * stride, stride}; }
+  const unsigned long long* p;
+  __device__ __forceinline__ double operator[](long long i) const { return __longlong_as_double((long long)p[i]); }
+  __device__ __forceinline__ SV at(long long k) const { return {p + k}; }
 };
+
+// Block state of the statistics: per-warp partial sums and a broadcast slot.
+struct W3 {
+  unsigned long long w0, w1, w2;  // 192-bit two's complement, w0 lowest
+};
+
+struct MeshShared {
+  W3 part[kMThreads / 32];
+  int low[kMThreads / 32];
+  double value;
+};
+
+// Thread 0's `v` in every thread of the block.
+__device__ double broadcast(double v, MeshShared& sh) {
+  if (threadIdx.x == 0) sh.value = v;
+  __syncthreads();
+  v = sh.value;
+  __syncthreads();
+  return v;
+}
 
 // median_sorted, src/background.rs:950-963.
 __device__ double m_median(SV v, long long n) {
@@ -92,48 +112,252 @@ __device__ double m_median(SV v, long long n) {
   return finite64(mid) ? mid : __dadd_rn(__ddiv_rn(a, 2.0), __ddiv_rn(b, 2.0));
 }
 
-// mean_of, src/background.rs:965-978 (mean_valid on overflow).
-__device__ double m_mean(SV v, long long n) {
-  Sum64 sum;
-  for (long long i = 0; i < n; ++i) sum.add(v[i]);
-  const double total = sum.total();
-  if (finite64(total)) return __ddiv_rn(total, (double)n);
-  Reduce r{};
-  r.count = (int)n;
-  return mom::mean_exact([&](int i) { return v[i]; }, r);
+// ---------------------------------------------------------------------------
+// Block-wide sums equal to the reference's sequential Neumaier sums.
+//
+// The reference adds a mesh's terms x_1..x_n in sorted order with Neumaier's
+// compensation (Sum64, src/mean.rs:7-26): s_i = RN(s_{i-1} + x_i), the error
+// e_i of each addition computed exactly (Fast2Sum with the larger magnitude
+// first), c_n = the rounded running sum of the e_i, result RN(s_n + c_n).
+// With S the exact sum, s_n + sum(e_i) = S, so the result is RN(S + delta),
+// delta = c_n - sum(e_i) the rounding of the correction sum. For n < 2^k
+// terms below 2^H (n < 2^31, no overflow):
+//  * sum|e_i| <= u n (1+u)^n sum|x_i| < 2^(2k + H - 52), u = 2^-53. When
+//    every term is a multiple of 2^Q, so are every s_i, e_i and running sum
+//    of the e_i; with Q >= 2k + H - 105 those running sums stay below
+//    2^(Q + 53), are exact, delta = 0, and the result is RN(S) exactly
+//    (ties included). This is the usual case for image data;
+//  * otherwise |delta| <= gamma_{n-1} sum|e_i| < 2 n^3 u^2 2^H. The block
+//    rounds both ends of [S - E, S + E], E = 2^(3k + 55) units of the fixed
+//    point (more than |delta| plus the n units of truncation); RN is
+//    monotone, so when the ends agree every point between them rounds to the
+//    same double, which is the sequential result.
+// The block adds the terms exactly, in any order, in 192-bit fixed point
+// with lowest bit 2^(H - 158) (bits below it truncated). When neither case
+// decides (S within E of a rounding boundary, huge magnitudes, a result
+// outside the normal range) thread 0 runs the sequential sum.
+
+__device__ __forceinline__ void add3(W3& s, unsigned long long a0, unsigned long long a1, unsigned long long a2) {
+  asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\taddc.u64 %2, %2, %5;"
+      : "+l"(s.w0), "+l"(s.w1), "+l"(s.w2)
+      : "l"(a0), "l"(a1), "l"(a2));
 }
 
-// std_about, src/background.rs:1000-1015.
-__device__ double m_std(SV v, long long n, double mean) {
+__device__ __forceinline__ void sub3(W3& s, unsigned long long a0, unsigned long long a1, unsigned long long a2) {
+  asm("sub.cc.u64 %0, %0, %3;\n\tsubc.cc.u64 %1, %1, %4;\n\tsubc.u64 %2, %2, %5;"
+      : "+l"(s.w0), "+l"(s.w1), "+l"(s.w2)
+      : "l"(a0), "l"(a1), "l"(a2));
+}
+
+// s += x / 2^L, |x| truncated to whole units; false when x is not finite or
+// |x| >= 2^(L + 158). `low` takes the exponent of x's lowest set bit.
+__device__ __forceinline__ bool add_fixed(W3& s, double x, int L, int& low) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  if (mag >= 0x7FF0000000000000ull) return false;
+  const int e = (int)(mag >> 52);
+  const unsigned long long m = (mag & 0x000FFFFFFFFFFFFFull) | (e ? 0x0010000000000000ull : 0ull);
+  if (m == 0) return true;
+  const int sh = (e ? e - 1075 : -1074) - L;  // x = m 2^(sh + L)
+  if (sh > 105) return false;
+  low = min(low, sh + L + __ffsll((long long)m) - 1);
+  unsigned long long a0 = 0, a1 = 0, a2 = 0;
+  if (sh < 0) {
+    a0 = sh > -64 ? m >> -sh : 0ull;
+  } else {
+    const int bs = sh & 63;
+    const unsigned long long lo = m << bs, hi = bs ? m >> (64 - bs) : 0ull;
+    if (sh < 64) {
+      a0 = lo;
+      a1 = hi;
+    } else {
+      a1 = lo;
+      a2 = hi;
+    }
+  }
+  if (b >> 63)
+    sub3(s, a0, a1, a2);
+  else
+    add3(s, a0, a1, a2);
+  return true;
+}
+
+// RN(s 2^L) for a 192-bit two's complement s with |s| < 2^190; false when s
+// is zero or the result is not a normal double.
+__device__ __forceinline__ bool fixed_rn(W3 s, int L, double* out) {
+  const bool neg = (long long)s.w2 < 0;
+  if (neg) {
+    s.w0 = ~s.w0;
+    s.w1 = ~s.w1;
+    s.w2 = ~s.w2;
+    add3(s, 1ull, 0ull, 0ull);
+  }
+  int top;
+  if (s.w2)
+    top = 191 - __clzll((long long)s.w2);
+  else if (s.w1)
+    top = 127 - __clzll((long long)s.w1);
+  else if (s.w0)
+    top = 63 - __clzll((long long)s.w0);
+  else
+    return false;
+  // Shift the leading one to bit 191: 53 significand bits, then round and
+  // sticky bits.
+  int z = 191 - top;
+  while (z >= 64) {
+    s.w2 = s.w1;
+    s.w1 = s.w0;
+    s.w0 = 0;
+    z -= 64;
+  }
+  if (z) {
+    s.w2 = (s.w2 << z) | (s.w1 >> (64 - z));
+    s.w1 = (s.w1 << z) | (s.w0 >> (64 - z));
+    s.w0 <<= z;
+  }
+  unsigned long long sig = s.w2 >> 11;
+  const bool half = (s.w2 >> 10) & 1ull;
+  const bool sticky = (s.w2 & 0x3FFull) != 0 || s.w1 != 0 || s.w0 != 0;
+  int exponent = L + top;  // s 2^L in [2^exponent, 2^(exponent + 1))
+  if (half && (sticky || (sig & 1ull))) ++sig;
+  if (sig >> 53) {
+    sig >>= 1;
+    ++exponent;
+  }
+  const int biased = exponent + 1023;
+  if (biased < 1 || biased > 2046) return false;
+  *out = __longlong_as_double((long long)(((unsigned long long)neg << 63) | ((unsigned long long)biased << 52) |
+                                          (sig & 0x000FFFFFFFFFFFFFull)));
+  return true;
+}
+
+// Smallest H with |x| < 2^H (x finite).
+__device__ __forceinline__ int bound_exponent(double x) {
+  const int e = (int)(mag_bits64(x) >> 52);
+  return e ? e - 1022 : -1022;
+}
+
+// The reference's sequential Neumaier sum of term(0..n-1), every |term|
+// below 2^H (a term that is not returns the sequential sum). Called by every
+// thread of the block with the same arguments; returns the same value in all.
+template <typename Term>
+__device__ double block_sum(Term&& term, long long n, int H, MeshShared& sh) {
+  const int L = H - 158;
+  const int k = 64 - __clzll(n);  // n < 2^k
+  bool ok = n >= 1 && n < (1ll << 31) && k + H <= 1000;
+  W3 s{0ull, 0ull, 0ull};
+  int low = INT_MAX;
+  if (ok)
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) ok = add_fixed(s, term(i), L, low) && ok;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long b0 = __shfl_down_sync(0xffffffffu, s.w0, off);
+    const unsigned long long b1 = __shfl_down_sync(0xffffffffu, s.w1, off);
+    const unsigned long long b2 = __shfl_down_sync(0xffffffffu, s.w2, off);
+    add3(s, b0, b1, b2);
+  }
+  low = __reduce_min_sync(0xffffffffu, low);
+  if ((threadIdx.x & 31) == 0) {
+    sh.part[threadIdx.x >> 5] = s;
+    sh.low[threadIdx.x >> 5] = low;
+  }
+  const bool failed = __syncthreads_or(!ok);
+  W3 total = sh.part[0];
+  low = sh.low[0];
+#pragma unroll
+  for (int w = 1; w < kMThreads / 32; ++w) {
+    add3(total, sh.part[w].w0, sh.part[w].w1, sh.part[w].w2);
+    low = min(low, sh.low[w]);
+  }
+  __syncthreads();
+  if (!failed) {
+    double result;
+    if (low >= 2 * k + H - 105) {
+      // Exact correction sum: the result is RN(S).
+      if ((total.w0 | total.w1 | total.w2) == 0ull) return 0.0;
+      if (fixed_rn(total, L, &result)) return result;
+    } else {
+      const int pos = 3 * k + 55;
+      const unsigned long long e0 = pos < 64 ? 1ull << pos : 0ull;
+      const unsigned long long e1 = pos >= 64 && pos < 128 ? 1ull << (pos - 64) : 0ull;
+      const unsigned long long e2 = pos >= 128 ? 1ull << (pos - 128) : 0ull;
+      W3 lo = total, hi = total;
+      sub3(lo, e0, e1, e2);
+      add3(hi, e0, e1, e2);
+      double high;
+      if (fixed_rn(lo, L, &result) && fixed_rn(hi, L, &high) &&
+          __double_as_longlong(result) == __double_as_longlong(high))
+        return result;
+    }
+  }
+  double sequential = 0.0;
+  if (threadIdx.x == 0) {
+    Sum64 sum;
+    for (long long i = 0; i < n; ++i) sum.add(term(i));
+    sequential = sum.total();
+  }
+  return broadcast(sequential, sh);
+}
+
+// mean_of, src/background.rs:965-978 (mean_valid on overflow).
+__device__ double m_mean(SV v, long long n, MeshShared& sh) {
+  const int H = bound_exponent(fmax(abs64(v[0]), abs64(v[n - 1])));
+  const double total = block_sum([&](long long i) { return v[i]; }, n, H, sh);
+  if (finite64(total)) return __ddiv_rn(total, (double)n);
+  double mean = 0.0;
+  if (threadIdx.x == 0) {
+    Reduce r{};
+    r.count = (int)n;
+    mean = mom::mean_exact([&](int i) { return v[i]; }, r);
+  }
+  return broadcast(mean, sh);
+}
+
+// std_about, src/background.rs:1000-1015. Every scaled deviation is at most
+// 1 in magnitude (the extremes of sorted samples set the scale and rounding
+// is monotone), so the squares lie below 2^1.
+__device__ double m_std(SV v, long long n, double mean, MeshShared& sh) {
   if (n == 0) return nan_of(0.0);
   const double scale = fmax(abs64(__dsub_rn(v[0], mean)), abs64(__dsub_rn(v[n - 1], mean)));
   if (scale == 0.0) return 0.0;
   if (!finite64(scale)) return nan_of(0.0);
-  Sum64 squares;
-  for (long long i = 0; i < n; ++i) {
-    const double d = __ddiv_rn(__dsub_rn(v[i], mean), scale);
-    squares.add(__dmul_rn(d, d));
-  }
-  return __dmul_rn(scale, __dsqrt_rn(__ddiv_rn(squares.total(), (double)n)));
+  const Divisor by = make_divisor(scale);
+  const double squares = block_sum(
+      [&](long long i) {
+        const double d = div_by(__dsub_rn(v[i], mean), by);
+        return __dmul_rn(d, d);
+      },
+      n, 1, sh);
+  return __dmul_rn(scale, __dsqrt_rn(__ddiv_rn(squares, (double)n)));
 }
 
 // mad_std, src/background.rs:1017-1022: the median of |v - median| over
-// sorted v, merged outwards from the smallest deviation (they ascend on both
-// sides), divided by Phi^-1(0.75).
+// sorted v, divided by Phi^-1(0.75). The deviations ascend on both sides of
+// the first sample at or above the median, so the two middle ranks of their
+// union come from a binary search over the split between the two sides.
 __device__ double m_mad_std(SV v, long long n, double median) {
-  long long right = 0;
-  while (right < n && __dsub_rn(v[right], median) < 0.0) ++right;
-  long long left = right;
-  double a = 0.0, b = 0.0;
-  for (long long k = 0; k <= n / 2; ++k) {
-    double next;
-    if (left > 0 && (right == n || abs64(__dsub_rn(v[left - 1], median)) <= abs64(__dsub_rn(v[right], median))))
-      next = abs64(__dsub_rn(v[--left], median));
-    else
-      next = abs64(__dsub_rn(v[right++], median));
-    if (k == (n - 1) / 2) a = next;
-    if (k == n / 2) b = next;
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    const long long mid = (lo + hi) / 2;
+    if (__dsub_rn(v[mid], median) < 0.0) lo = mid + 1; else hi = mid;
   }
+  const long long right = lo, na = right, nb = n - right;
+  auto A = [&](long long t) { return abs64(__dsub_rn(v[right - 1 - t], median)); };
+  auto B = [&](long long t) { return abs64(__dsub_rn(v[right + t], median)); };
+  // Rank r (0-based) of the union: p from A and r + 1 - p from B, the
+  // smallest p with no smaller key of A left out.
+  auto rank = [&](long long r) {
+    long long a = r + 1 - nb > 0 ? r + 1 - nb : 0, b = r + 1 < na ? r + 1 : na;
+    while (a < b) {
+      const long long p = (a + b) / 2, q = r + 1 - p;
+      if (p < na && q > 0 && A(p) < B(q - 1)) a = p + 1; else b = p;
+    }
+    const long long q = r + 1 - a;
+    if (a == 0) return B(q - 1);
+    if (q == 0) return A(a - 1);
+    return fmax(A(a - 1), B(q - 1));
+  };
+  const double a = rank((n - 1) / 2), b = rank(n / 2);
   const double mad = n % 2 == 1 ? b : (finite64(__ddiv_rn(__dadd_rn(a, b), 2.0))
                                            ? __ddiv_rn(__dadd_rn(a, b), 2.0)
                                            : __dadd_rn(__ddiv_rn(a, 2.0), __ddiv_rn(b, 2.0)));
@@ -159,14 +383,18 @@ __device__ void m_within(SV v, long long r0, long long r1, double low, double hi
 }
 
 // clip_sorted, src/background.rs:1034-1069.
-__device__ void m_clip(SV v, long long& r0, long long& r1, double lower, double upper,
-                       long long maxiters, int center, int spread) {
+__device__ void m_clip(SV v, long long& r0, long long& r1, double lower, double upper, long long maxiters,
+                       int center, int spread, MeshShared& sh) {
   long long iteration = 0;
   while (r1 - r0 >= 1 && (maxiters < 0 || iteration < maxiters)) {
     const SV kept = v.at(r0);
     const long long n = r1 - r0;
-    const double middle = center == 0 ? m_mean(kept, n) : m_median(kept, n);
-    const double width = spread == 0 ? m_std(kept, n, m_mean(kept, n)) : m_mad_std(kept, n, m_median(kept, n));
+    const double middle = center == 0 ? m_mean(kept, n, sh) : m_median(kept, n);
+    double width;
+    if (spread == 0)
+      width = m_std(kept, n, center == 0 ? middle : m_mean(kept, n, sh), sh);
+    else
+      width = m_mad_std(kept, n, center == 1 ? middle : m_median(kept, n));
     long long lo, hi;
     m_within(v, r0, r1, __dsub_rn(middle, __dmul_rn(lower, width)), __dadd_rn(middle, __dmul_rn(upper, width)),
              lo, hi);
@@ -187,28 +415,30 @@ __device__ double m_mode(double mean, double median, double sd, int estimator, d
   return pearson_mode;
 }
 
-// finish_stats with sextractor_stats / clipped_stats, src/background.rs:652-705, 1071-1152.
-__device__ void m_finish(SV v, long long n, long long volume, const MeshArgs& a, const MeshOut& o,
-                         long long mesh) {
+// finish_stats with sextractor_stats / clipped_stats, src/background.rs:652-705,
+// 1071-1152. Every thread of the block runs it with the same values; thread
+// 0 writes the mesh's results.
+__device__ void m_finish(SV v, long long n, long long volume, const MeshArgs& a, const MeshOut& o, long long mesh,
+                         MeshShared& sh) {
   double background = nan_of(0.0), rms = nan_of(0.0);
   long long retained = 0;
   if (n > 0) {
     if (a.estimator == 0) {
-      const double mean = m_mean(v, n);
-      const double sd = m_std(v, n, mean);
+      const double mean = m_mean(v, n, sh);
+      const double sd = m_std(v, n, mean, sh);
       long long f0, f1;
       m_within(v, 0, n, __dsub_rn(mean, __dmul_rn(2.0, sd)), __dadd_rn(mean, __dmul_rn(2.0, sd)), f0, f1);
       if (f0 != f1) {
-        const double mean2 = m_mean(v.at(f0), f1 - f0);
-        const double sd2 = m_std(v.at(f0), f1 - f0, mean2);
+        const double mean2 = m_mean(v.at(f0), f1 - f0, sh);
+        const double sd2 = m_std(v.at(f0), f1 - f0, mean2, sh);
         long long s0, s1;
         m_within(v, 0, n, __dsub_rn(mean2, __dmul_rn(5.0, sd2)), __dadd_rn(mean2, __dmul_rn(5.0, sd2)), s0, s1);
-        m_clip(v, s0, s1, 3.0, 3.0, 100, 1, 0);
+        m_clip(v, s0, s1, 3.0, 3.0, 100, 1, 0, sh);
         if (s0 != s1) {
           const SV k = v.at(s0);
           const long long c = s1 - s0;
-          const double mean3 = m_mean(k, c);
-          const double sd3 = m_std(k, c, mean3);
+          const double mean3 = m_mean(k, c, sh);
+          const double sd3 = m_std(k, c, mean3, sh);
           background = m_mode(mean3, m_median(k, c), sd3, kModeSex, a.pearson);
           rms = sd3;
           retained = c;
@@ -216,22 +446,25 @@ __device__ void m_finish(SV v, long long n, long long volume, const MeshArgs& a,
       }
     } else {
       long long r0 = 0, r1 = n;
-      m_clip(v, r0, r1, a.lower, a.upper, a.maxiters, a.center, a.spread);
+      m_clip(v, r0, r1, a.lower, a.upper, a.maxiters, a.center, a.spread, sh);
       retained = r1 - r0;
       if (retained > 0) {
         const SV k = v.at(r0);
-        const double mean = m_mean(k, retained);
+        const double mean = m_mean(k, retained, sh);
         const double median = m_median(k, retained);
+        const bool need_std = a.statistic == 2 || a.rms == 0;
+        const double sd = need_std ? m_std(k, retained, mean, sh) : 0.0;
         if (a.statistic == 0)
           background = mean;
         else if (a.statistic == 1)
           background = median;
         else
-          background = m_mode(mean, median, m_std(k, retained, mean), a.mode_estimator, a.pearson);
-        rms = a.rms == 0 ? m_std(k, retained, mean) : m_mad_std(k, retained, median);
+          background = m_mode(mean, median, sd, a.mode_estimator, a.pearson);
+        rms = a.rms == 0 ? sd : m_mad_std(k, retained, median);
       }
     }
   }
+  if (threadIdx.x != 0) return;
   const long long count = a.valid_count == 0 ? n : retained;
   const long long base = a.valid_base == 0 ? volume : a.box_volume;
   const bool valid = count > 0 && (double)count >= __dmul_rn(a.min_valid_fraction, (double)base) &&
@@ -243,16 +476,16 @@ __device__ void m_finish(SV v, long long n, long long volume, const MeshArgs& a,
   o.valid[mesh] = valid ? 1 : 0;
 }
 
-// Gather and sort: one block per mesh; the sorted samples go to `sorted`
-// (meshes of one warp interleaved: mesh m's sample i at
-// (m / 32) * 32 * cap + i * 32 + m % 32) and their count to `counts`.
+// One block per mesh (grid-stride over meshes): gather the finite, unmasked
+// samples as order-preserving 64-bit keys, bitonic-sort them, turn them back
+// into float64 samples in place and run the statistics with the whole block.
 template <typename T>
 __global__ void __launch_bounds__(kMThreads)
-    mesh_sort_kernel(const T* __restrict__ in, const unsigned char* __restrict__ mask,
-                     const __grid_constant__ MeshArgs a, unsigned long long* __restrict__ scratch,
-                     double* __restrict__ sorted, long long* __restrict__ counts) {
+    mesh_stats_kernel(const T* __restrict__ in, const unsigned char* __restrict__ mask,
+                      const __grid_constant__ MeshArgs a, unsigned long long* __restrict__ scratch, MeshOut o) {
   extern __shared__ __align__(16) unsigned long long skeys[];
   __shared__ unsigned int count;
+  __shared__ MeshShared sh;
   unsigned long long* keys = a.capacity > 0 ? scratch + blockIdx.x * a.capacity : skeys;
   const int ndim = a.ndim;
   for (long long mesh = blockIdx.x; mesh < a.mesh_len; mesh += gridDim.x) {
@@ -299,27 +532,12 @@ __global__ void __launch_bounds__(kMThreads)
         __syncthreads();
       }
     }
-    double* dst = sorted + (mesh / 32) * 32 * a.cap + mesh % 32;
-    for (unsigned int i = threadIdx.x; i < n; i += blockDim.x) dst[(long long)i * 32] = mval(keys[i]);
-    if (threadIdx.x == 0) counts[mesh] = n;
+    for (unsigned int i = threadIdx.x; i < n; i += blockDim.x)
+      keys[i] = (unsigned long long)__double_as_longlong(mval(keys[i]));
+    __syncthreads();
+    m_finish(SV{keys}, n, volume, a, o, mesh, sh);
     __syncthreads();
   }
-}
-
-// The statistics: one thread per mesh, so the float64 chain of every mesh
-// runs in its own lane (a warp's lanes hold 32 meshes).
-__global__ void mesh_finish_kernel(const __grid_constant__ MeshArgs a, const double* __restrict__ sorted,
-                                   const long long* __restrict__ counts, MeshOut o) {
-  const long long mesh = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (mesh >= a.mesh_len) return;
-  long long rest = mesh, volume = 1;
-  for (int d = a.ndim - 1; d >= 0; --d) {
-    const long long k = rest % a.mesh_shape[d];
-    rest /= a.mesh_shape[d];
-    volume *= min(k * a.box[d] + a.box[d], a.shape[d]) - k * a.box[d];
-  }
-  const SV v{sorted + (mesh / 32) * 32 * a.cap + mesh % 32, 32};
-  m_finish(v, counts[mesh], volume, a, o, mesh);
 }
 
 // ---------------------------------------------------------------------------
@@ -575,23 +793,46 @@ void unravel(long long flat, const std::vector<long long>& dims, long long* inde
   }
 }
 
-// fill_invalid / replacement, src/background.rs:715-798.
+// body(i) for every i in [0, count), spread over host threads when `work`
+// (a rough operation count) is large enough to pay for them.
+template <typename Body>
+void parallel_for(long long count, long long work, Body&& body) {
+  long long threads = std::max(1u, std::thread::hardware_concurrency());
+  threads = std::min({threads, 32ll, count, std::max(1ll, work / 200000)});
+  if (threads <= 1) {
+    for (long long i = 0; i < count; ++i) body(i);
+    return;
+  }
+  std::atomic<long long> next{0};
+  auto run = [&] {
+    for (long long i = next.fetch_add(1); i < count; i = next.fetch_add(1)) body(i);
+  };
+  std::vector<std::thread> pool;
+  for (long long t = 1; t < threads; ++t) pool.emplace_back(run);
+  run();
+  for (std::thread& t : pool) t.join();
+}
+
+// fill_invalid / replacement, src/background.rs:715-798: each invalid mesh takes the mean
+// of its nearest valid meshes ('nearest') or the inverse-distance weighted
+// mean of the valid meshes within its idw_neighbors-th smallest distance
+// ('idw'), summed in (distance, index) order. The invalid meshes are
+// independent: they run on host threads, and 'idw' selects the cut-off
+// distance with nth_element and sorts only the meshes within it.
 void fill_invalid(std::vector<double>& bg, std::vector<double>& rms, const std::vector<unsigned char>& valid,
                   const Rules& r) {
   const long long n = r.mesh_len;
   const size_t ndim = r.mesh_shape.size();
-  std::vector<long long> good;
-  for (long long i = 0; i < n; ++i)
-    if (valid[i]) good.push_back(i);
-  if ((long long)good.size() == n || good.empty()) return;
-  std::vector<long long> gi(good.size() * ndim), idx(ndim);
+  std::vector<long long> good, bad;
+  for (long long i = 0; i < n; ++i) (valid[i] ? good : bad).push_back(i);
+  if (bad.empty() || good.empty()) return;
+  std::vector<long long> gi(good.size() * ndim);
   for (size_t s = 0; s < good.size(); ++s) unravel(good[s], r.mesh_shape, &gi[s * ndim]);
-  std::vector<std::tuple<long long, double, double>> out;
-  std::vector<std::pair<uint64_t, long long>> d;
-  for (long long flat = 0; flat < n; ++flat) {
-    if (valid[flat]) continue;
-    unravel(flat, r.mesh_shape, idx.data());
-    d.clear();
+  std::vector<double> values(bad.size()), spreads(bad.size());
+  parallel_for((long long)bad.size(), (long long)(bad.size() * good.size()), [&](long long j) {
+    std::vector<long long> idx(ndim);
+    unravel(bad[j], r.mesh_shape, idx.data());
+    std::vector<std::pair<uint64_t, long long>> d(good.size());
     for (size_t s = 0; s < good.size(); ++s) {
       uint64_t d2 = 0;
       for (size_t a = 0; a < ndim; ++a) {
@@ -599,7 +840,7 @@ void fill_invalid(std::vector<double>& bg, std::vector<double>& rms, const std::
         const uint64_t ad = (uint64_t)(diff < 0 ? -diff : diff);
         d2 += ad * ad;
       }
-      d.push_back({d2, good[s]});
+      d[s] = {d2, good[s]};
     }
     double value, spread;
     if (r.c.fill == NDF_MESH_FILL_NEAREST) {
@@ -616,11 +857,17 @@ void fill_invalid(std::vector<double>& bg, std::vector<double>& rms, const std::
       value = v.total() / (double)count;
       spread = s.total() / (double)count;
     } else {
-      std::sort(d.begin(), d.end());
-      const uint64_t last = d[std::min<size_t>(r.c.idw_neighbors, d.size()) - 1].first;
+      const size_t kth = std::min<size_t>(r.c.idw_neighbors, d.size()) - 1;
+      std::vector<uint64_t> distances(d.size());
+      for (size_t s = 0; s < d.size(); ++s) distances[s] = d[s].first;
+      std::nth_element(distances.begin(), distances.begin() + (long long)kth, distances.end());
+      const uint64_t last = distances[kth];
+      std::vector<std::pair<uint64_t, long long>> near;
+      for (const auto& e : d)
+        if (e.first <= last) near.push_back(e);
+      std::sort(near.begin(), near.end());
       NeumaierHost weighted, weighted_rms, total;
-      for (const auto& e : d) {
-        if (e.first > last) break;
+      for (const auto& e : near) {
         const double weight = 1.0 / std::pow(std::sqrt((double)e.first), r.c.idw_power);
         weighted.add(weight * bg[e.second]);
         weighted_rms.add(weight * rms[e.second]);
@@ -629,15 +876,15 @@ void fill_invalid(std::vector<double>& bg, std::vector<double>& rms, const std::
       value = weighted.total() / total.total();
       spread = weighted_rms.total() / total.total();
     }
-    out.emplace_back(flat, value, spread);
-  }
-  for (const auto& [flat, value, spread] : out) {
-    bg[flat] = value;
-    rms[flat] = spread;
+    values[j] = value;
+    spreads[j] = spread;
+  });
+  for (size_t j = 0; j < bad.size(); ++j) {
+    bg[bad[j]] = values[j];
+    rms[bad[j]] = spreads[j];
   }
 }
 
-// filter, src/background.rs:800-856.
 void median_filter(std::vector<double>& bg, std::vector<double>& rms, const Rules& r) {
   bool all_one = true;
   for (long long f : r.filter) all_one = all_one && f == 1;
@@ -970,7 +1217,9 @@ int run_device(const T* d_in, const uint8_t* d_mask, const Rules& r, T* d_bg, T*
     for (int d = 0; d < a.ndim; ++d) largest *= std::min(r.box[d], r.shape[d]);
     long long padded = 1;
     while (padded < largest) padded <<= 1;
-    long long blocks = std::min(m, (long long)std::max(1, sm_count) * 16);
+    // One block per mesh when the sort fits in shared memory; otherwise the
+    // blocks share a bounded global workspace and stride over the meshes.
+    long long blocks = std::min(m, (long long)INT_MAX);
     unsigned long long* scratch = nullptr;
     size_t smem = 0;
     if (padded * 8 <= std::min((long long)smem_optin, kMeshSmemBytes)) {
@@ -978,32 +1227,21 @@ int run_device(const T* d_in, const uint8_t* d_mask, const Rules& r, T* d_bg, T*
       a.capacity = 0;
     } else {
       a.capacity = padded;
-      blocks = std::min(blocks, std::max(1ll, (1ll << 30) / (padded * 8)));
+      blocks = std::min({m, (long long)std::max(1, sm_count) * 16, std::max(1ll, (1ll << 30) / (padded * 8))});
       cudaError_t e = buf.alloc(&scratch, (size_t)(blocks * padded) * 8);
       if (e != cudaSuccess) return fail(NDF_ERR_MEMORY, "unable to allocate mesh workspace");
     }
-    a.cap = largest;
-    double* sorted = nullptr;
-    long long* counts = nullptr;
-    const long long groups = (m + 31) / 32;
     MeshOut o;
-    cudaError_t e = buf.alloc(&sorted, (size_t)(groups * 32 * largest) * 8);
-    if (e == cudaSuccess) e = buf.alloc(&counts, (size_t)m * 8);
-    if (e == cudaSuccess) e = buf.alloc(&o.background, (size_t)m * 8);
+    cudaError_t e = buf.alloc(&o.background, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.rms, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.finite, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.retained, (size_t)m * 8);
     if (e == cudaSuccess) e = buf.alloc(&o.valid, (size_t)m);
     if (e != cudaSuccess) return fail(NDF_ERR_MEMORY, "unable to allocate mesh workspace");
-    auto k = mesh_sort_kernel<T>;
+    auto k = mesh_stats_kernel<T>;
     if ((e = allow_max_smem((const void*)k)) != cudaSuccess) return cuda_fail(e, "mesh statistics");
-    k<<<(unsigned)blocks, kMThreads, smem, s>>>(d_in, d_mask, a, scratch, sorted, counts);
+    k<<<(unsigned)blocks, kMThreads, smem, s>>>(d_in, d_mask, a, scratch, o);
     e = cudaGetLastError();
-    if (e == cudaSuccess) {
-      // One warp per block spreads the meshes' warps over the most SMs.
-      mesh_finish_kernel<<<(unsigned)groups, 32, 0, s>>>(a, sorted, counts, o);
-      e = cudaGetLastError();
-    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(bg.data(), o.background, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(rms.data(), o.rms, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fin.data(), o.finite, (size_t)m * 8, cudaMemcpyDeviceToHost, s);

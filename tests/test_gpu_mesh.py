@@ -37,6 +37,9 @@ CASES = [
     ((200, 301), (100, 101), {**PHOTUTILS, "statistic": "median", "center": "mean", "fill": "nearest"}),
     ((130, 200), (7, 9), {"estimator": "sigma_clip", "statistic": "mean", "maxiters": None, "spread": "mad",
                           "sigma_lower": 2.0, "sigma_upper": 1.0, "interpolation": "sextractor"}),
+    # 5,625 meshes, a third masked: the fill runs on several host threads.
+    ((600, 600), (8, 8), PHOTUTILS),
+    ((600, 600), (8, 8), {"fill": "nearest", "min_valid_fraction": 0.9}),
 ]
 
 
