@@ -85,10 +85,6 @@ struct SV {
 };
 
 // Block state of the statistics: per-warp partial sums and a broadcast slot.
-struct W3 {
-  unsigned long long w0, w1, w2;  // 192-bit two's complement, w0 lowest
-};
-
 struct MeshShared {
   W3 part[kMThreads / 32];
   int low[kMThreads / 32];
@@ -112,184 +108,41 @@ __device__ double m_median(SV v, long long n) {
   return finite64(mid) ? mid : __dadd_rn(__ddiv_rn(a, 2.0), __ddiv_rn(b, 2.0));
 }
 
-// ---------------------------------------------------------------------------
-// Block-wide sums equal to the reference's sequential Neumaier sums.
-//
-// The reference adds a mesh's terms x_1..x_n in sorted order with Neumaier's
-// compensation (Sum64, src/mean.rs:7-26): s_i = RN(s_{i-1} + x_i), the error
-// e_i of each addition computed exactly (Fast2Sum with the larger magnitude
-// first), c_n = the rounded running sum of the e_i, result RN(s_n + c_n).
-// With S the exact sum, s_n + sum(e_i) = S, so the result is RN(S + delta),
-// delta = c_n - sum(e_i) the rounding of the correction sum. For n < 2^k
-// terms below 2^H (n < 2^31, no overflow):
-//  * sum|e_i| <= u n (1+u)^n sum|x_i| < 2^(2k + H - 52), u = 2^-53. When
-//    every term is a multiple of 2^Q, so are every s_i, e_i and running sum
-//    of the e_i; with Q >= 2k + H - 105 those running sums stay below
-//    2^(Q + 53), are exact, delta = 0, and the result is RN(S) exactly
-//    (ties included). This is the usual case for image data;
-//  * otherwise |delta| <= gamma_{n-1} sum|e_i| < 2 n^3 u^2 2^H. The block
-//    rounds both ends of [S - E, S + E], E = 2^(3k + 55) units of the fixed
-//    point (more than |delta| plus the n units of truncation); RN is
-//    monotone, so when the ends agree every point between them rounds to the
-//    same double, which is the sequential result.
-// The block adds the terms exactly, in any order, in 192-bit fixed point
-// with lowest bit 2^(H - 158) (bits below it truncated). When neither case
-// decides (S within E of a rounding boundary, huge magnitudes, a result
-// outside the normal range) thread 0 runs the sequential sum.
-
-__device__ __forceinline__ void add3(W3& s, unsigned long long a0, unsigned long long a1, unsigned long long a2) {
-  asm("add.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\taddc.u64 %2, %2, %5;"
-      : "+l"(s.w0), "+l"(s.w1), "+l"(s.w2)
-      : "l"(a0), "l"(a1), "l"(a2));
-}
-
-__device__ __forceinline__ void sub3(W3& s, unsigned long long a0, unsigned long long a1, unsigned long long a2) {
-  asm("sub.cc.u64 %0, %0, %3;\n\tsubc.cc.u64 %1, %1, %4;\n\tsubc.u64 %2, %2, %5;"
-      : "+l"(s.w0), "+l"(s.w1), "+l"(s.w2)
-      : "l"(a0), "l"(a1), "l"(a2));
-}
-
-// s += x / 2^L, |x| truncated to whole units; false when x is not finite or
-// |x| >= 2^(L + 158). `low` takes the exponent of x's lowest set bit.
-__device__ __forceinline__ bool add_fixed(W3& s, double x, int L, int& low) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  if (mag >= 0x7FF0000000000000ull) return false;
-  const int e = (int)(mag >> 52);
-  const unsigned long long m = (mag & 0x000FFFFFFFFFFFFFull) | (e ? 0x0010000000000000ull : 0ull);
-  if (m == 0) return true;
-  const int sh = (e ? e - 1075 : -1074) - L;  // x = m 2^(sh + L)
-  if (sh > 105) return false;
-  low = min(low, sh + L + __ffsll((long long)m) - 1);
-  unsigned long long a0 = 0, a1 = 0, a2 = 0;
-  if (sh < 0) {
-    a0 = sh > -64 ? m >> -sh : 0ull;
-  } else {
-    const int bs = sh & 63;
-    const unsigned long long lo = m << bs, hi = bs ? m >> (64 - bs) : 0ull;
-    if (sh < 64) {
-      a0 = lo;
-      a1 = hi;
-    } else {
-      a1 = lo;
-      a2 = hi;
-    }
-  }
-  if (b >> 63)
-    sub3(s, a0, a1, a2);
-  else
-    add3(s, a0, a1, a2);
-  return true;
-}
-
-// RN(s 2^L) for a 192-bit two's complement s with |s| < 2^190; false when s
-// is zero or the result is not a normal double.
-__device__ __forceinline__ bool fixed_rn(W3 s, int L, double* out) {
-  const bool neg = (long long)s.w2 < 0;
-  if (neg) {
-    s.w0 = ~s.w0;
-    s.w1 = ~s.w1;
-    s.w2 = ~s.w2;
-    add3(s, 1ull, 0ull, 0ull);
-  }
-  int top;
-  if (s.w2)
-    top = 191 - __clzll((long long)s.w2);
-  else if (s.w1)
-    top = 127 - __clzll((long long)s.w1);
-  else if (s.w0)
-    top = 63 - __clzll((long long)s.w0);
-  else
-    return false;
-  // Shift the leading one to bit 191: 53 significand bits, then round and
-  // sticky bits.
-  int z = 191 - top;
-  while (z >= 64) {
-    s.w2 = s.w1;
-    s.w1 = s.w0;
-    s.w0 = 0;
-    z -= 64;
-  }
-  if (z) {
-    s.w2 = (s.w2 << z) | (s.w1 >> (64 - z));
-    s.w1 = (s.w1 << z) | (s.w0 >> (64 - z));
-    s.w0 <<= z;
-  }
-  unsigned long long sig = s.w2 >> 11;
-  const bool half = (s.w2 >> 10) & 1ull;
-  const bool sticky = (s.w2 & 0x3FFull) != 0 || s.w1 != 0 || s.w0 != 0;
-  int exponent = L + top;  // s 2^L in [2^exponent, 2^(exponent + 1))
-  if (half && (sticky || (sig & 1ull))) ++sig;
-  if (sig >> 53) {
-    sig >>= 1;
-    ++exponent;
-  }
-  const int biased = exponent + 1023;
-  if (biased < 1 || biased > 2046) return false;
-  *out = __longlong_as_double((long long)(((unsigned long long)neg << 63) | ((unsigned long long)biased << 52) |
-                                          (sig & 0x000FFFFFFFFFFFFFull)));
-  return true;
-}
-
-// Smallest H with |x| < 2^H (x finite).
-__device__ __forceinline__ int bound_exponent(double x) {
-  const int e = (int)(mag_bits64(x) >> 52);
-  return e ? e - 1022 : -1022;
-}
-
 // The reference's sequential Neumaier sum of term(0..n-1), every |term|
-// below 2^H (a term that is not returns the sequential sum). Called by every
-// thread of the block with the same arguments; returns the same value in all.
+// below 2^H (a term that is not gives the sequential sum): the block adds
+// the terms exactly (ExactSum, in any order) and proves the rounding; thread
+// 0 runs the sequential sum when the proof fails. Called by every thread of
+// the block with the same arguments; returns the same value in all.
 template <typename Term>
 __device__ double block_sum(Term&& term, long long n, int H, MeshShared& sh) {
-  const int L = H - 158;
-  const int k = 64 - __clzll(n);  // n < 2^k
-  bool ok = n >= 1 && n < (1ll << 31) && k + H <= 1000;
-  W3 s{0ull, 0ull, 0ull};
-  int low = INT_MAX;
-  if (ok)
-    for (long long i = threadIdx.x; i < n; i += blockDim.x) ok = add_fixed(s, term(i), L, low) && ok;
+  ExactSum e(H);
+  if (n < (1ll << 31))
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) e.add(term(i));
+  else
+    e.ok = false;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    const unsigned long long b0 = __shfl_down_sync(0xffffffffu, s.w0, off);
-    const unsigned long long b1 = __shfl_down_sync(0xffffffffu, s.w1, off);
-    const unsigned long long b2 = __shfl_down_sync(0xffffffffu, s.w2, off);
-    add3(s, b0, b1, b2);
+    const unsigned long long b0 = __shfl_down_sync(0xffffffffu, e.s.w0, off);
+    const unsigned long long b1 = __shfl_down_sync(0xffffffffu, e.s.w1, off);
+    const unsigned long long b2 = __shfl_down_sync(0xffffffffu, e.s.w2, off);
+    add3(e.s, b0, b1, b2);
   }
-  low = __reduce_min_sync(0xffffffffu, low);
+  e.low = __reduce_min_sync(0xffffffffu, e.low);
   if ((threadIdx.x & 31) == 0) {
-    sh.part[threadIdx.x >> 5] = s;
-    sh.low[threadIdx.x >> 5] = low;
+    sh.part[threadIdx.x >> 5] = e.s;
+    sh.low[threadIdx.x >> 5] = e.low;
   }
-  const bool failed = __syncthreads_or(!ok);
-  W3 total = sh.part[0];
-  low = sh.low[0];
+  e.ok = !__syncthreads_or(!e.ok);
+  e.s = sh.part[0];
+  e.low = sh.low[0];
 #pragma unroll
   for (int w = 1; w < kMThreads / 32; ++w) {
-    add3(total, sh.part[w].w0, sh.part[w].w1, sh.part[w].w2);
-    low = min(low, sh.low[w]);
+    add3(e.s, sh.part[w].w0, sh.part[w].w1, sh.part[w].w2);
+    e.low = min(e.low, sh.low[w]);
   }
   __syncthreads();
-  if (!failed) {
-    double result;
-    if (low >= 2 * k + H - 105) {
-      // Exact correction sum: the result is RN(S).
-      if ((total.w0 | total.w1 | total.w2) == 0ull) return 0.0;
-      if (fixed_rn(total, L, &result)) return result;
-    } else {
-      const int pos = 3 * k + 55;
-      const unsigned long long e0 = pos < 64 ? 1ull << pos : 0ull;
-      const unsigned long long e1 = pos >= 64 && pos < 128 ? 1ull << (pos - 64) : 0ull;
-      const unsigned long long e2 = pos >= 128 ? 1ull << (pos - 128) : 0ull;
-      W3 lo = total, hi = total;
-      sub3(lo, e0, e1, e2);
-      add3(hi, e0, e1, e2);
-      double high;
-      if (fixed_rn(lo, L, &result) && fixed_rn(hi, L, &high) &&
-          __double_as_longlong(result) == __double_as_longlong(high))
-        return result;
-    }
-  }
+  double result;
+  if (e.result(n, &result)) return result;
   double sequential = 0.0;
   if (threadIdx.x == 0) {
     Sum64 sum;

@@ -236,6 +236,47 @@ __device__ double finite_mean(const double* v, int n) {
   return clamp64(__ddiv_rn(scaled.total(), __ddiv_rn((double)n, scale)), lower, upper);
 }
 
+// finite_mean of finite samples `v` whose sorted copy is `s`: the Neumaier
+// total proven from the exact sum (ExactSum), else the sequential code.
+__device__ double finite_mean_exact(const double* v, const double* s, int n) {
+  if (n > 0) {
+    ExactSum e(bound_exponent(fmax(abs64(s[0]), abs64(s[n - 1]))));
+    for (int i = 0; i < n; ++i) e.add(v[i]);
+    double total;
+    if (e.result(n, &total) && finite64(total)) return __ddiv_rn(total, (double)n);
+  }
+  return finite_mean(v, n);
+}
+
+// Sum of the scaled deviations w[0..n) (each at most 1 in magnitude: the
+// scale is their largest magnitude) and of the squared residuals about
+// their mean (each at most 4), in tap order.
+__device__ __forceinline__ double scaled_total(const double* w, int n) {
+  ExactSum e(1);
+  for (int i = 0; i < n; ++i) e.add(w[i]);
+  double total;
+  if (e.result(n, &total)) return total;
+  Sum64 sum;
+  for (int i = 0; i < n; ++i) sum.add(w[i]);
+  return sum.total();
+}
+
+__device__ __forceinline__ double residual_squares(const double* w, int n, double center) {
+  ExactSum e(3);
+  for (int i = 0; i < n; ++i) {
+    const double residual = __dsub_rn(w[i], center);
+    e.add(__dmul_rn(residual, residual));
+  }
+  double total;
+  if (e.result(n, &total)) return total;
+  Sum64 squares;
+  for (int i = 0; i < n; ++i) {
+    const double residual = __dsub_rn(w[i], center);
+    squares.add(__dmul_rn(residual, residual));
+  }
+  return squares.total();
+}
+
 // std_parts, src/robust.rs:594-630, in tap order. `w` keeps each sample's
 // delta / scale between the two sums (the same quotient both times).
 __device__ Scaled std_parts(const double* v, int n, double* w) {
@@ -251,21 +292,12 @@ __device__ Scaled std_parts(const double* v, int n, double* w) {
     scale = fmax(scale, abs64(w[i]));
   }
   if (scale == 0.0) return {0.0, 0};
-  Sum64 sum;
   const Divisor by = make_divisor(scale);
-  for (int i = 0; i < n; ++i) {
-    w[i] = div_by(w[i], by);
-    sum.add(w[i]);
-  }
-  const double center = __ddiv_rn(sum.total(), (double)n);
-  Sum64 squares;
-  for (int i = 0; i < n; ++i) {
-    const double residual = __dsub_rn(w[i], center);
-    squares.add(__dmul_rn(residual, residual));
-  }
+  for (int i = 0; i < n; ++i) w[i] = div_by(w[i], by);
+  const double center = __ddiv_rn(scaled_total(w, n), (double)n);
+  const double squares = residual_squares(w, n, center);
   const Scaled parts = binary_parts(scale);
-  return {__dmul_rn(parts.value, __dsqrt_rn(__ddiv_rn(squares.total(), (double)n))),
-          parts.exponent + (halve ? 1 : 0)};
+  return {__dmul_rn(parts.value, __dsqrt_rn(__ddiv_rn(squares, (double)n))), parts.exponent + (halve ? 1 : 0)};
 }
 
 // mode_from_moments, src/location.rs:56-84.
@@ -291,19 +323,10 @@ __device__ double population_std(const double* v, int n, double* w) {
     scale = fmax(scale, abs64(w[i]));
   }
   if (scale == 0.0) return 0.0;
-  Sum64 sum;
   const Divisor by = make_divisor(scale);
-  for (int i = 0; i < n; ++i) {
-    w[i] = div_by(w[i], by);
-    sum.add(w[i]);
-  }
-  const double center = __ddiv_rn(sum.total(), (double)n);
-  Sum64 squares;
-  for (int i = 0; i < n; ++i) {
-    const double residual = __dsub_rn(w[i], center);
-    squares.add(__dmul_rn(residual, residual));
-  }
-  const double result = __dmul_rn(scale, __dsqrt_rn(__ddiv_rn(squares.total(), (double)n)));
+  for (int i = 0; i < n; ++i) w[i] = div_by(w[i], by);
+  const double center = __ddiv_rn(scaled_total(w, n), (double)n);
+  const double result = __dmul_rn(scale, __dsqrt_rn(__ddiv_rn(residual_squares(w, n, center), (double)n)));
   return halve ? __dmul_rn(result, 2.0) : result;
 }
 
@@ -312,9 +335,7 @@ __device__ double population_std(const double* v, int n, double* w) {
 __device__ double mode_estimate(const double* v, const double* s, int n, int estimator, double pearson,
                                 double* w) {
   if (n == 0) return nan_of(0.0);
-  Reduce r{};
-  r.count = n;
-  const double mean = mom::mean_exact([&](int i) { return v[i]; }, r);
+  const double mean = finite_mean_exact(v, s, n);
   const double std_dev = estimator == kModeSex ? population_std(v, n, w) : nan_of(0.0);
   return mode_from_moments(mean, median_sorted(s, n), std_dev, estimator, pearson);
 }
@@ -361,22 +382,40 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   const double width = __dmul_rn(c, mad);
   factor = __dmul_rn(factor, extra);
   const Divisor by_extra = make_divisor(extra), by_width = make_divisor(width);
+  // The weighted terms lie below 1 in magnitude (|u| < 1, weights in
+  // [0, 1]); the scale's denominator terms in (-4, 1].
   if (location) {
-    Sum64 weighted, weights;
+    ExactSum weighted_e(1), weights_e(1);
+    int kept = 0;
     for (int i = 0; i < n; ++i) {
       const double u = div_by(div_by(dev[i], by_extra), by_width);
       if (!(abs64(u) < 1.0)) continue;
       const double t = __dsub_rn(1.0, __dmul_rn(u, u));
       const double weight = __dmul_rn(t, t);
-      weighted.add(__dmul_rn(u, weight));
-      weights.add(weight);
+      weighted_e.add(__dmul_rn(u, weight));
+      weights_e.add(weight);
+      ++kept;
     }
-    const double correction = __dmul_rn(width, __ddiv_rn(weighted.total(), weights.total()));
+    double weighted_total, weights_total;
+    if (!weighted_e.result(kept, &weighted_total) || !weights_e.result(kept, &weights_total)) {
+      Sum64 weighted, weights;
+      for (int i = 0; i < n; ++i) {
+        const double u = div_by(div_by(dev[i], by_extra), by_width);
+        if (!(abs64(u) < 1.0)) continue;
+        const double t = __dsub_rn(1.0, __dmul_rn(u, u));
+        const double weight = __dmul_rn(t, t);
+        weighted.add(__dmul_rn(u, weight));
+        weights.add(weight);
+      }
+      weighted_total = weighted.total();
+      weights_total = weights.total();
+    }
+    const double correction = __dmul_rn(width, __ddiv_rn(weighted_total, weights_total));
     const double unscaled = __dmul_rn(correction, factor);
     if (finite64(unscaled)) return __dadd_rn(median, unscaled);
     return __dmul_rn(__dadd_rn(__ddiv_rn(median, factor), correction), factor);
   }
-  Sum64 numerator, denominator;
+  ExactSum numerator_e(1), denominator_e(3);
   int kept = 0;
   for (int i = 0; i < n; ++i) {
     const double u = div_by(div_by(dev[i], by_extra), by_width);
@@ -384,12 +423,27 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
     const double u2 = __dmul_rn(u, u);
     const double w = __dsub_rn(1.0, u2);
     const double taper = __dmul_rn(w, w);
-    numerator.add(__dmul_rn(__dmul_rn(u2, taper), taper));
-    denominator.add(__dmul_rn(w, __dsub_rn(1.0, __dmul_rn(5.0, u2))));
+    numerator_e.add(__dmul_rn(__dmul_rn(u2, taper), taper));
+    denominator_e.add(__dmul_rn(w, __dsub_rn(1.0, __dmul_rn(5.0, u2))));
     ++kept;
   }
+  double numerator_total, denominator_total;
+  if (!numerator_e.result(kept, &numerator_total) || !denominator_e.result(kept, &denominator_total)) {
+    Sum64 numerator, denominator;
+    for (int i = 0; i < n; ++i) {
+      const double u = div_by(div_by(dev[i], by_extra), by_width);
+      if (!(abs64(u) < 1.0)) continue;
+      const double u2 = __dmul_rn(u, u);
+      const double w = __dsub_rn(1.0, u2);
+      const double taper = __dmul_rn(w, w);
+      numerator.add(__dmul_rn(__dmul_rn(u2, taper), taper));
+      denominator.add(__dmul_rn(w, __dsub_rn(1.0, __dmul_rn(5.0, u2))));
+    }
+    numerator_total = numerator.total();
+    denominator_total = denominator.total();
+  }
   const double count = (double)(ra.modify_sample_size ? kept : n);
-  const double ratio = __ddiv_rn(__dsqrt_rn(__dmul_rn(count, numerator.total())), abs64(denominator.total()));
+  const double ratio = __ddiv_rn(__dsqrt_rn(__dmul_rn(count, numerator_total)), abs64(denominator_total));
   return __dmul_rn(__dmul_rn(width, ratio), factor);
 }
 
@@ -399,7 +453,7 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
 __device__ double clipped(double* v, double* s, double* w, int n, const RobustArgs& ra, int kind) {
   long long iteration = 0;
   while (n >= ra.clip_min_count && (ra.maxiters < 0 || iteration < ra.maxiters)) {
-    const double center = ra.center == 0 ? finite_mean(v, n) : percentile_sorted(s, n, 50.0);
+    const double center = ra.center == 0 ? finite_mean_exact(v, s, n) : percentile_sorted(s, n, 50.0);
     Scaled spread;
     if (ra.spread == 1) {
       const Scaled deviation = mad_parts(s, n);
@@ -426,7 +480,7 @@ __device__ double clipped(double* v, double* s, double* w, int n, const RobustAr
     if (stable) break;
   }
   if (n < ra.clip_min_count) return nan_of(0.0);
-  if (kind == kRobustSigmaMean) return finite_mean(v, n);
+  if (kind == kRobustSigmaMean) return finite_mean_exact(v, s, n);
   if (kind == kRobustSigmaMedian) return percentile_sorted(s, n, 50.0);
   return mode_estimate(v, s, n, ra.estimator, ra.pearson, w);
 }
