@@ -42,6 +42,37 @@ __device__ __forceinline__ unsigned long long total_key(double v) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// IEEE a == b and a < b on bit patterns (the integer pipe; GB300's float64
+// pipe is narrow): NaN compares false, -0 equals +0.
+__device__ __forceinline__ bool eq64(double a, double b) {
+  if (nan64(a) || nan64(b)) return false;
+  return (mag_bits64(a) | mag_bits64(b)) == 0ull || __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+__device__ __forceinline__ bool lt64(double a, double b) {
+  if (nan64(a) || nan64(b) || (mag_bits64(a) | mag_bits64(b)) == 0ull) return false;
+  return total_key(a) < total_key(b);
+}
+
+// RN(2 v): one more in the exponent field for normal v below the overflow
+// threshold (exact), the float64 multiply otherwise.
+__device__ __forceinline__ double twice(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned int e = (unsigned int)((b >> 52) & 0x7FF);
+  if (e >= 1 && e < 2046) return __longlong_as_double((long long)(b + (1ull << 52)));
+  return __dmul_rn(v, 2.0);
+}
+
+// A float or float64 sample as float64: normal and zero floats by integer
+// operations (exact), the rest by the hardware conversion.
+__device__ __forceinline__ double widen(float x) {
+  const unsigned int b = __float_as_uint(x);
+  const unsigned int e = (b >> 23) & 0xFFu;
+  if ((e != 0u && e != 255u) || (b << 1) == 0u) return f32_to_f64_exact(b);
+  return (double)x;
+}
+__device__ __forceinline__ double widen(double x) { return x; }
+
 __device__ __forceinline__ int total_cmp(double a, double b) {
   const unsigned long long ka = total_key(a), kb = total_key(b);
   return ka < kb ? -1 : (ka > kb ? 1 : 0);
@@ -89,8 +120,9 @@ __device__ __forceinline__ double inf64() { return __longlong_as_double(0x7ff000
 
 // absolute_deviation, src/robust.rs:438-466.
 __device__ Scaled absolute_deviation(double value, Scaled center) {
-  if (center.exponent == -1 && finite64(__dmul_rn(value, 2.0))) {
-    const double difference = __dsub_rn(__dmul_rn(value, 2.0), center.value);
+  const double doubled = twice(value);
+  if (center.exponent == -1 && finite64(doubled)) {
+    const double difference = __dsub_rn(doubled, center.value);
     if (finite64(difference)) return {abs64(difference), -1};
   }
   const double midpoint = center.exponent == -1 ? __dmul_rn(center.value, 0.5) : center.value;
@@ -101,7 +133,8 @@ __device__ Scaled absolute_deviation(double value, Scaled center) {
 
 // compare_scaled, src/robust.rs:468-481.
 __device__ int compare_scaled(Scaled left, Scaled right) {
-  if (left.value == 0.0 || right.value == 0.0 || inf64_test(left.value) || inf64_test(right.value))
+  if (mag_bits64(left.value) == 0ull || mag_bits64(right.value) == 0ull || inf64_test(left.value) ||
+      inf64_test(right.value))
     return total_cmp(left.value, right.value);
   const Scaled l = binary_parts(left.value), r = binary_parts(right.value);
   const int a = l.exponent + left.exponent, b = r.exponent + right.exponent;
@@ -189,7 +222,7 @@ __device__ Limit make_limit(Scaled spread, double sigma) {
 }
 
 __device__ __forceinline__ bool inside(double value, double center, const Limit& l) {
-  if (value == center) return true;
+  if (eq64(value, center)) return true;
   if (l.zero) return false;
   const double difference = __dsub_rn(value, center);
   Scaled d;
@@ -277,20 +310,33 @@ __device__ __forceinline__ double residual_squares(const double* w, int n, doubl
   return squares.total();
 }
 
+// The deltas v[i] - v[0] into w (all halved first when one overflows, as
+// std_parts and dispersion_valid do) and their largest magnitude.
+__device__ __forceinline__ double deltas(const double* v, int n, double* w, bool* halve) {
+  const double reference = v[0];
+  bool over = false;
+  unsigned long long peak = 0ull;
+  for (int i = 0; i < n; ++i) {
+    w[i] = __dsub_rn(v[i], reference);
+    over = over || !finite64(w[i]);
+    peak = max(peak, mag_bits64(w[i]));
+  }
+  if (over) {
+    peak = 0ull;
+    for (int i = 0; i < n; ++i) {
+      w[i] = __dsub_rn(__dmul_rn(v[i], 0.5), __dmul_rn(reference, 0.5));
+      peak = max(peak, mag_bits64(w[i]));
+    }
+  }
+  *halve = over;
+  return __longlong_as_double((long long)peak);
+}
+
 // std_parts, src/robust.rs:594-630, in tap order. `w` keeps each sample's
 // delta / scale between the two sums (the same quotient both times).
 __device__ Scaled std_parts(const double* v, int n, double* w) {
-  const double reference = v[0];
-  bool halve = false;
-  for (int i = 0; i < n; ++i) halve = halve || !finite64(__dsub_rn(v[i], reference));
-  auto delta = [&](double x) {
-    return halve ? __dsub_rn(__dmul_rn(x, 0.5), __dmul_rn(reference, 0.5)) : __dsub_rn(x, reference);
-  };
-  double scale = 0.0;
-  for (int i = 0; i < n; ++i) {
-    w[i] = delta(v[i]);
-    scale = fmax(scale, abs64(w[i]));
-  }
+  bool halve;
+  const double scale = deltas(v, n, w, &halve);
   if (scale == 0.0) return {0.0, 0};
   const Divisor by = make_divisor(scale);
   for (int i = 0; i < n; ++i) w[i] = div_by(w[i], by);
@@ -314,14 +360,8 @@ __device__ double mode_from_moments(double mean, double median, double std_dev, 
 // dispersion_valid(values, 0, true), src/dispersion.rs:5-61, for finite
 // samples in tap order; `w` keeps each delta / scale between the two sums.
 __device__ double population_std(const double* v, int n, double* w) {
-  const double reference = v[0];
-  bool halve = false;
-  for (int i = 0; i < n; ++i) halve = halve || !finite64(__dsub_rn(v[i], reference));
-  double scale = 0.0;
-  for (int i = 0; i < n; ++i) {
-    w[i] = halve ? __dsub_rn(__dmul_rn(v[i], 0.5), __dmul_rn(reference, 0.5)) : __dsub_rn(v[i], reference);
-    scale = fmax(scale, abs64(w[i]));
-  }
+  bool halve;
+  const double scale = deltas(v, n, w, &halve);
   if (scale == 0.0) return 0.0;
   const Divisor by = make_divisor(scale);
   for (int i = 0; i < n; ++i) w[i] = div_by(w[i], by);
@@ -358,12 +398,12 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   // Median of |dev|: the deviations ascend, so their magnitudes ascend
   // outwards from the smallest; merge both sides up to the middle ranks.
   int right = 0;
-  while (right < n && dev[right] < 0.0) ++right;
+  while (right < n && lt64(dev[right], 0.0)) ++right;
   int left = right;
   double a = 0.0, b = 0.0;
   for (int k = 0; k <= n / 2; ++k) {
     double next;
-    if (left > 0 && (right == n || abs64(dev[left - 1]) <= abs64(dev[right]))) {
+    if (left > 0 && (right == n || mag_bits64(dev[left - 1]) <= mag_bits64(dev[right]))) {
       next = abs64(dev[--left]);
     } else {
       next = abs64(dev[right++]);
@@ -382,14 +422,15 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   const double width = __dmul_rn(c, mad);
   factor = __dmul_rn(factor, extra);
   const Divisor by_extra = make_divisor(extra), by_width = make_divisor(width);
+  const bool unit_extra = extra == 1.0;  // x / 1 is x exactly
   // The weighted terms lie below 1 in magnitude (|u| < 1, weights in
   // [0, 1]); the scale's denominator terms in (-4, 1].
   if (location) {
     ExactSum weighted_e(1), weights_e(1);
     int kept = 0;
     for (int i = 0; i < n; ++i) {
-      const double u = div_by(div_by(dev[i], by_extra), by_width);
-      if (!(abs64(u) < 1.0)) continue;
+      const double u = div_by(unit_extra ? dev[i] : div_by(dev[i], by_extra), by_width);
+      if (!(mag_bits64(u) < 0x3FF0000000000000ull)) continue;
       const double t = __dsub_rn(1.0, __dmul_rn(u, u));
       const double weight = __dmul_rn(t, t);
       weighted_e.add(__dmul_rn(u, weight));
@@ -400,8 +441,8 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
     if (!weighted_e.result(kept, &weighted_total) || !weights_e.result(kept, &weights_total)) {
       Sum64 weighted, weights;
       for (int i = 0; i < n; ++i) {
-        const double u = div_by(div_by(dev[i], by_extra), by_width);
-        if (!(abs64(u) < 1.0)) continue;
+        const double u = div_by(unit_extra ? dev[i] : div_by(dev[i], by_extra), by_width);
+        if (!(mag_bits64(u) < 0x3FF0000000000000ull)) continue;
         const double t = __dsub_rn(1.0, __dmul_rn(u, u));
         const double weight = __dmul_rn(t, t);
         weighted.add(__dmul_rn(u, weight));
@@ -418,8 +459,8 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   ExactSum numerator_e(1), denominator_e(3);
   int kept = 0;
   for (int i = 0; i < n; ++i) {
-    const double u = div_by(div_by(dev[i], by_extra), by_width);
-    if (!(abs64(u) < 1.0)) continue;
+    const double u = div_by(unit_extra ? dev[i] : div_by(dev[i], by_extra), by_width);
+    if (!(mag_bits64(u) < 0x3FF0000000000000ull)) continue;
     const double u2 = __dmul_rn(u, u);
     const double w = __dsub_rn(1.0, u2);
     const double taper = __dmul_rn(w, w);
@@ -431,8 +472,8 @@ __device__ double biweight(const double* s, int n, double* dev, const RobustArgs
   if (!numerator_e.result(kept, &numerator_total) || !denominator_e.result(kept, &denominator_total)) {
     Sum64 numerator, denominator;
     for (int i = 0; i < n; ++i) {
-      const double u = div_by(div_by(dev[i], by_extra), by_width);
-      if (!(abs64(u) < 1.0)) continue;
+      const double u = div_by(unit_extra ? dev[i] : div_by(dev[i], by_extra), by_width);
+      if (!(mag_bits64(u) < 0x3FF0000000000000ull)) continue;
       const double u2 = __dmul_rn(u, u);
       const double w = __dsub_rn(1.0, u2);
       const double taper = __dmul_rn(w, w);
@@ -470,9 +511,9 @@ __device__ double clipped(double* v, double* s, double* w, int n, const RobustAr
     int kept = 0, kept_sorted = 0;
     for (int i = 0; i < n; ++i) {
       const double x = v[i];
-      if (inside(x, center, x < center ? below : above)) v[kept++] = x;
+      if (inside(x, center, lt64(x, center) ? below : above)) v[kept++] = x;
       const double y = s[i];
-      if (inside(y, center, y < center ? below : above)) s[kept_sorted++] = y;
+      if (inside(y, center, lt64(y, center) ? below : above)) s[kept_sorted++] = y;
     }
     ++iteration;
     const bool stable = kept == n;
@@ -549,15 +590,15 @@ __global__ void __launch_bounds__(kRThreads)
       interior = interior && coord[d] + a.low[d] >= 0 && coord[d] + a.high[d] < a.shape[d];
     }
     auto fetch = [&](int i) -> double {
-      if (interior) return (double)__ldg(in + o + flat[i]);
+      if (interior) return widen(__ldg(in + o + flat[i]));
       const long long* tap = taps + (long long)i * rank;
       long long src = 0;
       for (int d = 0; d < rank; ++d) {
         long long m;
-        if (!map_index(coord[d] + tap[d], a.shape[d], a.mode[d], &m)) return (double)cval;
+        if (!map_index(coord[d] + tap[d], a.shape[d], a.mode[d], &m)) return widen(cval);
         src += m * a.stride[d];
       }
-      return (double)__ldg(in + src);
+      return widen(__ldg(in + src));
     };
     const double result = robust_window(fetch, V, a.r, ra, v, s, w);
     T value;
