@@ -269,6 +269,19 @@ int ndf_plan_compute_download(ndf_plan* plan, void* h_out);
  * "tile_radix", "histogram", "moments_tile", "generic", ...). */
 const char* ndf_plan_algorithm(const ndf_plan* plan);
 
+/* Number of row bands ndf_plan_run_host pipelines (uploads, kernels and
+ * downloads of successive bands overlap); 0 while it runs the whole array in
+ * one piece. A plan tries bands on its third host-buffer run and keeps them
+ * when that run was at least 5% faster than the second (whole-array) one;
+ * they apply to arrays of at least 16 MiB with 256 or more rows per band,
+ * exact statistics (not the float32-compensated moments) and a first-axis
+ * mode other than wrap. No counterpart in the reference. */
+int32_t ndf_plan_host_bands(const ndf_plan* plan);
+
+/* Band policy of ndf_plan_run_host: 0 never, 1 the timed choice above
+ * (default), 2 always where bands apply (from the next run on). */
+int ndf_plan_set_host_bands(ndf_plan* plan, int32_t mode);
+
 /* ---- Batched persistent path. Many images of uneven sizes, each with its
  * own window, footprint and reduction, run as one persistent launch per
  * kernel family (register networks, radix select, moments) plus one launch

@@ -178,6 +178,10 @@ def _load() -> tuple[ctypes.CDLL, ctypes.PyDLL]:
                 handle.ndf_plan_compute_download.restype = ctypes.c_int
                 handle.ndf_plan_algorithm.argtypes = [plan_p]
                 handle.ndf_plan_algorithm.restype = ctypes.c_char_p
+                handle.ndf_plan_host_bands.argtypes = [plan_p]
+                handle.ndf_plan_host_bands.restype = ctypes.c_int32
+                handle.ndf_plan_set_host_bands.argtypes = [plan_p, ctypes.c_int32]
+                handle.ndf_plan_set_host_bands.restype = ctypes.c_int
                 handle.ndf_get_num_threads.restype = ctypes.c_int32
                 handle.ndf_device_info.argtypes = [
                     ctypes.POINTER(ctypes.c_int32),
@@ -362,6 +366,21 @@ class Plan:
     def algorithm(self) -> str:
         lib, _ = _load()
         return lib.ndf_plan_algorithm(self._handle).decode()
+
+    @property
+    def host_bands(self) -> int:
+        """Row bands ``run_host_async`` pipelines (0: the whole array at once)."""
+        lib, _ = _load()
+        return int(lib.ndf_plan_host_bands(self._handle))
+
+    def set_host_bands(self, mode: str) -> None:
+        """Band policy of ``run_host_async``: 'never', 'timed' (default: tried
+        on the third run, kept when faster) or 'always' (where bands apply)."""
+        lib, _ = _load()
+        modes = {"never": 0, "timed": 1, "always": 2}
+        if mode not in modes:
+            raise ValueError("band mode must be 'never', 'timed' or 'always'")
+        _check(lib.ndf_plan_set_host_bands(self._handle, modes[mode]), lib)
 
     @property
     def handle(self) -> ctypes.c_void_p:

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -312,6 +313,8 @@ int upload_tile_taps(Plan& p) {
 }
 
 void release(Plan& p) {
+  p.strips.reset();
+  p.strips_tried = false;
   if (p.d_tile_taps) cudaFree(p.d_tile_taps);
   if (p.d_gen_taps) cudaFree(p.d_gen_taps);
   if (p.d_in) cudaFree(p.d_in);
@@ -839,6 +842,172 @@ void plan_release(Plan& p) { release(p); }
 int plan_run(const Plan& p, const void* in, void* out, cudaStream_t s) { return run_plan(p, in, out, s); }
 int plan_apply(Plan& p, const Candidate& c, int smem_limit) { return apply_candidate_impl(p, c, smem_limit); }
 
+// ---------------------------------------------------------------------------
+// Host-buffer runs in row bands.
+//
+// A host-buffer run copies the array in, filters it and copies the result
+// out; done in that order the host link idles during the kernel and carries
+// one direction at a time. Split along the first axis into overlapping bands
+// (each band's input reaches as far as its kept outputs' windows), each band
+// filtered by a plan of its own over the band, the uploads of later bands,
+// the kernels and the downloads of earlier bands overlap on three streams,
+// and both directions of the link run at once. Every kept output's window
+// lies inside its band's real rows except at the array's own first and last
+// rows, where the band's edge is the array's edge, so boundary modes behave
+// as for the whole array. Not used for the wrap mode along the first axis
+// (its windows reach the far edge), for float32-compensated moments (their
+// per-tile pivots make the last bits depend on the tiling), for robust
+// windows beyond 256 samples (their per-plan scratch), or for small arrays.
+// Bands pay for recomputing their overlaps and for smaller launches, which
+// costs more than it saves for kernels slower than the copies (wide
+// histograms, the rolling-mean band kernel): a plan times its second
+// host-buffer run (whole array) and its third (bands) and keeps the bands
+// when they were at least 5% faster.
+struct StripSet {
+  struct Band {
+    Plan plan;
+    long long in_row0 = 0, in_rows = 0;    // rows the band's plan filters
+    long long out_row0 = 0, out_rows = 0;  // rows it keeps
+    long long upload_end = 0;              // rows uploaded before it runs
+    size_t out_offset = 0;                 // its outputs in `out` (elements)
+  };
+  std::vector<Band> bands;
+  void* out = nullptr;
+  cudaStream_t up = nullptr, down = nullptr;
+  std::vector<cudaEvent_t> uploaded, filtered;
+  cudaEvent_t start = nullptr, done = nullptr;
+  ~StripSet() {
+    for (Band& b : bands) release(b.plan);
+    if (out) cudaFree(out);
+    for (cudaEvent_t e : uploaded) cudaEventDestroy(e);
+    for (cudaEvent_t e : filtered) cudaEventDestroy(e);
+    if (start) cudaEventDestroy(start);
+    if (done) cudaEventDestroy(done);
+    if (up) cudaStreamDestroy(up);
+    if (down) cudaStreamDestroy(down);
+  }
+};
+
+constexpr int kMaxBands = 8;
+constexpr size_t kBandMinBytes = 16u << 20;
+
+// Bands for `p`, or none (an empty set) when banding does not apply.
+int build_strips(Plan& p) {
+  p.strips_tried = true;
+  if (p.algo == Algo::kEmpty || p.ndim < 1 || p.modes[0] == NDF_MODE_WRAP) return NDF_OK;
+  if (is_moment(p.r.kind) && p.r.moments == 0) return NDF_OK;
+  if (p.robust_threads > 0) return NDF_OK;  // per-thread scratch of up to 1 GiB per plan
+  const size_t bytes = (size_t)p.n_out * element_bytes(p);
+  if (bytes < kBandMinBytes) return NDF_OK;
+  long long low = 0, high = 0;  // input rows reached above / below an output
+  for (size_t t = 0; t < p.taps.size(); t += (size_t)p.ndim) {
+    low = std::min(low, p.taps[t]);
+    high = std::max(high, p.taps[t]);
+  }
+  const long long rows = p.shape[0];
+  const long long min_rows = std::max(256ll, 8 * (high - low + 1));
+  const long long count = std::min<long long>(kMaxBands, rows / min_rows);
+  if (count < 2) return NDF_OK;
+  int device = 0, sm_count = 0, smem_limit = 0;
+  int rc = ensure_device(&device, &sm_count, &smem_limit);
+  if (rc != NDF_OK) return rc;
+  auto set = std::make_shared<StripSet>();
+  set->bands.resize((size_t)count);
+  size_t total = 0;
+  long long uploaded = 0;
+  for (long long i = 0; i < count; ++i) {
+    StripSet::Band& b = set->bands[(size_t)i];
+    b.out_row0 = rows * i / count;
+    b.out_rows = rows * (i + 1) / count - b.out_row0;
+    b.in_row0 = std::max(0ll, b.out_row0 + low);
+    const long long end = std::min(rows, b.out_row0 + b.out_rows + high);
+    b.in_rows = end - b.in_row0;
+    uploaded = std::max(uploaded, end);
+    b.upload_end = uploaded;
+    // The band's plan: the array's configuration over the band's rows.
+    b.plan = p;
+    Plan& q = b.plan;
+    q.strips.reset();
+    q.strips_tried = true;
+    q.d_tile_taps = nullptr;
+    q.d_gen_taps = nullptr;
+    q.d_in = q.d_out = q.d_scratch = nullptr;
+    q.buffer_bytes = q.scratch_bytes = 0;
+    q.d_status = nullptr;
+    q.d_hist_lists = nullptr;
+    q.d_pct = nullptr;
+    q.r.pct = nullptr;
+    q.shape[0] = b.in_rows;
+    q.n_out = p.n_out / rows * b.in_rows;
+    q.device = device;
+    q.sm_count = sm_count;
+    rc = choose_algorithm(q, smem_limit);
+    if (rc != NDF_OK) return rc;
+    b.out_offset = total;
+    total += (size_t)q.n_out;
+  }
+  cudaError_t e = cudaMalloc(&set->out, total * element_bytes(p));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&set->up, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&set->down, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&set->start, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&set->done, cudaEventDisableTiming);
+  for (long long i = 0; i < count && e == cudaSuccess; ++i) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming);
+    if (e == cudaSuccess) set->uploaded.push_back(a);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming);
+    if (e == cudaSuccess) set->filtered.push_back(b);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return NDF_OK;  // the whole-array path runs instead
+  }
+  p.strips = std::move(set);
+  return NDF_OK;
+}
+
+int run_host_strips(Plan& p, const void* h_in, void* h_out, cudaStream_t s) {
+  StripSet& set = *p.strips;
+  const size_t row_bytes = (size_t)(p.n_out / p.shape[0]) * element_bytes(p);
+  const char* src = static_cast<const char*>(h_in);
+  char* dst = static_cast<char*>(h_out);
+  char* d_in = static_cast<char*>(p.d_in);
+  char* d_out = static_cast<char*>(set.out);
+  cudaError_t e = cudaEventRecord(set.start, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(set.up, set.start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(set.down, set.start, 0);
+  long long uploaded = 0;
+  for (size_t i = 0; i < set.bands.size() && e == cudaSuccess; ++i) {
+    const StripSet::Band& b = set.bands[i];
+    if (b.upload_end > uploaded) {
+      e = cudaMemcpyAsync(d_in + uploaded * row_bytes, src + uploaded * row_bytes,
+                          (size_t)(b.upload_end - uploaded) * row_bytes, cudaMemcpyHostToDevice, set.up);
+      uploaded = b.upload_end;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(set.uploaded[i], set.up);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, set.uploaded[i], 0);
+    if (e != cudaSuccess) break;
+    const int rc = run_plan(b.plan, d_in + b.in_row0 * row_bytes, d_out + b.out_offset * element_bytes(p), s);
+    if (rc != NDF_OK) return rc;
+    e = cudaEventRecord(set.filtered[i], s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "band upload");
+  prefault_output(h_out, (size_t)p.n_out * element_bytes(p));  // overlaps the uploads and kernels
+  for (size_t i = 0; i < set.bands.size() && e == cudaSuccess; ++i) {
+    const StripSet::Band& b = set.bands[i];
+    e = cudaStreamWaitEvent(set.down, set.filtered[i], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dst + b.out_row0 * row_bytes,
+                          d_out + b.out_offset * element_bytes(p) + (b.out_row0 - b.in_row0) * row_bytes,
+                          (size_t)b.out_rows * row_bytes, cudaMemcpyDeviceToHost, set.down);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(set.done, set.down);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, set.done, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "band download");
+  return check_status();
+}
+
 }  // namespace ndf
 
 using namespace ndf;
@@ -904,6 +1073,22 @@ const char* ndf_plan_algorithm(const ndf_plan* plan) {
   return plan ? algo_name(plan->p.algo) : "none";
 }
 
+int32_t ndf_plan_host_bands(const ndf_plan* plan) {
+  return plan && plan->p.strips ? (int32_t)plan->p.strips->bands.size() : 0;
+}
+
+int ndf_plan_set_host_bands(ndf_plan* plan, int32_t mode) {
+  if (!plan) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan");
+  if (mode < 0 || mode > 2) return fail(NDF_ERR_INVALID_CONFIGURATION, "band mode must be 0, 1 or 2");
+  Plan& p = plan->p;
+  p.band_mode = mode;
+  p.strips.reset();
+  p.strips_tried = false;
+  p.strips_decided = false;
+  p.host_runs = 0;
+  return NDF_OK;
+}
+
 int ndf_plan_run(ndf_plan* plan, const void* d_in, void* d_out, void* stream) {
   if (!plan) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan");
   if (plan->p.n_out == 0) return NDF_OK;
@@ -944,6 +1129,25 @@ int ndf_plan_run_host(ndf_plan* plan, const void* h_in, void* h_out, void* strea
   int rc = ensure_buffers(p);
   if (rc != NDF_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  ++p.host_runs;
+  if (!p.strips_tried && p.band_mode != 0 && (p.host_runs >= 3 || p.band_mode == 2)) {
+    rc = build_strips(p);
+    if (rc != NDF_OK) return rc;
+  }
+  const auto begin = std::chrono::steady_clock::now();
+  auto elapsed_ms = [&] {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - begin).count();
+  };
+  if (p.strips) {
+    rc = run_host_strips(p, h_in, h_out, s);
+    if (rc == NDF_OK && !p.strips_decided && p.band_mode == 1) {
+      p.strips_decided = true;
+      // Kept when at least 5% faster than the whole-array run (a single
+      // timing each; kernel-bound plans gain little and lose to noise).
+      if (elapsed_ms() >= 0.95 * p.whole_ms) p.strips.reset();
+    }
+    return rc;
+  }
   size_t bytes = (size_t)p.n_out * element_bytes(p);
   cudaError_t e = cudaMemcpyAsync(p.d_in, h_in, bytes, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(input)");
@@ -954,6 +1158,7 @@ int ndf_plan_run_host(ndf_plan* plan, const void* h_in, void* h_out, void* strea
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(output)");
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  if (p.host_runs == 2) p.whole_ms = elapsed_ms();
   return check_status();
 }
 

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -129,6 +130,8 @@ enum class Algo {
   kRobust,        // MAD, sigma clipping, mode, biweight: per-window float64
 };
 
+struct StripSet;  // row bands of host-buffer runs (capi.cu)
+
 struct Plan {
   // Validated description.
   int dtype = 0;
@@ -180,6 +183,16 @@ struct Plan {
   int ext_rows[2] = {0, 0};  // rows per block of the two extrema column passes
   RobustArgs robust{};       // robust estimator parameters
   long long robust_threads = 0;  // threads of the scratch-backed robust kernel
+
+  // Host-buffer runs in overlapping row bands: built on a plan's third
+  // host-buffer run (one-shot calls skip the setup), timed against the
+  // second (whole-array) run, and kept only when 5% faster.
+  std::shared_ptr<StripSet> strips;
+  bool strips_tried = false;
+  bool strips_decided = false;
+  int band_mode = 1;  // 0: never, 1: timed choice, 2: always (where they apply)
+  int host_runs = 0;
+  double whole_ms = 0.0;
 };
 
 const char* algo_name(Algo a);
