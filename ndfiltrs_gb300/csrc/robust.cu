@@ -91,6 +91,47 @@ __device__ void sort_total(double* a, int n) {
   }
 }
 
+// The same order for up to 32 samples without thread-local traffic in the
+// inner loop: total-order keys in registers through the Batcher network
+// (slots past n hold the largest key and sort last), written back in order.
+__device__ __forceinline__ void sort_total32(const double* v, double* s, int n) {
+  unsigned long long k[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) k[i] = i < n ? total_key(v[i]) : ~0ull;
+  net::batcher_sort<32>(k);
+#pragma unroll
+  for (int i = 0; i < 32; ++i)
+    if (i < n) s[i] = __longlong_as_double((long long)((k[i] >> 63) ? (k[i] & 0x7FFFFFFFFFFFFFFFull) : ~k[i]));
+}
+
+// Up to 64 samples: each half sorted as above into `w` as keys, then one
+// merge of the two runs into `s`.
+__device__ __forceinline__ void sort_total64(const double* v, double* s, double* w, int n) {
+  unsigned long long* runs = reinterpret_cast<unsigned long long*>(w);
+  const int first = n < 32 ? n : 32;
+#pragma unroll 1
+  for (int half = 0; half < 2; ++half) {
+    const int base = half * 32, count = half == 0 ? first : n - first;
+    unsigned long long k[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) k[i] = i < count ? total_key(v[base + i]) : ~0ull;
+    net::batcher_sort<32>(k);
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      if (i < count) runs[base + i] = k[i];
+  }
+  int a = 0, b = 32;
+  const int b_end = 32 + (n - first);
+  for (int o = 0; o < n; ++o) {
+    unsigned long long key;
+    if (b >= b_end || (a < first && runs[a] <= runs[b]))
+      key = runs[a++];
+    else
+      key = runs[b++];
+    s[o] = __longlong_as_double((long long)((key >> 63) ? (key & 0x7FFFFFFFFFFFFFFFull) : ~key));
+  }
+}
+
 // 2^n by binary powering with a final reciprocal for negative n: exact
 // unless 2^|n| overflows, when the reciprocal is zero.
 __device__ double powi2(int n) {
@@ -527,7 +568,7 @@ __device__ double clipped(double* v, double* s, double* w, int n, const RobustAr
 }
 
 // One window: gather, the sample policy, the estimator.
-template <typename Fetch>
+template <int MAXV, bool MERGE, typename Fetch>
 __device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const RobustArgs& ra, double* v,
                                 double* s, double* w) {
   const bool clip = ra.kind >= kRobustSigmaMean;
@@ -550,8 +591,14 @@ __device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const Rob
   if (!clip) {
     if (nan || (r.omit && n < r.min_count) || n == 0) return nan_of(0.0);
   }
-  for (int i = 0; i < n; ++i) s[i] = v[i];
-  sort_total(s, n);
+  if constexpr (MAXV == 32) {
+    sort_total32(v, s, n);
+  } else if constexpr (MAXV == 64 && MERGE) {
+    sort_total64(v, s, w, n);
+  } else {
+    for (int i = 0; i < n; ++i) s[i] = v[i];
+    sort_total(s, n);
+  }
   switch (ra.kind) {
     case kRobustMad:
       return multiply_scaled(mad_parts(s, n), ra.parameter);
@@ -566,7 +613,7 @@ __device__ double robust_window(Fetch&& fetch, int V, const Reduce& r, const Rob
 }
 
 // MAXV > 0: thread-local arrays; MAXV == 0: per-thread slices of `scratch`.
-template <typename T, int MAXV>
+template <typename T, int MAXV, bool MERGE>
 __global__ void __launch_bounds__(kRThreads)
     robust_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ GenericArgs a,
                   const long long* __restrict__ taps, const __grid_constant__ RobustArgs ra,
@@ -600,7 +647,7 @@ __global__ void __launch_bounds__(kRThreads)
       }
       return widen(__ldg(in + src));
     };
-    const double result = robust_window(fetch, V, a.r, ra, v, s, w);
+    const double result = robust_window<MAXV, MERGE>(fetch, V, a.r, ra, v, s, w);
     T value;
     if constexpr (sizeof(T) == 4)
       value = nan64(result) ? nan_of(0.0f) : __double2float_rn(result);
@@ -610,13 +657,13 @@ __global__ void __launch_bounds__(kRThreads)
   }
 }
 
-template <typename T, int MAXV>
+template <typename T, int MAXV, bool MERGE = false>
 cudaError_t launch_robust_v(const Plan& p, const T* in, T* out, cudaStream_t s) {
   const long long blocks = MAXV > 0 ? std::max(1ll, std::min((p.n_out + kRThreads - 1) / kRThreads,
                                                              (long long)std::max(1, p.sm_count) * 16))
                                     : p.robust_threads / kRThreads;
-  robust_kernel<T, MAXV><<<(unsigned)blocks, kRThreads, 0, s>>>(in, out, p.generic, p.d_gen_taps, p.robust,
-                                                                 reinterpret_cast<double*>(p.d_scratch));
+  robust_kernel<T, MAXV, MERGE><<<(unsigned)blocks, kRThreads, 0, s>>>(in, out, p.generic, p.d_gen_taps, p.robust,
+                                                                        reinterpret_cast<double*>(p.d_scratch));
   return cudaGetLastError();
 }
 
@@ -624,7 +671,12 @@ template <typename T>
 cudaError_t launch_robust_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   const int V = p.r.count;
   if (V <= 32) return launch_robust_v<T, 32>(p, in, out, s);
-  if (V <= 64) return launch_robust_v<T, 64>(p, in, out, s);
+  // Windows of 33-64 samples: the merged register sort, except for the
+  // clipping kinds, whose iterations run faster in the kernel without it
+  // (fewer registers).
+  if (V <= 64)
+    return p.robust.kind >= kRobustSigmaMean ? launch_robust_v<T, 64, false>(p, in, out, s)
+                                             : launch_robust_v<T, 64, true>(p, in, out, s);
   if (V <= 128) return launch_robust_v<T, 128>(p, in, out, s);
   if (V <= 256) return launch_robust_v<T, 256>(p, in, out, s);
   return launch_robust_v<T, 0>(p, in, out, s);

@@ -79,8 +79,12 @@ def _oracle(oracle, array, kind, size, footprint, origin, mode, cval, omit, igno
 def test_robust_matches_oracle(gpu, oracle, kind, dtype) -> None:
     radius2 = np.add.outer(np.arange(-3, 4) ** 2, np.arange(-3, 4) ** 2)
     ring = (radius2 <= 9) & (radius2 > 2)
+    # Windows of 25, 28, 9, 18 (register sort of 32), 49 and 64 (two
+    # register-sorted runs merged) and 121 samples (insertion sort).
     cases = [((23, 31), (5, 5), None, (1, -2)), ((19, 26), None, ring, (0, 1)),
-             ((40,), (9,), None, (3,)), ((5, 7, 6), (3, 2, 3), None, (0, 0, -1))]
+             ((40,), (9,), None, (3,)), ((5, 7, 6), (3, 2, 3), None, (0, 0, -1)),
+             ((21, 19), (7, 7), None, (-1, 2)), ((18, 20), (8, 8), None, (0, -3)),
+             ((17, 16), (11, 11), None, (0, 0))]
     clip = kind.startswith("sigma")
     for shape, size, footprint, origin in cases:
         values = _values(shape, dtype, seed=len(shape) * 13 + (size or (0,))[0])
