@@ -369,17 +369,16 @@ __global__ void __launch_bounds__(kMThreads)
     while (padded < n) padded <<= 1;
     for (unsigned int i = n + threadIdx.x; i < padded; i += blockDim.x) keys[i] = ~0ull;
     __syncthreads();
-    // Bitonic sort, ascending.
+    // Bitonic sort, ascending: each stage's padded / 2 compare-exchanges
+    // (i, i + j), i with bit j clear, spread over the block.
     for (unsigned int k = 2; k <= padded; k <<= 1) {
       for (unsigned int j = k >> 1; j > 0; j >>= 1) {
-        for (unsigned int i = threadIdx.x; i < padded; i += blockDim.x) {
-          const unsigned int ixj = i ^ j;
-          if (ixj > i) {
-            const unsigned long long x = keys[i], y = keys[ixj];
-            if ((x > y) == ((i & k) == 0)) {
-              keys[i] = y;
-              keys[ixj] = x;
-            }
+        for (unsigned int p = threadIdx.x; p < padded / 2; p += blockDim.x) {
+          const unsigned int i = 2 * p - (p & (j - 1));
+          const unsigned long long x = keys[i], y = keys[i + j];
+          if ((x > y) == ((i & k) == 0)) {
+            keys[i] = y;
+            keys[i + j] = x;
           }
         }
         __syncthreads();
