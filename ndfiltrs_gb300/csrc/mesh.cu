@@ -39,6 +39,7 @@
 
 #include "../../include/ndfiltrs_gb300.h"
 #include "common.cuh"
+#include "hostpool.h"
 #include "moments.cuh"
 #include "plan.h"
 
@@ -1171,12 +1172,26 @@ int ndf_mesh_background(const void* h_in, const uint8_t* h_mask, int32_t dtype, 
     cudaGetLastError();
     return fail(NDF_ERR_MEMORY, "unable to allocate filtering workspace");
   }
+  // Fresh pageable maps fault their pages one at a time inside a copy: touch
+  // them on the host pool while the upload and the pipeline run.
+  std::thread prefault([&] {
+    for (void* h : {h_background, h_rms}) {
+      cudaPointerAttributes attr{};
+      if (cudaPointerGetAttributes(&attr, h) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if (attr.type == cudaMemoryTypeUnregistered) prefault_pages(h, bytes);
+    }
+  });
   if (bytes) e = cudaMemcpy(d_in, h_in, bytes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && h_mask && r.len) e = cudaMemcpy(d_mask, h_mask, (size_t)r.len, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    rc = ndf_mesh_background_device(d_in, h_mask ? d_mask : nullptr, dtype, ndim, shape, box_size, filter_size,
+                                    config, d_bg, d_rms, mesh_background, mesh_rms, mesh_valid, mesh_finite_count,
+                                    mesh_retained_count, globals, nullptr);
+  prefault.join();
   if (e != cudaSuccess) return cuda_fail(e, "mesh upload");
-  rc = ndf_mesh_background_device(d_in, h_mask ? d_mask : nullptr, dtype, ndim, shape, box_size, filter_size, config,
-                                  d_bg, d_rms, mesh_background, mesh_rms, mesh_valid, mesh_finite_count,
-                                  mesh_retained_count, globals, nullptr);
   if (rc != NDF_OK) return rc;
   if (bytes) {
     e = cudaMemcpy(h_background, d_bg, bytes, cudaMemcpyDeviceToHost);
