@@ -549,13 +549,41 @@ __device__ double clipped(double* v, double* s, double* w, int n, const RobustAr
       spread = std_parts(v, n, w);
     }
     const Limit below = make_limit(spread, ra.lower), above = make_limit(spread, ra.upper);
-    int kept = 0, kept_sorted = 0;
-    for (int i = 0; i < n; ++i) {
-      const double x = v[i];
-      if (inside(x, center, lt64(x, center) ? below : above)) v[kept++] = x;
-      const double y = s[i];
-      if (inside(y, center, lt64(y, center) ? below : above)) s[kept_sorted++] = y;
+    // The test depends on the value alone and the distance to the center
+    // grows away from it on both sides (rounding is monotone), so the kept
+    // sorted samples are one run [lo, hi): binary searches find it (the
+    // first sample at or above the center, then the run's two ends), and the
+    // tap-order samples are kept by their total-order key against the run's
+    // ends (equal values share their fate, so no value straddles an end).
+    auto in = [&](int i) { return inside(s[i], center, lt64(s[i], center) ? below : above); };
+    int a = 0, b = n;
+    while (a < b) {
+      const int m = (a + b) / 2;
+      if (lt64(s[m], center)) a = m + 1; else b = m;
     }
+    const int c = a;
+    int lo = 0;
+    b = c;
+    while (lo < b) {
+      const int m = (lo + b) / 2;
+      if (in(m)) b = m; else lo = m + 1;
+    }
+    int hi = c;
+    b = n;
+    while (hi < b) {
+      const int m = (hi + b) / 2;
+      if (in(m)) hi = m + 1; else b = m;
+    }
+    if (lo == c && hi == c) lo = hi = 0;
+    int kept = 0;
+    if (hi > lo) {
+      const unsigned long long first = total_key(s[lo]), last = total_key(s[hi - 1]);
+      for (int i = 0; i < n; ++i) {
+        const unsigned long long k = total_key(v[i]);
+        if (k >= first && k <= last) v[kept++] = v[i];
+      }
+    }
+    s += lo;
     ++iteration;
     const bool stable = kept == n;
     n = kept;
