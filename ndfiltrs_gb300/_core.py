@@ -22,7 +22,9 @@ the GIL is held, and the computation runs with the GIL released.
 
 from __future__ import annotations
 
+import collections
 import ctypes
+import os
 import threading
 from pathlib import Path
 
@@ -368,6 +370,10 @@ class Plan:
         return lib.ndf_plan_algorithm(self._handle).decode()
 
     @property
+    def is_open(self) -> bool:
+        return getattr(self, "_handle", None) is not None and bool(self._handle.value)
+
+    @property
     def host_bands(self) -> int:
         """Row bands ``run_host_async`` pipelines (0: the whole array at once)."""
         lib, _ = _load()
@@ -531,6 +537,77 @@ class Batch:
             pass
 
 
+class _PlanCache:
+    """Plans of recent one-call filters, reused by later calls with the same
+    configuration. Creating a plan validates it, uploads its window tables,
+    picks and sizes its kernels and allocates its device buffers, which
+    costs more than filtering a small array; pipelines that filter many
+    frames of one shape pay it once. Least recently used plans are closed
+    beyond ``capacity`` plans or ``max_bytes`` of their device buffers. A
+    lock per plan serializes the calls that share it; changing the kernel
+    choice rules (``set_autotune``, ``pin_kernel``) empties the cache."""
+
+    def __init__(self, capacity: int = 8, max_bytes: int = 4 << 30) -> None:
+        self.capacity = capacity
+        self.max_bytes = max_bytes
+        self._lock = threading.Lock()
+        self._plans: collections.OrderedDict = collections.OrderedDict()
+
+    def _evict_locked(self) -> None:
+        while self._plans and (len(self._plans) > self.capacity
+                               or sum(e[2] for e in self._plans.values()) > self.max_bytes):
+            _, (plan, lock, _) = self._plans.popitem(last=False)
+            with lock:
+                plan.close()
+
+    def run(self, key, make, array: np.ndarray) -> np.ndarray:
+        with self._lock:
+            entry = self._plans.get(key)
+            if entry is not None:
+                self._plans.move_to_end(key)
+        if entry is None:
+            plan = make()  # a configuration error raises here; nothing is cached
+            with self._lock:
+                entry = self._plans.get(key)
+                if entry is None:
+                    entry = (plan, threading.Lock(), 2 * array.nbytes)
+                    self._plans[key] = entry
+                    self._evict_locked()
+                else:
+                    plan.close()
+        plan, lock, _ = entry
+        with lock:
+            if plan.is_open:
+                return plan.run_host(array)
+        with make() as fresh:  # evicted by another thread meanwhile
+            return fresh.run_host(array)
+
+    def clear(self) -> None:
+        with self._lock:
+            while self._plans:
+                _, (plan, lock, _) = self._plans.popitem()
+                with lock:
+                    plan.close()
+
+
+_plan_cache = _PlanCache()
+
+
+def clear_plan_cache() -> None:
+    """Close every cached plan of the one-call filters."""
+    _plan_cache.clear()
+
+
+def _cache_key(array: np.ndarray, kind, size, footprint, origin, mode, *rest) -> tuple:
+    fp = None
+    if footprint is not None:
+        mask = np.asarray(footprint, dtype=bool)
+        fp = (mask.shape, mask.tobytes())
+    return (array.shape, array.dtype.str, kind, tuple(int(v) for v in size), fp,
+            None if origin is None else tuple(int(v) for v in origin),
+            None if mode is None else tuple(mode), os.environ.get("NDF_MOMENTS", "fp32c"), *rest)
+
+
 def _typed_array(array: object) -> np.ndarray:
     if not isinstance(array, np.ndarray) or array.dtype not in (np.float32, np.float64):
         raise TypeError("argument 'array': expected a float32 or float64 numpy.ndarray")
@@ -555,21 +632,14 @@ def window_filter(
     if not array.flags.c_contiguous:
         raise ValueError("native input must be C-contiguous")
     cval = float(np.float32(cval)) if array.dtype == np.float32 else float(cval)
-    with Plan(
-        array.shape,
-        array.dtype,
-        kind,
-        size,
-        footprint=footprint,
-        origin=origin,
-        mode=mode,
-        cval=cval,
-        omit_nan=omit_nan,
-        ignore_inf=ignore_inf,
-        min_count=min_count,
-        parameter=parameter,
-    ) as plan:
-        return plan.run_host(array)
+
+    def make() -> Plan:
+        return Plan(array.shape, array.dtype, kind, size, footprint=footprint, origin=origin, mode=mode, cval=cval,
+                    omit_nan=omit_nan, ignore_inf=ignore_inf, min_count=min_count, parameter=parameter)
+
+    key = _cache_key(array, kind, size, footprint, origin, mode, np.float64(cval).tobytes(), bool(omit_nan),
+                     bool(ignore_inf), int(min_count), int(parameter))
+    return _plan_cache.run(key, make, array)
 
 
 def robust_filter(
@@ -617,22 +687,16 @@ def robust_filter(
                    spread=spread if clip else "std",
                    estimator=estimator if kind in ("mode", "sigma_mode") else "sex",
                    modify_sample_size=modify_sample_size, pearson=pearson)
-    with Plan(
-        array.shape,
-        array.dtype,
-        kind,
-        size,
-        footprint=footprint,
-        origin=origin,
-        mode=mode,
-        cval=float(cval),
-        omit_nan=True if clip else omit_nan,
-        ignore_inf=True if clip else ignore_inf,
-        min_count=min_count,
-        percentile=float(parameter),
-        robust=options,
-    ) as plan:
-        return plan.run_host(array)
+    def make() -> Plan:
+        return Plan(array.shape, array.dtype, kind, size, footprint=footprint, origin=origin, mode=mode,
+                    cval=float(cval), omit_nan=True if clip else omit_nan, ignore_inf=True if clip else ignore_inf,
+                    min_count=min_count, percentile=float(parameter), robust=options)
+
+    key = _cache_key(array, kind, size, footprint, origin, mode, np.float64(cval).tobytes(), bool(omit_nan),
+                     bool(ignore_inf), int(min_count), np.float64(parameter).tobytes(),
+                     tuple((k, np.float64(v).tobytes() if isinstance(v, float) else v)
+                           for k, v in sorted(options.items())))
+    return _plan_cache.run(key, make, array)
 
 
 def _unsupported(name: str) -> ValueError:
@@ -759,6 +823,7 @@ def set_autotune(mode: int, cache_path: str | None = None) -> None:
     lib, _ = _load()
     path = None if cache_path is None else str(cache_path).encode()
     _check(lib.ndf_set_autotune(int(mode), path), lib)
+    _plan_cache.clear()
 
 
 def autotune_entries() -> int:
@@ -774,6 +839,7 @@ def pin_kernel(family: str | None) -> None:
     depend on it."""
     lib, _ = _load()
     _check(lib.ndf_pin_kernel(None if family is None else str(family).encode()), lib)
+    _plan_cache.clear()
 
 
 def set_tma(enabled: bool) -> None:
