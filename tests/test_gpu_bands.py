@@ -38,6 +38,9 @@ CASES = [
     ((2048, 2048), np.float32, dict(kind="std", size=(9, 9), omit_nan=True, moments="fp64"), True),
     ((2048, 2048), np.float32, dict(kind="mad", size=(5, 5), omit_nan=True, robust={"parameter": 1.4826}), True),
     ((1500, 1400), np.float64, dict(kind="median", size=(3, 3), mode=("reflect", "nearest")), True),
+    ((1 << 23,), np.float32, dict(kind="median", size=(9,), origin=(2,), mode=("mirror",), omit_nan=True), True),
+    ((512, 96, 96), np.float32, dict(kind="median", size=(3, 5, 5), mode=("nearest", "reflect", "wrap"),
+                                     omit_nan=True), True),
     # Not banded: wrap along the first axis, float32-compensated moments,
     # arrays below 16 MiB.
     ((2048, 2048), np.float32, dict(kind="median", size=(5, 5), mode=("wrap", "reflect"), omit_nan=True), False),
