@@ -273,6 +273,68 @@ def _robust_params(robust: dict | None) -> RobustParams:
     )
 
 
+class _Lease:
+    """The owner of one pooled host buffer while arrays view it: numpy keeps
+    it as their base, and its finalizer returns the buffer to the pool."""
+
+    __slots__ = ("raw", "pool", "__array_interface__")
+
+    def __init__(self, raw: np.ndarray, pool: "_HostBuffers", shape: tuple, dtype: np.dtype) -> None:
+        self.raw = raw
+        self.pool = pool
+        self.__array_interface__ = {"data": (raw.ctypes.data, False), "shape": tuple(shape),
+                                    "typestr": np.dtype(dtype).str, "version": 3}
+
+    def __del__(self) -> None:
+        try:
+            self.pool.give_back(self.raw)
+        except Exception:  # interpreter shutdown
+            pass
+
+
+class _HostBuffers:
+    """Host buffers for the output arrays of host-buffer runs. A fresh
+    output array's pages are mapped one fault at a time as the device copy
+    writes them, which costs more than the filter on large arrays; outputs
+    are therefore views of pooled buffers whose pages are already resident,
+    and a buffer returns to the pool when the last array viewing it is
+    released (a loop that drops each frame's result reuses two buffers).
+    Every element of an output is written by the filter. Idle buffers are
+    kept up to ``max_idle_bytes``; arrays under 1 MiB are plain numpy
+    allocations."""
+
+    def __init__(self, max_idle_bytes: int = 2 << 30) -> None:
+        self.max_idle_bytes = max_idle_bytes
+        self._free: dict = {}
+        self._idle = 0
+
+    def array(self, shape: tuple, dtype: np.dtype) -> np.ndarray:
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape, dtype=np.int64)) * dtype.itemsize
+        if nbytes < (1 << 20):
+            return np.zeros(shape, dtype=dtype)
+        raw = None
+        queue = self._free.get(nbytes)
+        if queue:
+            try:
+                raw = queue.popleft()
+                self._idle -= nbytes
+            except IndexError:
+                raw = None
+        if raw is None:
+            raw = np.empty(nbytes, np.uint8)
+        return np.asarray(_Lease(raw, self, shape, dtype))
+
+    def give_back(self, raw: np.ndarray) -> None:
+        if self._idle + raw.nbytes > self.max_idle_bytes:
+            return
+        self._free.setdefault(raw.nbytes, collections.deque()).append(raw)
+        self._idle += raw.nbytes
+
+
+_host_buffers = _HostBuffers()
+
+
 class Plan:
     """A validated filter plan (``WindowFilter::new``, src/plan.rs:260-324).
 
@@ -403,7 +465,7 @@ class Plan:
         if not array.flags.c_contiguous:
             raise ValueError("native input must be C-contiguous")
         if out is None:
-            out = np.zeros(self.shape, dtype=self.dtype)
+            out = np.zeros(self.shape, dtype=self.dtype) if array.size == 0 else _host_buffers.array(self.shape, self.dtype)
         if array.size == 0:
             return out
         _check(pylib.ndf_plan_upload(self._handle, array.ctypes.data), lib)

@@ -78,3 +78,20 @@ def test_keys_separate_configurations(gpu) -> None:
     np.testing.assert_array_equal(b.view(np.uint32), c.view(np.uint32))
     assert len(_core._plan_cache._plans) == 3
     assert d.shape == image.shape
+
+
+def test_outputs_do_not_alias(gpu) -> None:
+    """Outputs come from pooled host buffers: a live result is never
+    overwritten by a later call, and a released one is reused."""
+    nf = gpu
+    first, second = _image((1024, 1024), 21), _image((1024, 1024), 22)
+    want_first, want_second = _fresh(first, 5), _fresh(second, 5)
+    out_first = nf.nanmedian_filter(first, 5)
+    out_second = nf.nanmedian_filter(second, 5)
+    np.testing.assert_array_equal(out_first.view(np.uint32), want_first.view(np.uint32))
+    np.testing.assert_array_equal(out_second.view(np.uint32), want_second.view(np.uint32))
+    assert out_first.ctypes.data != out_second.ctypes.data
+    for _ in range(3):
+        out_first = nf.nanmedian_filter(first, 5)
+        np.testing.assert_array_equal(out_first.view(np.uint32), want_first.view(np.uint32))
+        np.testing.assert_array_equal(out_second.view(np.uint32), want_second.view(np.uint32))
