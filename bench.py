@@ -203,6 +203,33 @@ MEASURED_TRAFFIC = {
 }
 
 
+# Warp instructions one filter call issues (all its launches), from the
+# workload's ncu capture: the issue-rate roofline of the selection and
+# integer kernels, whose bound is the instruction issue rather than HBM.
+MEASURED_INSTRUCTIONS = {
+    "nanmedian_sortnet_5x5_4096_f32": (211559951, "profiles/tile_box_kernel_nanmedian_sortnet_5x5_4096_f32.md"),
+    "nanmedian_hist_65x65_4096_f32": (4473801729, "profiles/histogram_kernel_nanmedian_hist_65x65_4096_f32.md"),
+    "nanmedian_ring_4_6_4096_f32": (1541069691, "profiles/tile_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
+    "nanstd_31x31_4096_f32": (926756594, "profiles/moments_slide_kernel_nanstd_31x31_4096_f32.md"),
+    "nanmin_31x31_4096_f32": (60.5e6 + 57.8e6, "profiles/extrema_pass_kernel_nanmin_31x31_4096_f32.md"),
+    "nanmean_boxcar_31x31_4096_f32": (501907311, "profiles/boxcar_band_kernel_nanmean_boxcar_31x31_4096_f32.md"),
+    "nanmad_5x5_4096_f32": (3313524878, "profiles/robust_kernel_nanmad_5x5_4096_f32.md"),
+}
+
+
+def issue_roofline(workload: str, ms_per_step: float, sm_count: int, sm_mhz: float | None) -> dict | None:
+    """Warp instructions per second against the SMs' issue peak (four
+    schedulers per SM, one warp instruction each per clock, at the sampled
+    SM clock)."""
+    known = MEASURED_INSTRUCTIONS.get(workload)
+    if known is None or not sm_mhz:
+        return None
+    achieved = known[0] / (ms_per_step / 1e3) / 1e9
+    peak = sm_count * 4 * sm_mhz * 1e6 / 1e9
+    return {"achieved": round(achieved, 1), "peak": round(peak, 1), "unit": "G warp instructions/s",
+            "frac": round(achieved / peak, 4), "instructions_per_call": int(known[0]), "source": known[1]}
+
+
 # Kernels of this library one filter call launches, per algorithm (the band
 # and tiled exact means add a wider pass and the direct pass for bands or
 # tiles their words cannot hold; the separable extrema run two passes).
@@ -1033,6 +1060,8 @@ def main() -> None:
                 "note": f"selection is instruction-bound; algorithmic bytes = 2 x {image.itemsize} B/pixel "
                         "(one read, one write), halo re-reads excluded",
             },
+            "issue_roofline": issue_roofline(args.workload, ms_per_step, int(torch.cuda.get_device_properties(
+                device).multi_processor_count), clocks.summary().get("sm_mhz")),
             "cpu_baseline": base,
             "clocks": clocks.summary(),
             "gpu_launches": args.steps * LAUNCHES_PER_CALL.get(plan.algorithm, 1),
