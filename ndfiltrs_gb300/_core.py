@@ -833,8 +833,9 @@ def mesh_background(array, mask, box_size, filter_size, estimator, sigma_lower, 
         flags = np.ascontiguousarray(mask, dtype=np.uint8)
         if flags.shape != shape:
             raise ValueError("mask must have the same shape as data")
-    background = np.zeros(shape, dtype=array.dtype)
-    rms_map = np.zeros(shape, dtype=array.dtype)
+    # Both maps are written whole by the device pipeline.
+    background = _host_buffers.array(shape, array.dtype) if array.size else np.zeros(shape, dtype=array.dtype)
+    rms_map = _host_buffers.array(shape, array.dtype) if array.size else np.zeros(shape, dtype=array.dtype)
     mesh_bg = np.zeros(mesh_shape, np.float64)
     mesh_rms = np.zeros(mesh_shape, np.float64)
     valid = np.zeros(mesh_shape, np.uint8)
