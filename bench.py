@@ -7,8 +7,9 @@ one 4096x4096 float32 image (the robust-statistics image: background
 
 * ``value``: Mpix/s with the input already in HBM (device pointers through
   the C-ABI plan), timed with CUDA events on the launching stream. Inputs
-  rotate over four device buffers (268 MB > 129 MB L2), so no step reads an
-  input that the previous step left in L2.
+  rotate over ``max(4, ceil(3 x 129 MiB / image bytes))`` device buffers
+  (seven 67 MB images for the default workload, 470 MB > 3 x 129 MB L2), so
+  no step reads an input that the previous steps left in L2.
 * ``e2e``: the same metric through the C-ABI host-buffer entry point
   (``ndf_plan_run_host``): pinned host input -> device -> kernel -> pinned
   host output, synchronized every step.
@@ -650,6 +651,32 @@ def precision_study(rows: int = 192, width: int = 4096) -> dict:
 
 # ---------------------------------------------------------------------------
 
+def rotation_buffers(image_bytes: int) -> int:
+    """Input buffers the device timing rotates over: together they exceed
+    the 129 MB L2 three times over."""
+    return max(4, -(-3 * 129 * 2**20 // image_bytes))
+
+
+def workload_config(workload: str, spec, image: np.ndarray, world: int) -> dict:
+    """The ``config`` object of a filter workload's line, identical in both
+    arms (the reference arm's sample size is in its ``cpu_baseline``)."""
+    n_buffers = rotation_buffers(image.nbytes)
+    return {
+        "workload": workload,
+        "image": list(image.shape),
+        "kind": spec.kind,
+        "size": list(spec.window()),
+        "footprint": None if spec.footprint_fn is None else int(spec.footprint().sum()),
+        "origin": spec.origin,
+        "percentile": spec.q if spec.kind == "percentile" else None,
+        "mode": spec.mode,
+        "omit_nan": spec.omit,
+        "l2": f"device timing: inputs rotate over {n_buffers} device buffers "
+              f"({n_buffers} x {image.nbytes / 1e6:.0f} MB > 129 MB L2)",
+        "parallelism": f"replicas x{world}",
+    }
+
+
 def run_reference(args, spec, workload: str) -> None:
     image = spec.gen()
     steps, warmup = args.steps, args.warmup
@@ -681,7 +708,7 @@ def run_reference(args, spec, workload: str) -> None:
         "vs_baseline": None,
         "dtype": "f32" if image.dtype == np.float32 else "f64",
         "data": "synthetic",
-        "config": {"workload": workload, "sample_rows": rows, "image": list(image.shape)},
+        "config": workload_config(workload, spec, image, args.gpus),
         "cpu_baseline": base,
         "e2e": {"value": round(value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -923,7 +950,7 @@ def main() -> None:
     # Rotate over enough input buffers that together they exceed the 129 MB L2
     # three times over, so no step reads an input the previous ones left in L2.
     image_bytes = image.nbytes
-    n_buffers = max(4, -(-3 * 129 * 2**20 // image_bytes))
+    n_buffers = rotation_buffers(image_bytes)
     buffers = [torch.from_numpy(np.roll(image, k * 97, axis=-1).copy()).to(device) for k in range(n_buffers)]
     outputs = [torch.empty_like(buffers[0]) for _ in range(2)]
     stream = torch.cuda.Stream(device)
@@ -1023,21 +1050,8 @@ def main() -> None:
             "vs_baseline": None,
             "dtype": "f32" if image.dtype == np.float32 else "f64",
             "data": "synthetic",
-            "config": {
-                "workload": args.workload,
-                "image": list(shape),
-                "kind": kind,
-                "size": list(spec.window()),
-                "footprint": None if spec.footprint_fn is None else int(spec.footprint().sum()),
-                "origin": spec.origin,
-                "percentile": spec.q if kind == "percentile" else None,
-                "mode": mode,
-                "omit_nan": spec.omit,
-                "algorithm": plan.algorithm,
-                "l2": f"inputs rotate over {n_buffers} device buffers "
-                      f"({n_buffers} x {image_bytes / 1e6:.0f} MB > 129 MB L2)",
-                "parallelism": f"replicas x{world}",
-            },
+            "config": workload_config(args.workload, spec, image, world),
+            "algorithm": plan.algorithm,
             "e2e": {
                 "value": round(e2e_value, 3),
                 "unit": "Mpix/s",

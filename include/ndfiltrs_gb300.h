@@ -198,8 +198,11 @@ int ndf_mesh_background_device(const void* d_in, const uint8_t* d_mask, int32_t 
                                int64_t* mesh_retained_count, double* globals, void* stream);
 
 /* Replaces `_core.get_num_threads()`, src/pyapi/filter.rs:378-380. Returns
- * the number of streaming multiprocessors of the current device (the
- * library's unit of parallelism), or 0 without a device. */
+ * the number of host threads of the library's host-side pools (pageable
+ * copies, page prefaulting, mesh fill): RAYON_NUM_THREADS when it is set to a
+ * positive integer, else the hardware thread count capped at 16; fixed at
+ * the first call of the process, like the reference's global Rayon pool.
+ * Needs no device. */
 int32_t ndf_get_num_threads(void);
 
 /* Thread-local message of the last error on the calling thread. */
@@ -321,8 +324,10 @@ int32_t ndf_batch_launches(const ndf_batch* batch);
  * every call and keeps the last call's contents (the kernel overwrites what
  * it reads, nothing needs clearing); calls that overlap on the GPU race on
  * it. The first call on a device looks up the array's address with that
- * device current: make it before any stream capture. A window whose sort slot
- * does not fit in the array returns NDF_ERR_MEMORY. */
+ * device current: make it before any stream capture. The address is kept
+ * for the process, so the call must not be used on a device after
+ * cudaDeviceReset. A window whose sort slot does not fit in the array returns
+ * NDF_ERR_MEMORY. */
 int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32_t dtype, int32_t ndim,
                                  const uint64_t* shape, const uint64_t* size, const int64_t* origin,
                                  const int32_t* modes, double cval, int32_t kind, int32_t omit_nan,

@@ -302,6 +302,10 @@ def rank_filter(
 
 
 def get_num_threads() -> int:
-    """Number of streaming multiprocessors the GPU library spreads work over
-    (the reference returns its Rayon pool size)."""
+    """Return the number of threads in the library's host-side pool.
+
+    As with the reference's global Rayon pool, ``RAYON_NUM_THREADS`` (set
+    before the first call of the process) fixes it; the default is the
+    hardware thread count capped at 16. Device work always spans every SM.
+    """
     return _core.get_num_threads()

@@ -307,6 +307,10 @@ class _HostBuffers:
         self.max_idle_bytes = max_idle_bytes
         self._free: dict = {}
         self._idle = 0
+        # Guards _free and _idle: a lease's finalizer can run on any thread at
+        # any garbage-collection point. give_back never re-enters the pool, so
+        # taking the lock there cannot deadlock.
+        self._lock = threading.Lock()
 
     def array(self, shape: tuple, dtype: np.dtype) -> np.ndarray:
         dtype = np.dtype(dtype)
@@ -314,22 +318,21 @@ class _HostBuffers:
         if nbytes < (1 << 20):
             return np.zeros(shape, dtype=dtype)
         raw = None
-        queue = self._free.get(nbytes)
-        if queue:
-            try:
+        with self._lock:
+            queue = self._free.get(nbytes)
+            if queue:
                 raw = queue.popleft()
                 self._idle -= nbytes
-            except IndexError:
-                raw = None
         if raw is None:
             raw = np.empty(nbytes, np.uint8)
         return np.asarray(_Lease(raw, self, shape, dtype))
 
     def give_back(self, raw: np.ndarray) -> None:
-        if self._idle + raw.nbytes > self.max_idle_bytes:
-            return
-        self._free.setdefault(raw.nbytes, collections.deque()).append(raw)
-        self._idle += raw.nbytes
+        with self._lock:
+            if self._idle + raw.nbytes > self.max_idle_bytes:
+                return
+            self._free.setdefault(raw.nbytes, collections.deque()).append(raw)
+            self._idle += raw.nbytes
 
 
 _host_buffers = _HostBuffers()
@@ -615,10 +618,19 @@ class _PlanCache:
         self._lock = threading.Lock()
         self._plans: collections.OrderedDict = collections.OrderedDict()
 
-    def _evict_locked(self) -> None:
+    def _evict_locked(self) -> list:
+        """Remove the entries beyond the limits (the cache lock is held) and
+        return them; the caller closes them after releasing the cache lock,
+        so a long filter on an evicted plan never blocks other lookups."""
+        evicted = []
         while self._plans and (len(self._plans) > self.capacity
                                or sum(e[2] for e in self._plans.values()) > self.max_bytes):
-            _, (plan, lock, _) = self._plans.popitem(last=False)
+            evicted.append(self._plans.popitem(last=False)[1])
+        return evicted
+
+    @staticmethod
+    def _close(entries) -> None:
+        for plan, lock, _ in entries:
             with lock:
                 plan.close()
 
@@ -629,14 +641,16 @@ class _PlanCache:
                 self._plans.move_to_end(key)
         if entry is None:
             plan = make()  # a configuration error raises here; nothing is cached
+            evicted = []
             with self._lock:
                 entry = self._plans.get(key)
                 if entry is None:
                     entry = (plan, threading.Lock(), 2 * array.nbytes)
                     self._plans[key] = entry
-                    self._evict_locked()
-                else:
-                    plan.close()
+                    evicted = self._evict_locked()
+            if entry[0] is not plan:
+                plan.close()
+            self._close(evicted)
         plan, lock, _ = entry
         with lock:
             if plan.is_open:
@@ -646,10 +660,9 @@ class _PlanCache:
 
     def clear(self) -> None:
         with self._lock:
-            while self._plans:
-                _, (plan, lock, _) = self._plans.popitem()
-                with lock:
-                    plan.close()
+            entries = list(self._plans.values())
+            self._plans.clear()
+        self._close(entries)
 
 
 _plan_cache = _PlanCache()
@@ -855,12 +868,15 @@ def mesh_background(array, mask, box_size, filter_size, estimator, sigma_lower, 
 
 
 def get_num_threads() -> int:
-    """Number of streaming multiprocessors the library spreads work over."""
+    """Number of host threads in the library's host-side pool.
+
+    Like the reference's global Rayon pool it honours ``RAYON_NUM_THREADS``
+    (a positive integer) read once per process; otherwise it is the hardware
+    thread count capped at 16. The device work is spread over the GPU's SMs
+    regardless (``device_info()["sm_count"]``).
+    """
     lib, _ = _load()
-    count = int(lib.ndf_get_num_threads())
-    if count <= 0:
-        _raise(9, lib)
-    return count
+    return int(lib.ndf_get_num_threads())
 
 
 def device_info() -> dict:

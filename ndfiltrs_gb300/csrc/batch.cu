@@ -483,8 +483,7 @@ int setup_host(ndf_batch* b) {
   for (cudaStream_t* s : {&h.up, &h.compute, &h.down})
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(e, "batch host pipeline setup");
-  const unsigned hc = std::thread::hardware_concurrency();
-  h.pool = std::make_unique<CopyPool>((int)std::max(1u, std::min(hc == 0 ? 4u : hc, 16u)) - 1);
+  h.pool = std::make_unique<CopyPool>(host_thread_count() - 1);
   b->host_ready = true;
   return NDF_OK;
 }

@@ -1034,11 +1034,7 @@ int ndf_device_info(int32_t* sm_count, int32_t* major, int32_t* minor, char* nam
   return NDF_OK;
 }
 
-int32_t ndf_get_num_threads(void) {
-  int dev, sms, smem;
-  if (ensure_device(&dev, &sms, &smem) != NDF_OK) return 0;
-  return sms;
-}
+int32_t ndf_get_num_threads(void) { return (int32_t)ndf::host_thread_count(); }
 
 int ndf_plan_create(const ndf_filter_desc* desc, ndf_plan** out) {
   if (!out) return fail(NDF_ERR_INVALID_CONFIGURATION, "missing plan output pointer");

@@ -953,7 +953,10 @@ cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStrea
 //    threads) race on it and must be serialized by the caller;
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    before any stream capture;
+//  * the address is kept for the life of the process: do not use the entry
+//    point on a device after cudaDeviceReset (or another teardown of its
+//    primary context), which can move the array.
 
 constexpr size_t kNoAllocScratchBytes = 16u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -992,6 +995,13 @@ int noalloc_fail(int code, const char* message) {
   return fail(code, message);
 }
 
+// a * b into *out; false when the product does not fit in 64 bits.
+bool mul_fits(unsigned long long a, unsigned long long b, unsigned long long* out) {
+  if (a != 0 && b > ~0ull / a) return false;
+  *out = a * b;
+  return true;
+}
+
 }  // namespace
 }  // namespace ndf
 
@@ -1028,8 +1038,8 @@ extern "C" int ndf_histogram_filter_noalloc(const void* d_in, void* d_out, int32
     sz[a + pad] = length;
     org[a + pad] = origin[a];
     md[a + pad] = modes[a];
-    volume *= size[a];
-    n_out *= shape[a];
+    if (!mul_fits(volume, size[a], &volume) || !mul_fits(n_out, shape[a], &n_out))
+      return noalloc_fail(NDF_ERR_OVERFLOW, "shape or index arithmetic overflowed");
   }
   if (omit_nan && (min_count == 0 || min_count > volume))
     return noalloc_fail(NDF_ERR_INVALID_CONFIGURATION,

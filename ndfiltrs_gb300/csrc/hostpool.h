@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <condition_variable>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -101,6 +102,25 @@ inline void add_pieces(std::vector<CopyPool::Piece>& out, void* dst, const void*
     out.push_back({(unsigned char*)dst + off, (const unsigned char*)src + off, std::min(piece, bytes - off)});
 }
 
+// Number of host threads the library works with (the calling thread plus
+// the workers of a pool), fixed at the first call of the process: the value
+// of RAYON_NUM_THREADS when it is a positive integer (the variable the
+// reference's thread pool reads, so one setting sizes either library), else
+// the hardware thread count capped at 16. get_num_threads() reports it.
+inline int host_thread_count() {
+  static const int count = [] {
+    const char* env = std::getenv("RAYON_NUM_THREADS");
+    if (env && *env) {
+      char* end = nullptr;
+      const long v = std::strtol(env, &end, 10);
+      if (end && *end == '\0' && v > 0) return (int)std::min<long>(v, 1024);
+    }
+    const unsigned hc = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(hc == 0 ? 4u : hc, 16u));
+  }();
+  return count;
+}
+
 // The process-wide pool used by plans (one job at a time; callers serialize
 // through `lock`).
 struct SharedHostPool {
@@ -120,10 +140,7 @@ inline void prefault_pages(void* p, size_t bytes) {
   if (!p || bytes < kMin) return;
   SharedHostPool& s = shared_host_pool();
   std::lock_guard<std::mutex> guard(s.lock);
-  if (!s.pool) {
-    const unsigned hc = std::thread::hardware_concurrency();
-    s.pool = new CopyPool((int)std::max(1u, std::min(hc == 0 ? 4u : hc, 16u)) - 1);
-  }
+  if (!s.pool) s.pool = new CopyPool(host_thread_count() - 1);
   std::vector<CopyPool::Piece> pieces;
   for (size_t off = 0; off < bytes; off += kPiece)
     pieces.push_back({static_cast<unsigned char*>(p) + off, nullptr, std::min(kPiece, bytes - off)});

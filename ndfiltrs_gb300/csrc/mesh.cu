@@ -650,8 +650,8 @@ void unravel(long long flat, const std::vector<long long>& dims, long long* inde
 // (a rough operation count) is large enough to pay for them.
 template <typename Body>
 void parallel_for(long long count, long long work, Body&& body) {
-  long long threads = std::max(1u, std::thread::hardware_concurrency());
-  threads = std::min({threads, 32ll, count, std::max(1ll, work / 200000)});
+  long long threads = host_thread_count();
+  threads = std::min({threads, count, std::max(1ll, work / 200000)});
   if (threads <= 1) {
     for (long long i = 0; i < count; ++i) body(i);
     return;

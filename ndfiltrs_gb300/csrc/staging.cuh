@@ -108,7 +108,16 @@ __device__ __forceinline__ bool stage_tile(S* s, long long* maps, unsigned char*
       tma::load_3d(raw, tmap, &bar, (int)xa, (int)ys, (int)zs);
   }
   const bool ok = __syncthreads_and(tma::mbar_wait(&bar, 0, kWaitLimitNs, a.status) ? 1 : 0) != 0;
-  if (!ok) return false;
+  if (!ok) {
+    // The copy was issued and may still land: wait once more (bounded) so
+    // that the block does not retire while the copy can write shared memory
+    // that the next block on this SM would own. If the second wait runs out
+    // too the block returns anyway (a wait never spins without a limit); the
+    // status word already makes the call report NDF_ERR_TIMEOUT.
+    if (threadIdx.x == 0) tma::mbar_wait(&bar, 0, kWaitLimitNs, nullptr);
+    __syncthreads();
+    return false;
+  }
   const int r = (int)(xs - xa);
   const int rows = g.kd * t.SH;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;

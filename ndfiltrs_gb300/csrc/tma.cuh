@@ -13,7 +13,8 @@
 //
 // Every wait is bounded (1 s of %globaltimer by default): a wait that runs
 // out sets the status word that the host reads after its next synchronization
-// (NDF_ERR_TIMEOUT) and the block returns without writing outputs.
+// (NDF_ERR_TIMEOUT), drains the issued copy with a second bounded wait, and
+// the block returns without writing outputs.
 #pragma once
 
 #include <cuda.h>

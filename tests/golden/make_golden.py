@@ -27,6 +27,7 @@ from __future__ import annotations
 import argparse
 import json
 import math
+import os
 import sys
 from pathlib import Path
 
@@ -38,9 +39,15 @@ MODES = ("reflect", "constant", "nearest", "mirror", "wrap")
 
 def main() -> None:
     parser = argparse.ArgumentParser()
-    parser.add_argument("--reference", default="/root/reference")
+    parser.add_argument(
+        "--reference",
+        default=os.environ.get("NDFILTRS_REFERENCE"),
+        help="checkout of the reference project (or set NDFILTRS_REFERENCE)",
+    )
     parser.add_argument("--output", default=str(HERE / "golden_v1"))
     args = parser.parse_args()
+    if not args.reference:
+        parser.error("--reference (or NDFILTRS_REFERENCE) is required")
     sys.path.insert(0, args.reference)
     from scipy import ndimage
     from tests._mean_reference import mean_filter_reference

@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -71,9 +72,15 @@ def image(shape: tuple[int, ...], seed: int) -> np.ndarray:
 
 def main() -> None:
     parser = argparse.ArgumentParser()
-    parser.add_argument("--reference", default="/root/reference")
+    parser.add_argument(
+        "--reference",
+        default=os.environ.get("NDFILTRS_REFERENCE"),
+        help="checkout of the reference project (or set NDFILTRS_REFERENCE)",
+    )
     parser.add_argument("--output", default=str(HERE / "mesh_v1"))
     args = parser.parse_args()
+    if not args.reference:
+        parser.error("--reference (or NDFILTRS_REFERENCE) is required")
     sys.path.insert(0, args.reference)
     from tests._background_reference import mesh_background as reference
 

@@ -73,3 +73,19 @@ def test_no_cpu_fallback_without_device(monkeypatch) -> None:
         pass
     with pytest.raises(RuntimeError, match="CUDA device"):
         nf.median_filter(np.ones((4, 4), dtype=np.float32), 3)
+
+
+@pytest.mark.parametrize("threads", [1, 2, 4])
+def test_fresh_process_observes_rayon_thread_count(threads: int) -> None:
+    """get_num_threads needs no device and honours RAYON_NUM_THREADS like the
+    reference's pool (tests/test_parallel.py:9-21 of the reference)."""
+    import os
+    import subprocess
+    import sys
+
+    env = dict(os.environ, RAYON_NUM_THREADS=str(threads))
+    result = subprocess.run(
+        [sys.executable, "-c", "import ndfiltrs_gb300 as nf; print(nf.get_num_threads())"],
+        check=True, capture_output=True, text=True, env=env, cwd=str(ROOT),
+    )
+    assert result.stdout.strip() == str(threads)

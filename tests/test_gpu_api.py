@@ -93,8 +93,10 @@ def test_validation_errors_before_device_work(gpu) -> None:
         nf.mean_filter(np.ones((5, 5)), footprint=np.ones((2, 3)), method="boxcar")
 
 
-def test_get_num_threads_is_device_parallelism(gpu) -> None:
-    assert gpu.get_num_threads() == gpu.device_info()["sm_count"]
+def test_get_num_threads_is_the_host_pool_size(gpu) -> None:
+    """The host pool size, as in the reference; the SM count is separate."""
+    assert 1 <= gpu.get_num_threads() <= 1024
+    assert gpu.device_info()["sm_count"] > 0
 
 
 def test_autotuner_changes_speed_not_results(gpu, oracle) -> None:

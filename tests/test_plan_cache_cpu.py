@@ -116,3 +116,48 @@ def test_threads_share_one_plan_one_at_a_time() -> None:
     assert cached.open and cached.max_busy == 1
     # Plans made by threads that lost the race to insert are closed.
     assert all(not p.open for p in made if p is not cached)
+
+
+class SlowPlan(FakePlan):
+    """A plan whose filter runs until `release` is set."""
+
+    def __init__(self, tag, started, release):
+        super().__init__(tag)
+        self.started = started
+        self.release = release
+
+    def run_host(self, array):
+        self.started.set()
+        self.release.wait(10)
+        return (self.tag, 0)
+
+
+def test_evicting_a_busy_plan_does_not_block_other_lookups() -> None:
+    """A thread whose insertion evicts a plan that another thread is still
+    filtering with waits for that filter outside the cache lock, so lookups
+    of unrelated plans go on."""
+    cache = _core._PlanCache(capacity=2)
+    array = np.ones(4)
+    started, release = threading.Event(), threading.Event()
+    slow = SlowPlan("slow", started, release)
+    cache.run("other", lambda: FakePlan("other"), array)
+    filtering = threading.Thread(target=cache.run, args=("slow", lambda: slow, array))
+    filtering.start()
+    assert started.wait(10)
+    cache.run("other", lambda: FakePlan("unused"), array)  # "slow" becomes the least recent
+    evicting = threading.Thread(target=cache.run, args=("new", lambda: FakePlan("new"), array))
+    evicting.start()
+    deadline = time.monotonic() + 10
+    while "slow" in cache._plans and time.monotonic() < deadline:
+        time.sleep(0.001)
+    assert "slow" not in cache._plans
+    hit = []
+    lookup = threading.Thread(target=lambda: hit.append(cache.run("other", lambda: FakePlan("x"), array)))
+    lookup.start()
+    lookup.join(2)
+    assert hit and hit[0][0] == "other"  # answered while the evicted plan is still busy
+    assert slow.open and evicting.is_alive()  # its closer waits for the filter
+    release.set()
+    filtering.join(10)
+    evicting.join(10)
+    assert not slow.open
