@@ -492,12 +492,26 @@ def public_call(nf, spec, image):
                             ignore_inf=spec["ignore_inf"])
 
 
-def run_batch(args) -> None:
+def batch_comparison(args, public_loop: bool = True) -> dict:
+    """The mixed-size batch (512 float32 images, window 3..15, box / tophat /
+    ring, nanmedian / nanpercentile 84 / nanstd) through one batched launch
+    set against the plain per-call GPU path. Device-resident, CUDA events on
+    the launching stream:
+
+    * ``plain_per_call``: per image, create the plan (``ndf_plan_create``:
+      validation, window tables, kernel choice, device buffers), run it on
+      the device buffers and destroy it -- what a caller looping the
+      one-call API over images of different shapes and windows pays;
+    * ``plain_prebuilt``: the same loop over plans built beforehand (the
+      kernels alone, launched one image after another);
+    * ``batched``: ``ndf_batch_run`` (persistent family launches replayed from
+      a CUDA graph).
+
+    End to end (host arrays in, host arrays out): one ``Batch.run_host`` call
+    against the public per-call API in a loop. Outputs are compared bit for
+    bit."""
     import torch
 
-    import __graft_entry__
-
-    __graft_entry__.build()
     import ndfiltrs_gb300 as nf
 
     specs, images = mixed_batch(args.batch_images)
@@ -513,24 +527,32 @@ def run_batch(args) -> None:
     t0 = time.perf_counter()
     batch = nf.Batch(specs)
     batch_create_s = time.perf_counter() - t0
-    plans = []
-    for spec in specs:
+
+    def make_plan(spec):
         kw = dict(footprint=spec["footprint"], omit_nan=True, ignore_inf=spec["ignore_inf"],
                   min_count=1, parameter=spec["parameter"], percentile=84.0, mode=["reflect"] * 2)
         size = spec["footprint"].shape if spec["footprint"] is not None else spec["size"]
-        plans.append(nf.Plan(spec["shape"], np.float32, spec["kind"], size, **kw))
+        return nf.Plan(spec["shape"], np.float32, spec["kind"], size, **kw)
+
+    plans = [make_plan(spec) for spec in specs]
     in_ptrs = [t.data_ptr() for t in d_in]
     out_ptrs = [t.data_ptr() for t in d_batch]
 
-    def plain_step() -> None:
+    def percall_step() -> None:
+        for spec, src, dst in zip(specs, d_in, d_plain):
+            plan = make_plan(spec)
+            plan.run_device(src.data_ptr(), dst.data_ptr(), handle)
+            plan.close()
+
+    def prebuilt_step() -> None:
         for plan, src, dst in zip(plans, d_in, d_plain):
             plan.run_device(src.data_ptr(), dst.data_ptr(), handle)
 
     def batch_step() -> None:
         batch.run_device(in_ptrs, out_ptrs, handle)
 
-    def timed(fn, steps):
-        for _ in range(args.warmup):
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -550,60 +572,90 @@ def run_batch(args) -> None:
             result = fn()
         return (time.perf_counter() - t0) / steps * 1e3, result
 
-    steps = max(3, min(args.steps, 20))
+    steps = max(3, min(args.steps, 10))
     e2e_steps = 3
     with ClockSampler(0) as clocks:
-        plain_ms, plain_wall = timed(plain_step, steps)
-        batch_ms, batch_wall = timed(batch_step, steps)
-        # End to end from host arrays to host arrays: the public per-call API
-        # in a loop (plan, upload, kernel, download per image) against one
-        # batched host run (grouped, overlapped copies and kernels).
-        percall_ms, percall_out = wall(lambda: [public_call(nf, sp, im) for sp, im in zip(specs, images)],
-                                       e2e_steps)
+        prebuilt_ms, _ = timed(prebuilt_step, steps, args.warmup)
+        batch_ms, batch_wall = timed(batch_step, steps, args.warmup)
+        prebuilt_identical = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+                                 for a, b in zip(d_plain, d_batch))
+        for t in d_plain:
+            t.fill_(0)
+        percall_ms, _ = timed(percall_step, 3, 1)
+        percall_identical = all(torch.equal(a.view(torch.int32), b.view(torch.int32))
+                                for a, b in zip(d_plain, d_batch))
         host_ms, host_out = wall(lambda: batch.run_host(images), e2e_steps)
-    identical = all(torch.equal(a.view(torch.int32), b.view(torch.int32)) for a, b in zip(d_plain, d_batch))
-    e2e_identical = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
-                        for a, b in zip(percall_out, host_out))
+        public_ms, public_identical = None, None
+        if public_loop:
+            public_ms, public_out = wall(
+                lambda: [public_call(nf, sp, im) for sp, im in zip(specs, images)], e2e_steps)
+            public_identical = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                                   for a, b in zip(public_out, host_out))
+    launches = batch.launches
+    batch.close()
+    for plan in plans:
+        plan.close()
+
+    def rate(ms):
+        return None if ms is None else round(pixels / (ms / 1e3) / 1e6, 3)
+
+    return {
+        "workload": "batch_mixed",
+        "images": len(images),
+        "pixels": pixels,
+        "l2": "inputs total 3.7 GB (> 129 MB L2)",
+        "unit": "Mpix/s",
+        "batched": {"device": rate(batch_ms), "ms_per_step": round(batch_ms, 3),
+                    "host_ms_per_step": round(batch_wall, 3),
+                    "images_per_s": round(len(images) / (batch_ms / 1e3), 1),
+                    "path": "ndf_batch_run: persistent family launches replayed from a CUDA graph",
+                    "gpu_launches": launches},
+        "plain_per_call": {"device": rate(percall_ms), "ms_per_step": round(percall_ms, 3),
+                           "path": "per image: ndf_plan_create, ndf_plan_run on device buffers, "
+                                   "ndf_plan_destroy"},
+        "plain_prebuilt": {"device": rate(prebuilt_ms), "ms_per_step": round(prebuilt_ms, 3),
+                           "path": "ndf_plan_run per image, plans built beforehand"},
+        "speedup_vs_plain": {"device": round(percall_ms / batch_ms, 3),
+                             "device_vs_prebuilt": round(prebuilt_ms / batch_ms, 3)},
+        "e2e": {"batched": rate(host_ms), "ms_per_step": round(host_ms, 3),
+                "path": "ndf_batch_run_host (pageable host arrays in and out)",
+                "h2d_bytes_per_step": pixels * 4, "d2h_bytes_per_step": pixels * 4,
+                "public_per_call": rate(public_ms),
+                "public_ms_per_step": None if public_ms is None else round(public_ms, 3),
+                "public_path": "public per-call API per image (nanmedian/nanpercentile/nanstd_filter)",
+                "speedup_vs_public_per_call": None if public_ms is None else round(public_ms / host_ms, 3)},
+        "outputs_identical": {"plain_per_call": bool(percall_identical),
+                              "plain_prebuilt": bool(prebuilt_identical),
+                              "public_per_call": public_identical},
+        "autotune": {"keys": nf.autotune_entries(), "batch_create_s": round(batch_create_s, 3)},
+        "clocks": clocks.summary(),
+    }
+
+
+def run_batch(args) -> None:
+    import __graft_entry__
+
+    __graft_entry__.build()
+    r = batch_comparison(args)
     line = {
         "metric": METRIC,
-        "value": round(pixels / (batch_ms / 1e3) / 1e6, 3),
+        "value": r["batched"]["device"],
         "unit": "Mpix/s",
         "n_gpus": 1,
-        "steps": steps,
+        "steps": max(3, min(args.steps, 10)),
         "warmup": args.warmup,
-        "ms_per_step": round(batch_ms, 3),
+        "ms_per_step": r["batched"]["ms_per_step"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "batch_mixed", "images": len(images), "pixels": pixels,
-                   "l2": "inputs total 3.7 GB (> 129 MB L2)",
-                   "autotune": {"keys": nf.autotune_entries(), "batch_create_s": round(batch_create_s, 3)}},
-        "e2e": {"value": round(pixels / (host_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
-                "h2d_bytes_per_step": pixels * 4, "d2h_bytes_per_step": pixels * 4,
-                "path": "ndf_batch_run_host (pageable host arrays in and out)", "steps": e2e_steps,
-                "images_per_s": round(len(images) / (host_ms / 1e3), 1)},
-        "plain_per_call": {
-            "device": {"value": round(pixels / (plain_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
-                       "ms_per_step": round(plain_ms, 3), "path": "ndf_plan_run per image, plans prebuilt"},
-            "e2e": {"value": round(pixels / (percall_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
-                    "ms_per_step": round(percall_ms, 3),
-                    "path": "public per-call API per image (nanmedian/nanpercentile/nanstd_filter)"},
-        },
-        "batched": {
-            "device": {"value": round(pixels / (batch_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
-                       "ms_per_step": round(batch_ms, 3), "host_ms_per_step": round(batch_wall, 3),
-                       "images_per_s": round(len(images) / (batch_ms / 1e3), 1)},
-            "e2e": {"value": round(pixels / (host_ms / 1e3) / 1e6, 3), "unit": "Mpix/s",
-                    "ms_per_step": round(host_ms, 3),
-                    "images_per_s": round(len(images) / (host_ms / 1e3), 1)},
-        },
-        "speedup_batched_vs_plain": {"device": round(plain_ms / batch_ms, 3),
-                                     "e2e": round(percall_ms / host_ms, 3)},
-        "outputs_identical": {"device": bool(identical), "e2e": bool(e2e_identical)},
-        "clocks": clocks.summary(),
-        "gpu_launches": batch.launches,
+        "config": {"workload": "batch_mixed", "images": r["images"], "pixels": r["pixels"], "l2": r["l2"]},
+        "e2e": {"value": r["e2e"]["batched"], "unit": "Mpix/s", "h2d_bytes_per_step": r["e2e"]["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": r["e2e"]["d2h_bytes_per_step"], "path": r["e2e"]["path"]},
+        "batched": r,
+        "clocks": r["clocks"],
+        "gpu_launches": r["batched"]["gpu_launches"],
     }
     print(json.dumps(line))
 
@@ -893,6 +945,9 @@ def main() -> None:
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--precision", action=argparse.BooleanOptionalAction, default=True,
                         help="add the nanstd precision study to the line")
+    parser.add_argument("--batch", action=argparse.BooleanOptionalAction, default=None,
+                        help="add the mixed-size batch comparison (batched vs plain per-call GPU path) "
+                             "to the line; on by default for the default workload")
     parser.add_argument("--pin-kernel", default=None,
                         help="kernel family the plan takes when it is a candidate (A/B comparisons)")
     args = parser.parse_args()
@@ -1035,6 +1090,9 @@ def main() -> None:
         base = cpu_baseline(image, spec)
     if rank == 0 and world == 1 and args.precision:
         precision = precision_study()
+    batched = None
+    if rank == 0 and world == 1 and (args.batch if args.batch is not None else args.workload == DEFAULT_WORKLOAD):
+        batched = batch_comparison(args)
 
     if rank == 0:
         line = {
@@ -1080,6 +1138,7 @@ def main() -> None:
             "clocks": clocks.summary(),
             "gpu_launches": args.steps * LAUNCHES_PER_CALL.get(plan.algorithm, 1),
             "nanstd_precision": precision,
+            "batched": batched,
             "parity_check_rows64": check,
         }
         print(json.dumps(line))

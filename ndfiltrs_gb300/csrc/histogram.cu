@@ -50,9 +50,10 @@ struct HistArgs {
   Geom3 g;
   int TW, TH, SW, SH, S;
   long long tiles_x, tiles;
-  int cols_per_warp;
-  int words;                // per-warp bit histogram: 32-bit words
+  int cols_per_warp;        // columns walked by each half-warp segment
+  int words;                // per-segment bit histogram: 32-bit words
   long long slot_bytes;     // scratch bytes per block slot
+  int digit_bits;           // radix digit width of the block sort (8 or 11)
   Reduce r;
   // Footprint windows: support-linear offsets (y * SW + x) of the taps
   // (nf), of the top and bottom ends of every vertical run of taps (nv
@@ -62,19 +63,20 @@ struct HistArgs {
   int nf, nv, nh;
 };
 
+// A block's sort slot: ping-pong keys and 16-bit payloads (support indices).
 template <typename K>
 struct Slot {
   K* keys_a;
   K* keys_b;
-  uint32_t* pay_a;
-  uint32_t* pay_b;
+  uint16_t* pay_a;
+  uint16_t* pay_b;
 };
 
 __host__ __device__ inline long long align16(long long v) { return (v + 15) & ~15ll; }
 
 template <typename K>
 __host__ __device__ inline long long slot_bytes_for(int S) {
-  return 2 * align16((long long)S * sizeof(K)) + 2 * align16((long long)S * 4);
+  return 2 * align16((long long)S * sizeof(K)) + 2 * align16((long long)S * 2);
 }
 
 template <typename K>
@@ -85,29 +87,33 @@ __device__ inline Slot<K> slot_at(unsigned char* base, int S) {
   off += align16((long long)S * sizeof(K));
   s.keys_b = reinterpret_cast<K*>(base + off);
   off += align16((long long)S * sizeof(K));
-  s.pay_a = reinterpret_cast<uint32_t*>(base + off);
-  off += align16((long long)S * 4);
-  s.pay_b = reinterpret_cast<uint32_t*>(base + off);
+  s.pay_a = reinterpret_cast<uint16_t*>(base + off);
+  off += align16((long long)S * 2);
+  s.pay_b = reinterpret_cast<uint16_t*>(base + off);
   return s;
 }
 
-// One stable counting pass over 8-bit digits. `table` holds kHWarps x 256
-// counters, `totals` 256. Each warp owns a contiguous segment and ranks its
-// 32-key chunks in order with match_any, so equal digits keep their order.
-// Loads are batched (kBatch keys per lane in registers) so a pass costs one
-// memory round trip per batch rather than one per chunk.
+// Shared-memory words of the sort's counter tables for `nd` digits: one
+// table of nd counters per warp plus the nd digit totals.
+__host__ __device__ inline long long sort_table_words(int nd) { return (long long)(kHWarps + 1) * nd; }
+
+// One stable counting pass over `nd`-valued digits. `table` holds
+// kHWarps x nd counters, `totals` nd. Each warp owns a contiguous segment
+// and ranks its 32-key chunks in order with match_any, so equal digits keep
+// their order. Loads are batched (kBatch keys per lane in registers) so a
+// pass costs one memory round trip per batch rather than one per chunk.
 constexpr int kBatch = 16;
 
 template <typename K, typename Digit>
-__device__ void radix_pass(const K* src_k, const uint32_t* src_p, K* dst_k, uint32_t* dst_p, int S,
-                           unsigned int* table, unsigned int* totals, Digit digit) {
+__device__ void radix_pass(const K* src_k, const uint16_t* src_p, K* dst_k, uint16_t* dst_p, int S,
+                           unsigned int* table, unsigned int* totals, int nd, Digit digit) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < kHWarps * 256; i += blockDim.x) table[i] = 0;
+  for (int i = threadIdx.x; i < kHWarps * nd; i += blockDim.x) table[i] = 0;
   __syncthreads();
   const int chunk = (((S + kHWarps - 1) / kHWarps) + 31) & ~31;
   const int begin = warp * chunk;
   const int end = min(S, begin + chunk);
-  unsigned int* wt = table + warp * 256;
+  unsigned int* wt = table + warp * nd;
   for (int b = begin; b < end; b += 32 * kBatch) {
     K keys[kBatch];
 #pragma unroll
@@ -120,51 +126,52 @@ __device__ void radix_pass(const K* src_k, const uint32_t* src_p, K* dst_k, uint
       if (b + j * 32 + lane < end) atomicAdd(&wt[digit(keys[j])], 1u);
   }
   __syncthreads();
-  if (threadIdx.x < 256) {
+  for (int d = threadIdx.x; d < nd; d += blockDim.x) {
     unsigned int sum = 0;
-    for (int w = 0; w < kHWarps; ++w) sum += table[w * 256 + threadIdx.x];
-    totals[threadIdx.x] = sum;
+    for (int w = 0; w < kHWarps; ++w) sum += table[w * nd + d];
+    totals[d] = sum;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
-    // Exclusive scan of 256 totals by one warp (8 per lane).
-    unsigned int local[8];
+    // Exclusive scan of the nd totals by one warp (nd / 32 per lane).
+    const int per = nd >> 5;
     unsigned int run = 0;
-    for (int j = 0; j < 8; ++j) {
-      local[j] = run;
-      run += totals[lane * 8 + j];
+    for (int j = 0; j < per; ++j) {
+      const unsigned int t = totals[lane * per + j];
+      totals[lane * per + j] = run;
+      run += t;
     }
     unsigned int inc = run;
     for (int o = 1; o < 32; o <<= 1) {
-      unsigned int t = __shfl_up_sync(0xffffffffu, inc, o);
+      const unsigned int t = __shfl_up_sync(0xffffffffu, inc, o);
       if (lane >= o) inc += t;
     }
-    unsigned int excl = inc - run;
-    for (int j = 0; j < 8; ++j) totals[lane * 8 + j] = excl + local[j];
+    const unsigned int excl = inc - run;
+    for (int j = 0; j < per; ++j) totals[lane * per + j] += excl;
   }
   __syncthreads();
-  if (threadIdx.x < 256) {
-    unsigned int run = totals[threadIdx.x];
+  for (int d = threadIdx.x; d < nd; d += blockDim.x) {
+    unsigned int run = totals[d];
     for (int w = 0; w < kHWarps; ++w) {
-      unsigned int c = table[w * 256 + threadIdx.x];
-      table[w * 256 + threadIdx.x] = run;
+      const unsigned int c = table[w * nd + d];
+      table[w * nd + d] = run;
       run += c;
     }
   }
   __syncthreads();
   for (int b = begin; b < end; b += 32 * kBatch) {
     K keys[kBatch];
-    uint32_t pays[kBatch];
+    uint16_t pays[kBatch];
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int i = b + j * 32 + lane;
       keys[j] = i < end ? src_k[i] : K(0);
-      pays[j] = i < end ? src_p[i] : 0u;
+      pays[j] = i < end ? src_p[i] : uint16_t(0);
     }
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const bool valid = b + j * 32 + lane < end;
-      const int d = valid ? (int)digit(keys[j]) : 256 + lane;
+      const int d = valid ? (int)digit(keys[j]) : nd + lane;
       const unsigned int peers = __match_any_sync(0xffffffffu, d);
       const int before = __popc(peers & ((1u << lane) - 1u));
       unsigned int pos = 0;
@@ -195,23 +202,26 @@ __device__ __forceinline__ int select_in_word32(unsigned int word, int k) {
   return position;
 }
 
-// Each half-warp (16 lanes, a "segment") owns one bit histogram, so a warp
-// advances two windows per step. `pivot` is a word-aligned rank and `below`
-// the number of window samples ranked below it; both are uniform within the
-// segment. A selection scans 16 words (512 ranks) per iteration from the
-// pivot and leaves the pivot at the word it found, so the next window's
-// order statistic (a few ranks away) is usually found in one iteration.
-// Every loop that contains warp-synchronous operations runs until both
-// segments are done, so the two halves stay converged.
+// Each half-warp (16 lanes, a "segment") owns one bit histogram of the
+// ranks in its window, so a warp advances two windows per step. The segment
+// tracks the rank `m` of its last selected order statistic and the number
+// `lt` of window samples ranked below it, kept up to date by every histogram
+// update. A selection walks from m word by word (every lane loads the same
+// word, so the walk costs what one thread's would); the next window's order
+// statistic is usually a few window samples away, within a word or two. A
+// walk longer than kSeqWords words continues as a parallel scan of 16 words
+// per iteration. Every loop that contains warp-synchronous operations runs
+// until both segments of the warp are done, so the two halves stay converged.
 constexpr int kSeg = 16;
 constexpr int kSegs = kHThreads / kSeg;
 constexpr unsigned int kFull = 0xffffffffu;
+constexpr int kSeqWords = 4;
 
 struct SegHist {
   unsigned int* words;
   int nwords;
-  int pivot;  // multiple of 32
-  int below;
+  int m;      // tracked rank (the last order statistic selected)
+  int lt;     // window samples ranked below m
   int count;  // retained samples in the window
   int nan;    // propagated NaN samples in the window
 };
@@ -243,77 +253,118 @@ __device__ __forceinline__ V seg_bcast(V v, int src) {
   return __shfl_sync(kFull, v, src, kSeg);
 }
 
-// Rank of the k-th (0-based) set bit of the segment's histogram; `active`
-// false runs the loop for convergence only and leaves the state untouched.
-__device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
+// Parallel continuation of a walk. Forward: the rem-th (0-based) set bit at
+// or above word wi. Backward: the rem-th (1-based) set bit counting down
+// from the top of word wi. `active` false takes part for convergence only
+// and returns r unchanged.
+__device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int rem, bool fwd, bool active, int r) {
   const int hl = seg_lane();
-  const bool fwd = k >= h.below;
-  int w0 = h.pivot >> 5;
-  int base = h.below;  // set bits below word w0
   bool found = !active;
-  int result = 0;
   for (int guard = 0; guard < 8192; ++guard) {
-    const int lo = fwd ? w0 : w0 - kSeg;
-    const int wi = lo + hl;
-    const unsigned int word = (wi >= 0 && wi < h.nwords) ? h.words[wi] : 0u;
+    if (!__any_sync(kFull, !found)) break;
+    const int widx = fwd ? wi + hl : wi - hl;
+    const unsigned int word = (widx >= 0 && widx < h.nwords) ? h.words[widx] : 0u;
     const unsigned int pc = __popc(word);
     const unsigned int incl = seg_scan(pc);
     const int total = (int)seg_bcast(incl, kSeg - 1);
-    const int start = fwd ? base : base - total;  // set bits below word lo
-    const bool edge = fwd ? (lo + kSeg >= h.nwords) : (lo <= 0);
-    const unsigned int ball = seg_ballot(start + (int)incl > k);
-    const int L = ball ? __ffs(ball) - 1 : kSeg - 1;
-    const int before = start + (int)seg_bcast(incl - pc, L);
-    const unsigned int w = seg_bcast(word, L);
-    if (!found) {
-      if ((fwd ? start + total > k : start <= k) || edge) {
-        h.pivot = max(lo + L, 0) * 32;
-        h.below = before;
-        result = h.pivot + select_in_word32(w, k - before);
-        found = true;
-      } else if (fwd) {
-        base += total;
-        w0 += kSeg;
-      } else {
-        base = start;
-        w0 = lo;
-      }
-    }
-    if (!__any_sync(kFull, !found)) break;
-  }
-  return result;
-}
-
-// Rank of the first set bit above `rank` (the next retained sample).
-__device__ __forceinline__ int seg_next(const SegHist& h, int rank, bool active) {
-  const int hl = seg_lane();
-  const int wf = rank >> 5;
-  unsigned int first = (rank & 31) == 31 ? 0u : (h.words[wf] & ~((2u << (rank & 31)) - 1u));
-  bool found = !active || first != 0u;
-  int result = first ? (wf << 5) + __ffs(first) - 1 : rank;
-  int w0 = wf + 1;
-  for (int guard = 0; guard < 8192; ++guard) {
-    if (!__any_sync(kFull, !found)) break;
-    const int wi = w0 + hl;
-    const unsigned int word = wi < h.nwords ? h.words[wi] : 0u;
-    const unsigned int ball = seg_ballot(word != 0u);
+    const unsigned int ball = seg_ballot(fwd ? (int)incl > rem : (int)incl >= rem);
     const int L = ball ? __ffs(ball) - 1 : 0;
     const unsigned int w = seg_bcast(word, L);
+    const int excl = (int)seg_bcast(incl - pc, L);
     if (!found) {
       if (ball) {
-        result = ((w0 + L) << 5) + __ffs(w) - 1;
-        found = true;
-      } else if (w0 + kSeg >= h.nwords) {
+        const int within = rem - excl;
+        r = ((fwd ? wi + L : wi - L) << 5) + select_in_word32(w, fwd ? within : __popc(w) - within);
         found = true;
       } else {
-        w0 += kSeg;
+        rem -= total;
+        wi = fwd ? wi + kSeg : wi - kSeg;
+        if (wi < 0 || wi >= h.nwords) found = true;  // no such bit: leave r
       }
     }
   }
-  return result;
+  return r;
 }
 
-// Per-step bookkeeping of a lane: retained, below-pivot and propagated-NaN
+// Rank of the k-th (0-based) retained sample of the segment's window; the
+// tracked rank moves to it. `active` false leaves the state untouched.
+__device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
+  int r = 0, wi = 0, rem = 0;
+  bool fwd = true, done = !active;
+  if (active) {
+    int d = k - h.lt;
+    wi = h.m >> 5;
+    const int bit = h.m & 31;
+    if (d >= 0) {
+      unsigned int w = h.words[wi] & (~0u << bit);
+      int pc = __popc(w);
+#pragma unroll 1
+      for (int s = 0; d >= pc && s < kSeqWords; ++s) {
+        d -= pc;
+        ++wi;
+        w = wi < h.nwords ? h.words[wi] : 0u;
+        pc = __popc(w);
+      }
+      if (d < pc) {
+        r = (wi << 5) + select_in_word32(w, d);
+        done = true;
+      } else {
+        rem = d - pc;
+        ++wi;
+      }
+    } else {
+      int e = -d;
+      unsigned int w = h.words[wi] & ((1u << bit) - 1u);
+      int pc = __popc(w);
+#pragma unroll 1
+      for (int s = 0; e > pc && s < kSeqWords; ++s) {
+        e -= pc;
+        --wi;
+        w = wi >= 0 ? h.words[wi] : 0u;
+        pc = __popc(w);
+      }
+      if (e <= pc) {
+        r = (wi << 5) + select_in_word32(w, pc - e);
+        done = true;
+      } else {
+        rem = e - pc;
+        --wi;
+        fwd = false;
+      }
+    }
+  }
+  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, rem, fwd, !done, r);
+  if (active) {
+    h.m = r;
+    h.lt = k;
+  }
+  return r;
+}
+
+// Rank of the first retained sample above `rank` (the next order statistic).
+__device__ __forceinline__ int seg_next(const SegHist& h, int rank, bool active) {
+  int r = rank, wi = 0;
+  bool done = !active;
+  if (active) {
+    wi = rank >> 5;
+    unsigned int w = h.words[wi] & ~((2u << (rank & 31)) - 1u);
+#pragma unroll 1
+    for (int s = 0; w == 0u && s < kSeqWords; ++s) {
+      ++wi;
+      w = wi < h.nwords ? h.words[wi] : 0u;
+    }
+    if (w) {
+      r = (wi << 5) + __ffs(w) - 1;
+      done = true;
+    } else {
+      ++wi;
+    }
+  }
+  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, 0, true, !done, r);
+  return r;
+}
+
+// Per-step bookkeeping of a lane: retained, below-m and propagated-NaN
 // deltas.
 struct StepDelta {
   int kept = 0, below = 0, nans = 0;
@@ -323,26 +374,25 @@ template <bool PROPAGATE>
 __device__ __forceinline__ void update(const SegHist& h, int c, int sign, StepDelta& d) {
   const bool valid = c < (int)kPropagated;
   if (valid) atomicXor(&h.words[c >> 5], 1u << (c & 31));
-  const int inc = valid ? sign : 0;
-  d.kept += inc;
-  d.below += c < h.pivot ? inc : 0;
+  d.kept += valid ? sign : 0;
+  d.below += c < h.m ? sign : 0;  // codes below m are retained (dropped codes are the largest)
   if (PROPAGATE) d.nans += c == (int)kPropagated ? sign : 0;
 }
 
-// Apply a step's deltas. Under the omit policy the retained and below-pivot
+// Apply a step's deltas. Under the omit policy the retained and below-m
 // deltas share one reduction in two 16-bit halves biased by 1024 per lane,
 // valid while a lane handles fewer than 512 codes (`narrow`).
 template <bool PROPAGATE>
 __device__ __forceinline__ void finish_update(SegHist& h, const StepDelta& d, bool narrow) {
   if (PROPAGATE || !narrow) {
     h.count += seg_sum(d.kept);
-    h.below += seg_sum(d.below);
+    h.lt += seg_sum(d.below);
     if (PROPAGATE) h.nan += seg_sum(d.nans);
   } else {
     const int packed = (d.kept + 1024) | ((d.below + 1024) << 16);
     const unsigned int sum = (unsigned int)seg_sum(packed);
     h.count += (int)(sum & 0xFFFFu) - kSeg * 1024;
-    h.below += (int)(sum >> 16) - kSeg * 1024;
+    h.lt += (int)(sum >> 16) - kSeg * 1024;
   }
   __syncwarp();
 }
@@ -401,58 +451,128 @@ __device__ __forceinline__ void add_taps(const uint16_t* codes, int base, const 
   finish_update<PROPAGATE>(h, d, false);
 }
 
-// The statistic of the segment's window. Every branch on per-segment data
+// The ranks a window's statistic is read from: lo (and hi for an even
+// median or an interpolated percentile), the retained count, and whether
+// the window has a value at all.
+struct Ranks {
+  int lo = 0, hi = 0, n = 0;
+  bool valid = false, two = false;
+};
+
+// Select the ranks of the segment's window. Every branch on per-segment data
 // calls the same sequence of selections, so the warp stays converged.
-template <typename T>
-__device__ __forceinline__ T hist_finish(SegHist& h, const HistArgs& a,
-                                         const typename KeyOf<T>::K* sorted) {
-  using KO = KeyOf<T>;
+__device__ __forceinline__ Ranks hist_ranks(SegHist& h, const HistArgs& a) {
   const Reduce& r = a.r;
+  Ranks o;
+  o.n = h.count;
   const bool valid = !((!r.omit && h.nan > 0) || (r.omit && h.count < r.min_count) || h.count == 0);
   const int last = max(h.count - 1, 0);
   switch (r.kind) {
     case kRank:
     case kRankHistogram: {
       const bool ok = valid && r.param < h.count;
-      const int rank = seg_select(h, ok ? (int)r.param : 0, ok);
-      return ok ? KO::value(sorted[rank]) : nan_of(T());
+      o.lo = o.hi = seg_select(h, ok ? (int)r.param : 0, ok);
+      o.valid = ok;
+      return o;
     }
-    case kMin: {
-      const int rank = seg_select(h, 0, valid);
-      return valid ? KO::value(sorted[rank]) : nan_of(T());
-    }
-    case kMax: {
-      const int rank = seg_select(h, last, valid);
-      return valid ? KO::value(sorted[rank]) : nan_of(T());
-    }
+    case kMin:
+      o.lo = o.hi = seg_select(h, 0, valid);
+      o.valid = valid;
+      return o;
+    case kMax:
+      o.lo = o.hi = seg_select(h, last, valid);
+      o.valid = valid;
+      return o;
     case kPercentile: {
       if (r.q_is_max) {
-        const int rank = seg_select(h, last, valid);
-        return valid ? KO::value(sorted[rank]) : nan_of(T());
+        o.lo = o.hi = seg_select(h, last, valid);
+        o.valid = valid;
+        return o;
       }
       const PctSplit ps = pct_split(r, max(h.count, 1));
-      const int lo = seg_select(h, valid ? ps.lower : 0, valid);
-      const int hi = seg_next(h, lo, valid && ps.upper != ps.lower);
-      if (!valid) return nan_of(T());
-      const T vlo = KO::value(sorted[lo]);
-      const T vhi = ps.upper == ps.lower ? vlo : KO::value(sorted[hi]);
-      return pct_value<T>(ps, vlo, vhi);
+      o.lo = seg_select(h, valid ? ps.lower : 0, valid);
+      o.two = ps.upper != ps.lower;
+      o.hi = seg_next(h, o.lo, valid && o.two);
+      o.valid = valid;
+      return o;
     }
     default: {
       const bool even = (h.count & 1) == 0;
       const int k = even ? h.count / 2 - 1 : h.count / 2;
-      const int lo = seg_select(h, valid ? k : 0, valid);
-      const int hi = seg_next(h, lo, valid && even);
-      if (!valid) return nan_of(T());
-      if (!even) return KO::value(sorted[lo]);
-      if constexpr (sizeof(T) == 4) {
-        return midpoint_f32(KO::value(sorted[lo]), KO::value(sorted[hi]));
-      } else {
-        return midpoint(KO::value(sorted[lo]), KO::value(sorted[hi]));
-      }
+      o.lo = seg_select(h, valid ? k : 0, valid);
+      o.hi = seg_next(h, o.lo, valid && even);
+      o.two = even;
+      o.valid = valid;
+      return o;
     }
   }
 }
+
+// The statistic of a window from its ranks' keys (kl = sorted[lo],
+// kh = sorted[hi]).
+template <typename T>
+__device__ __forceinline__ T hist_value(const Ranks& o, const HistArgs& a, typename KeyOf<T>::K kl,
+                                        typename KeyOf<T>::K kh) {
+  using KO = KeyOf<T>;
+  if (!o.valid) return nan_of(T());
+  const T vlo = KO::value(kl);
+  switch (a.r.kind) {
+    case kPercentile: {
+      if (a.r.q_is_max) return vlo;
+      const PctSplit ps = pct_split(a.r, max(o.n, 1));
+      return pct_value<T>(ps, vlo, o.two ? KO::value(kh) : vlo);
+    }
+    case kRank:
+    case kRankHistogram:
+    case kMin:
+    case kMax:
+      return vlo;
+    default:
+      if (!o.two) return vlo;
+      if constexpr (sizeof(T) == 4) {
+        return midpoint_f32(vlo, KO::value(kh));
+      } else {
+        return midpoint(vlo, KO::value(kh));
+      }
+  }
+}
+
+// Outputs of a walk, one per lane of the segment: the ranks are selected in
+// order (one window after another) and parked in lane i % 16; every 16
+// outputs the batch's keys are loaded (one independent load per lane), and
+// the previous batch's values are computed and stored, so the loads' latency
+// overlaps the next 16 windows.
+template <typename T>
+struct OutPipe {
+  using K = typename KeyOf<T>::K;
+  Ranks next;             // ranks parked in this lane
+  long long next_at = -1; // its output index (-1: none / not stored)
+  Ranks held;             // the previous batch: ranks and loaded keys
+  long long held_at = -1;
+  K kl = 0, kh = 0;
+
+  __device__ __forceinline__ void park(const Ranks& o, long long at, int slot) {
+    if (seg_lane() == slot) {
+      next = o;
+      next_at = at;
+    }
+  }
+  __device__ __forceinline__ void complete(const HistArgs& a, T* __restrict__ out) {
+    if (held_at >= 0) out[held_at] = canonical(hist_value<T>(held, a, kl, kh));
+    held_at = -1;
+  }
+  // Complete the held batch, then load the parked one's keys and hold it.
+  __device__ __forceinline__ void rotate(const HistArgs& a, const K* sorted, T* __restrict__ out) {
+    complete(a, out);
+    if (next_at >= 0) {
+      kl = next.valid ? sorted[next.lo] : K(0);
+      kh = next.valid && next.two ? sorted[next.hi] : kl;
+    }
+    held = next;
+    held_at = next_at;
+    next_at = -1;
+  }
+};
 
 // A segment's boustrophedon walk over columns [c_begin, c_begin + ncols)
 // of its tile; columns at or beyond `tw_eff` are computed for convergence
@@ -468,7 +588,6 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
                                      long long y0, long long x0, const Geom3& g, const HistArgs& a,
                                      const typename KeyOf<T>::K* sorted, T* __restrict__ out,
                                      SegHist& h) {
-  const int hl = seg_lane();
   const uint16_t* top = lists + a.nf;
   const uint16_t* bottom = top + a.nv;
   const uint16_t* left = bottom + a.nv;
@@ -477,13 +596,19 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
     add_taps<PROPAGATE>(codes, c_begin, lists, a.nf, h);
   else
     add_box<PROPAGATE>(codes, c_begin, kh, kw, SW, h);
+  OutPipe<T> pipe;
+  int slot = 0;
   int row = 0;
   int dir = 1;
   for (int j = 0; j < ncols; ++j) {
     const int c = c_begin + j;
     for (int i = 0; i < th_eff; ++i) {
-      T result = hist_finish<T>(h, a, sorted);
-      if (hl == 0 && c < tw_eff) out[(y0 + row) * g.W + x0 + c] = canonical(result);
+      const Ranks o = hist_ranks(h, a);
+      pipe.park(o, c < tw_eff ? (y0 + row) * g.W + x0 + c : -1, slot);
+      if (++slot == kSeg) {
+        pipe.rotate(a, sorted, out);
+        slot = 0;
+      }
       if (i + 1 < th_eff) {
         const int o = row * SW + c;
         if (dir > 0) {
@@ -510,6 +635,8 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
     }
     dir = -dir;
   }
+  pipe.rotate(a, sorted, out);
+  pipe.complete(a, out);
 }
 
 template <typename T, bool SDEC, bool FP>
@@ -519,7 +646,6 @@ __global__ void __launch_bounds__(kHThreads, 1)
   using K = typename KeyOf<T>::K;
   const K kSent = KeyOf<T>::kSentinel;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ unsigned int totals[256];
   __shared__ K red_and[kHWarps], red_or[kHWarps];
   __shared__ int red_sent[kHWarps];
   const Geom3& g = a.g;
@@ -533,6 +659,9 @@ __global__ void __launch_bounds__(kHThreads, 1)
   K* decode_s = reinterpret_cast<K*>(smem + align16((long long)a.S * 2) + list_bytes);
   unsigned int* work = reinterpret_cast<unsigned int*>(
       smem + align16((long long)a.S * 2) + list_bytes + (SDEC ? align16((long long)a.S * sizeof(K)) : 0));
+  const int nd = 1 << a.digit_bits;
+  unsigned int* table = work;
+  unsigned int* totals = work + kHWarps * nd;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (FP) {
     // Made visible by the first barrier of the tile loop.
@@ -558,7 +687,7 @@ __global__ void __launch_bounds__(kHThreads, 1)
                           map_index(x0 + sx - g.ax, g.W, g.mx, &mx);
       const K key = inside ? sample_key<T>(__ldg(in + my * g.W + mx), drop_inf) : outside;
       slot.keys_a[e] = key;
-      slot.pay_a[e] = (uint32_t)e;
+      slot.pay_a[e] = (uint16_t)e;
       if (key != kSent) {
         k_and &= key;
         k_or |= key;
@@ -585,36 +714,30 @@ __global__ void __launch_bounds__(kHThreads, 1)
       k_or |= red_or[w];
       sent += red_sent[w];
     }
-    // Sort keys (LSD, 8-bit digits over the varying bits, then sentinels last).
+    // Sort keys (LSD over the bits on which the retained keys differ). The
+    // dropped samples' all-ones keys take part like any other key: an LSD
+    // sort orders the retained keys among themselves whatever lies between
+    // them, and a dropped sample's position is never set in a histogram.
     K* src_k = slot.keys_a;
     K* dst_k = slot.keys_b;
-    uint32_t* src_p = slot.pay_a;
-    uint32_t* dst_p = slot.pay_b;
+    uint16_t* src_p = slot.pay_a;
+    uint16_t* dst_p = slot.pay_b;
     const K varying = sent == S ? K(0) : (k_and ^ k_or);
     if (varying != 0) {
       const int bits = (int)sizeof(K) * 8;
       const int lo = sizeof(K) == 8 ? __ffsll((long long)varying) - 1 : __ffs((int)varying) - 1;
       const int hi = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)varying) : __clz((int)varying));
-      for (int shift = lo; shift <= hi; shift += 8) {
-        radix_pass(src_k, src_p, dst_k, dst_p, S, work, totals,
-                   [shift](K key) { return (unsigned int)((key >> shift) & 0xFFu); });
+      const K mask = (K)(nd - 1);
+      for (int shift = lo; shift <= hi; shift += a.digit_bits) {
+        radix_pass(src_k, src_p, dst_k, dst_p, S, table, totals, nd,
+                   [shift, mask](K key) { return (unsigned int)((key >> shift) & mask); });
         K* tk = src_k;
         src_k = dst_k;
         dst_k = tk;
-        uint32_t* tp = src_p;
+        uint16_t* tp = src_p;
         src_p = dst_p;
         dst_p = tp;
       }
-    }
-    if (sent > 0 && sent < S) {
-      radix_pass(src_k, src_p, dst_k, dst_p, S, work, totals,
-                 [kSent](K key) { return key == kSent ? 1u : 0u; });
-      K* tk = src_k;
-      src_k = dst_k;
-      dst_k = tk;
-      uint32_t* tp = src_p;
-      src_p = dst_p;
-      dst_p = tp;
     }
     const uint16_t dropped = a.r.omit ? kOmitted : kPropagated;
     for (int pos = threadIdx.x; pos < S; pos += blockDim.x) {
@@ -632,8 +755,8 @@ __global__ void __launch_bounds__(kHThreads, 1)
     SegHist h;
     h.words = work + seg * a.words;
     h.nwords = a.words;
-    h.pivot = 0;
-    h.below = 0;
+    h.m = 0;
+    h.lt = 0;
     h.count = 0;
     h.nan = 0;
     for (int i = seg_lane(); i < a.words; i += kSeg) h.words[i] = 0u;
@@ -669,13 +792,23 @@ struct Runs {
   int entries() const { return footprint ? nf + 2 * nv + 2 * nh : 0; }
 };
 
+// Bytes of the work region (the sort's 8-bit-digit tables, or the
+// segments' bit histograms while sliding, whichever is larger).
+size_t work_bytes_for(int S) {
+  const size_t sort = (size_t)sort_table_words(256) * 4;
+  const size_t hist = (size_t)kSegs * ((S + 31) / 32) * 4;
+  return std::max(sort, hist);
+}
+
+// The sort uses 11-bit digits (three passes cover 32 varying bits) when
+// their tables fit in the work region, else 8-bit digits.
+int digit_bits_for(int S) { return work_bytes_for(S) >= (size_t)sort_table_words(2048) * 4 ? 11 : 8; }
+
 size_t smem_bytes_for(int S, bool sdec, size_t key_bytes, int list_entries) {
   size_t codes = (size_t)align16((long long)S * 2);
   size_t lists = (size_t)align16((long long)list_entries * 2);
   size_t decode = sdec ? (size_t)align16((long long)S * (long long)key_bytes) : 0;
-  size_t sort = (size_t)kHWarps * 256 * 4;
-  size_t hist = (size_t)kSegs * ((S + 31) / 32) * 4;
-  return codes + lists + decode + std::max(sort, hist);
+  return codes + lists + decode + work_bytes_for(S);
 }
 
 // Count the taps and the vertical and horizontal runs of a kh x kw
@@ -754,6 +887,7 @@ HistArgs make_args_core(const Geom3& g, int TW, int TH, int dtype, const Reduce&
   a.cols_per_warp = (a.TW + kSegs - 1) / kSegs;  // columns per half-warp segment
   a.words = (a.S + 31) / 32;
   a.slot_bytes = dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
+  a.digit_bits = digit_bits_for(a.S);
   a.r = r;
   a.lists = nullptr;
   a.nf = a.g.kh * a.g.kw;
@@ -775,6 +909,7 @@ HistArgs make_args(const Plan& p) {
   a.cols_per_warp = (a.TW + kSegs - 1) / kSegs;  // columns per half-warp segment
   a.words = (a.S + 31) / 32;
   a.slot_bytes = p.dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
+  a.digit_bits = digit_bits_for(a.S);
   a.r = p.r;
   if (p.hist_footprint) {
     a.lists = p.d_hist_lists;
