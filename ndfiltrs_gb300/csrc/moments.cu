@@ -6,14 +6,15 @@
 //    flags and the scaled overflow retry (src/filter_nd.rs:142-158,
 //    src/mean.rs:28-113), and dispersion_valid (src/dispersion.rs:5-61).
 //    Results are bit-identical to the reference.
-//  * NDF_MOMENTS_FP32C (default) shifts every retained sample by the
-//    window's pivot (its first retained sample, as dispersion_valid does)
-//    and accumulates the deviation sums in FP32 with error-free
-//    transformations: two-sum deviations, two-product squares, Neumaier sums
-//    (float32 input) or float-float sums over triple-float staged values
-//    (float64 input). FP64 runs only in the final combine (mean = p + S1/n,
-//    var = (S2 - S1^2/n) / (n - ddof), sqrt). Windows whose deviations leave
-//    the range where FP32 squares are safe fall back to the FP64 path.
+//  * NDF_MOMENTS_FP32C (default) sums exactly: per tile, every sample's
+//    deviation from the tile's pivot becomes an exact integer in units of
+//    the tile's lowest set bit (fixed_moments.cuh); each window sums X and
+//    X^2 in 64- / 128-bit integers, the mean is the exact n P + S1 divided
+//    once, the variance's numerator n S2 - S1^2 is exact in 192 bits, and
+//    FP64 runs only for the conversion, the division, the scaling and the
+//    square root (float32 outputs finish in float-float on the FP32 pipe).
+//    Results are the exact moments rounded to within about an ulp. Tiles
+//    whose span does not fit the integers take the FP64 path.
 #include "moments.cuh"
 
 namespace ndf {
@@ -84,12 +85,12 @@ cudaError_t launch_tile_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
 size_t tile_moments_smem(const Plan& p, const Tile& t) {
   size_t elem = p.dtype == 0 ? 4 : 8;
   size_t support = (size_t)p.tile.g.kd * t.SH * t.SW;
-  // Remap tables | staged values (| triple-float copies) | tap offsets, laid
-  // out as tile_moments_body does.
-  size_t staged = support * elem;
-  if (p.dtype == 1 && p.r.moments == 0) staged += support * sizeof(Triple);
-  return (size_t)(t.SW + t.SH + p.tile.g.kd) * 8 + (staged + 15) / 16 * 16 +
-         (size_t)p.r.count * sizeof(int32_t);
+  // Remap tables | staged values | (FP32C: deviations and count increments,
+  // 8 bytes each per sample) | tap offsets, laid out as tile_moments_body
+  // does.
+  size_t staged = (support * elem + 15) / 16 * 16;
+  if (p.r.moments == 0) staged += support * 16;
+  return (size_t)(t.SW + t.SH + p.tile.g.kd) * 8 + staged + (size_t)p.r.count * sizeof(int32_t);
 }
 
 cudaError_t launch_tile_moments(const Plan& p, const void* in, void* out, cudaStream_t s) {
