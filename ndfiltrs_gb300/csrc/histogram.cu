@@ -253,11 +253,11 @@ __device__ __forceinline__ V seg_bcast(V v, int src) {
   return __shfl_sync(kFull, v, src, kSeg);
 }
 
-// Parallel continuation of a walk. Forward: the rem-th (0-based) set bit at
-// or above word wi. Backward: the rem-th (1-based) set bit counting down
-// from the top of word wi. `active` false takes part for convergence only
-// and returns r unchanged.
-__device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int rem, bool fwd, bool active, int r) {
+// Parallel continuation of a walk: the t-th (1-based) set bit met when
+// walking from word wi upwards (fwd) or downwards, whole words at a time, 16
+// words per iteration. `active` false takes part for convergence only and
+// returns r unchanged.
+__device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int t, bool fwd, bool active, int r) {
   const int hl = seg_lane();
   bool found = !active;
   for (int guard = 0; guard < 8192; ++guard) {
@@ -267,17 +267,17 @@ __device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int rem, b
     const unsigned int pc = __popc(word);
     const unsigned int incl = seg_scan(pc);
     const int total = (int)seg_bcast(incl, kSeg - 1);
-    const unsigned int ball = seg_ballot(fwd ? (int)incl > rem : (int)incl >= rem);
+    const unsigned int ball = seg_ballot((int)incl >= t);
     const int L = ball ? __ffs(ball) - 1 : 0;
     const unsigned int w = seg_bcast(word, L);
     const int excl = (int)seg_bcast(incl - pc, L);
     if (!found) {
       if (ball) {
-        const int within = rem - excl;
-        r = ((fwd ? wi + L : wi - L) << 5) + select_in_word32(w, fwd ? within : __popc(w) - within);
+        const int within = t - excl;  // 1-based, in walking order
+        r = ((fwd ? wi + L : wi - L) << 5) + select_in_word32(w, fwd ? within - 1 : __popc(w) - within);
         found = true;
       } else {
-        rem -= total;
+        t -= total;
         wi = fwd ? wi + kSeg : wi - kSeg;
         if (wi < 0 || wi >= h.nwords) found = true;  // no such bit: leave r
       }
@@ -286,54 +286,45 @@ __device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int rem, b
   return r;
 }
 
+// Rank of the t-th (1-based) set bit met when walking from rank `from`
+// upwards (fwd: ranks >= from) or downwards (ranks < from). Both directions
+// run the same instructions, so the two segments of a warp never take
+// different paths; a walk longer than kSeqWords words continues in parallel.
+__device__ __forceinline__ int seg_walk(const SegHist& h, int from, int t, bool fwd, bool active) {
+  int r = 0, wi = 0;
+  bool done = !active;
+  if (active) {
+    wi = from >> 5;
+    const int bit = from & 31;
+    const int dir = fwd ? 1 : -1;
+    unsigned int w = wi < h.nwords ? h.words[wi] : 0u;
+    w &= fwd ? (~0u << bit) : ((1u << bit) - 1u);
+    int pc = __popc(w);
+#pragma unroll 1
+    for (int s = 0; t > pc && s < kSeqWords; ++s) {
+      t -= pc;
+      wi += dir;
+      w = (wi >= 0 && wi < h.nwords) ? h.words[wi] : 0u;
+      pc = __popc(w);
+    }
+    if (t <= pc) {
+      r = (wi << 5) + select_in_word32(w, fwd ? t - 1 : pc - t);
+      done = true;
+    } else {
+      t -= pc;
+      wi += dir;
+    }
+  }
+  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, t, fwd, !done, r);
+  return r;
+}
+
 // Rank of the k-th (0-based) retained sample of the segment's window; the
 // tracked rank moves to it. `active` false leaves the state untouched.
 __device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
-  int r = 0, wi = 0, rem = 0;
-  bool fwd = true, done = !active;
-  if (active) {
-    int d = k - h.lt;
-    wi = h.m >> 5;
-    const int bit = h.m & 31;
-    if (d >= 0) {
-      unsigned int w = h.words[wi] & (~0u << bit);
-      int pc = __popc(w);
-#pragma unroll 1
-      for (int s = 0; d >= pc && s < kSeqWords; ++s) {
-        d -= pc;
-        ++wi;
-        w = wi < h.nwords ? h.words[wi] : 0u;
-        pc = __popc(w);
-      }
-      if (d < pc) {
-        r = (wi << 5) + select_in_word32(w, d);
-        done = true;
-      } else {
-        rem = d - pc;
-        ++wi;
-      }
-    } else {
-      int e = -d;
-      unsigned int w = h.words[wi] & ((1u << bit) - 1u);
-      int pc = __popc(w);
-#pragma unroll 1
-      for (int s = 0; e > pc && s < kSeqWords; ++s) {
-        e -= pc;
-        --wi;
-        w = wi >= 0 ? h.words[wi] : 0u;
-        pc = __popc(w);
-      }
-      if (e <= pc) {
-        r = (wi << 5) + select_in_word32(w, pc - e);
-        done = true;
-      } else {
-        rem = e - pc;
-        --wi;
-        fwd = false;
-      }
-    }
-  }
-  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, rem, fwd, !done, r);
+  const int d = k - h.lt;
+  const bool fwd = d >= 0;
+  const int r = seg_walk(h, h.m, fwd ? d + 1 : -d, fwd, active);
   if (active) {
     h.m = r;
     h.lt = k;
@@ -343,25 +334,7 @@ __device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
 
 // Rank of the first retained sample above `rank` (the next order statistic).
 __device__ __forceinline__ int seg_next(const SegHist& h, int rank, bool active) {
-  int r = rank, wi = 0;
-  bool done = !active;
-  if (active) {
-    wi = rank >> 5;
-    unsigned int w = h.words[wi] & ~((2u << (rank & 31)) - 1u);
-#pragma unroll 1
-    for (int s = 0; w == 0u && s < kSeqWords; ++s) {
-      ++wi;
-      w = wi < h.nwords ? h.words[wi] : 0u;
-    }
-    if (w) {
-      r = (wi << 5) + __ffs(w) - 1;
-      done = true;
-    } else {
-      ++wi;
-    }
-  }
-  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, 0, true, !done, r);
-  return r;
+  return seg_walk(h, rank + 1, 1, true, active);
 }
 
 // Per-step bookkeeping of a lane: retained, below-m and propagated-NaN
@@ -398,17 +371,42 @@ __device__ __forceinline__ void finish_update(SegHist& h, const StepDelta& d, bo
 }
 
 // Remove the codes of one face and add those of another (n codes each,
-// `stride` apart, in shared memory).
-template <bool PROPAGATE>
+// `stride` apart, in shared memory; STRIDE > 0 fixes the stride at compile
+// time). Each lane takes every 16th pair of the first 16 * (n / 16); the
+// n % 16 left over pairs are spread one code per lane (lanes [0, r) remove,
+// [r, 2r) add) when they fit, so a 65-wide face costs four full iterations
+// and one single-code step instead of five pair iterations.
+template <bool PROPAGATE, int STRIDE>
 __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, int add_start, int n,
-                                     int stride, SegHist& h) {
+                                     int stride_rt, SegHist& h) {
+  const int stride = STRIDE > 0 ? STRIDE : stride_rt;
   const int hl = seg_lane();
   StepDelta d;
-  for (int i = hl; i < n; i += kSeg) {
-    const int rc = codes[remove_start + i * stride];
-    const int ac = codes[add_start + i * stride];
-    update<PROPAGATE>(h, rc, -1, d);
-    update<PROPAGATE>(h, ac, +1, d);
+  const int full = n / kSeg, rem = n - full * kSeg;
+  const uint16_t* rp = codes + remove_start + hl * stride;
+  const uint16_t* ap = codes + add_start + hl * stride;
+  const int jump = kSeg * stride;
+  for (int it = 0; it < full; ++it) {
+    update<PROPAGATE>(h, *rp, -1, d);
+    update<PROPAGATE>(h, *ap, +1, d);
+    rp += jump;
+    ap += jump;
+  }
+  if (rem) {
+    if (2 * rem <= kSeg) {
+      int c = kOmitted, sign = 0;
+      if (hl < rem) {
+        c = codes[remove_start + (full * kSeg + hl) * stride];
+        sign = -1;
+      } else if (hl < 2 * rem) {
+        c = codes[add_start + (full * kSeg + hl - rem) * stride];
+        sign = +1;
+      }
+      update<PROPAGATE>(h, c, sign, d);
+    } else if (hl < rem) {
+      update<PROPAGATE>(h, *rp, -1, d);
+      update<PROPAGATE>(h, *ap, +1, d);
+    }
   }
   finish_update<PROPAGATE>(h, d, n <= 8 * 1024);
 }
@@ -615,13 +613,13 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
           if (FP)
             step_lists<PROPAGATE>(codes, o, top, o + SW, bottom, a.nv, h);
           else
-            step<PROPAGATE>(codes, o, o + kh * SW, kw, 1, h);
+            step<PROPAGATE, 1>(codes, o, o + kh * SW, kw, 1, h);
           ++row;
         } else {
           if (FP)
             step_lists<PROPAGATE>(codes, o, bottom, o - SW, top, a.nv, h);
           else
-            step<PROPAGATE>(codes, o + (kh - 1) * SW, o - SW, kw, 1, h);
+            step<PROPAGATE, 1>(codes, o + (kh - 1) * SW, o - SW, kw, 1, h);
           --row;
         }
       }
@@ -631,7 +629,7 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
       if (FP)
         step_lists<PROPAGATE>(codes, o, left, o + 1, right, a.nh, h);
       else
-        step<PROPAGATE>(codes, o, o + kw, kh, SW, h);
+        step<PROPAGATE, 0>(codes, o, o + kw, kh, SW, h);
     }
     dir = -dir;
   }
