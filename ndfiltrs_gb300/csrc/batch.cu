@@ -195,9 +195,30 @@ struct FamilyState {
   int32_t* d_pool = nullptr;
 };
 
+// A family of a specialised kernel reached through FamilyOps (box pair,
+// sliding histogram, sliding moments): one (kind, variant) pair.
+constexpr int kOpsKinds = 3;
+
+const FamilyOps& ops_of(int kind) {
+  return kind == 0 ? box_family_ops() : kind == 1 ? histogram_family_ops() : slide_family_ops();
+}
+
+struct OpsFamily {
+  int kind = 0, variant = 0;
+  std::vector<int> images;
+  std::vector<long long> first;     // first tile of each image in the family's list
+  long long tiles = 0, slot_bytes = 0;
+  size_t smem = 0;
+  int grid = 0;
+  unsigned char* d_tasks = nullptr;
+  unsigned char* h_tasks = nullptr;  // pinned staging read by the graph's copy node
+  unsigned char* d_scratch = nullptr;
+};
+
 struct Segment {
   std::vector<int> images;  // batch image indices, ascending
   FamilyState families[kFamilies];
+  std::vector<OpsFamily> ops;  // box pair, histogram and sliding moments families
   std::vector<int> own;     // images launched through their own plan
   std::vector<const void*> in_ptrs;
   std::vector<void*> out_ptrs;
@@ -278,6 +299,12 @@ void release_segment(Segment& s) {
     f.d_pool = nullptr;
     f.h_tasks = nullptr;
   }
+  for (auto& f : s.ops) {
+    if (f.d_tasks) cudaFree(f.d_tasks);
+    if (f.h_tasks) cudaFreeHost(f.h_tasks);
+    if (f.d_scratch) cudaFree(f.d_scratch);
+    f.d_tasks = f.h_tasks = f.d_scratch = nullptr;
+  }
 }
 
 void destroy_batch(ndf_batch* b) {
@@ -319,7 +346,28 @@ int build_segment(ndf_batch* b, Segment& s, const std::vector<int>& images) {
     if (p.n_out == 0) continue;
     const int fam = b->family_of[i];
     if (fam < 0) {
-      s.own.push_back(i);
+      int kind = 0, variant = -1;
+      for (; kind < kOpsKinds && variant < 0; ++kind) variant = ops_of(kind).variant(p);
+      if (variant < 0) {
+        s.own.push_back(i);
+        continue;
+      }
+      --kind;
+      OpsFamily* f = nullptr;
+      for (auto& o : s.ops)
+        if (o.kind == kind && o.variant == variant) f = &o;
+      if (!f) {
+        s.ops.emplace_back();
+        f = &s.ops.back();
+        f->kind = kind;
+        f->variant = variant;
+      }
+      const FamilyOps& ops = ops_of(kind);
+      f->images.push_back(i);
+      f->first.push_back(f->tiles);
+      f->tiles += ops.tiles(p);
+      f->smem = std::max(f->smem, p.smem_bytes);
+      f->slot_bytes = std::max(f->slot_bytes, ops.slot_bytes(p));
       continue;
     }
     FamilyState& f = s.families[fam];
@@ -357,6 +405,20 @@ int build_segment(ndf_batch* b, Segment& s, const std::vector<int>& images) {
     std::memcpy(f.h_tasks, f.tasks.data(), task_bytes);
     f.grid = (int)std::min<long long>(f.tiles, (long long)std::max(per_sm, 1) * b->sm_count);
   }
+  for (auto& f : s.ops) {
+    const FamilyOps& ops = ops_of(f.kind);
+    const void* kernel = ops.kernel(f.variant);
+    cudaError_t e = allow_max_smem(kernel);
+    int per_sm = 1;
+    const int threads = f.kind == 1 ? 512 : kThreads;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, f.smem);
+    f.grid = (int)std::min<long long>(f.tiles, (long long)std::max(per_sm, 1) * b->sm_count);
+    const size_t bytes = f.images.size() * ops.task_bytes;
+    if (e == cudaSuccess) e = cudaMalloc(&f.d_tasks, bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&f.h_tasks, bytes);
+    if (e == cudaSuccess && f.slot_bytes > 0) e = cudaMalloc(&f.d_scratch, (size_t)f.grid * (size_t)f.slot_bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "batch setup");
+  }
   return NDF_OK;
 }
 
@@ -382,6 +444,13 @@ int capture_segment(ndf_batch* b, Segment& s, const void* const* d_in, void* con
       f.h_tasks[k].in = (const float*)d_in[f.images[k]];
       f.h_tasks[k].out = (float*)d_out[f.images[k]];
     }
+  for (auto& f : s.ops) {
+    const FamilyOps& ops = ops_of(f.kind);
+    for (size_t k = 0; k < f.images.size(); ++k) {
+      const int i = f.images[k];
+      ops.write_task(b->plans[i]->p, d_in[i], d_out[i], f.first[k], f.h_tasks + k * ops.task_bytes);
+    }
+  }
   if (s.exec) cudaGraphExecDestroy(s.exec);
   if (s.graph) cudaGraphDestroy(s.graph);
   s.exec = nullptr;
@@ -409,6 +478,16 @@ int capture_segment(ndf_batch* b, Segment& s, const void* const* d_in, void* con
     e = cudaMemcpyAsync(f.d_tasks, f.h_tasks, f.tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) break;
     e = launch_family(fam, f, st);
+    ++launches;
+  }
+  for (auto& f : s.ops) {
+    if (e != cudaSuccess) break;
+    const FamilyOps& ops = ops_of(f.kind);
+    cudaStream_t st = branch();
+    e = cudaMemcpyAsync(f.d_tasks, f.h_tasks, f.images.size() * ops.task_bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) break;
+    e = ops.launch(f.variant, f.d_tasks, (int)f.images.size(), f.tiles, f.d_scratch, f.slot_bytes, f.smem, f.grid,
+                   st);
     ++launches;
   }
   for (size_t k = 0; k < s.own.size() && e == cudaSuccess && rc == NDF_OK; ++k) {

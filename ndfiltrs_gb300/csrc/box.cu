@@ -1,6 +1,8 @@
 // Box-window pair kernel (see tile_box_kernel): 3x3, 5x5 and 7x7 windows in
 // 2-D arrays, two vertically adjacent outputs per thread sharing the sort of
 // their common rows.
+#include <cstring>
+
 #include "network.cuh"
 
 namespace ndf {
@@ -73,26 +75,26 @@ __device__ __forceinline__ T box_median(const K (&sh)[P], const K (&pv)[P], int 
   return network_finish<T, 2 * P, V, 1>(m, nv, r);
 }
 
+// One output tile (index `tile`) of the box pair kernel; `tmap` is the
+// launch's tensor map (nullptr: remapped staging only).
 template <typename T, int KH, int KW, int MODE>
-__global__ void __launch_bounds__(kThreads)
-    tile_box_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
-                    const __grid_constant__ CUtensorMap tmap) {
+__device__ __forceinline__ void tile_box_body(const T* __restrict__ in, T* __restrict__ out, const TileArgs& a,
+                                              long long tile, unsigned char* smem_raw, const CUtensorMap* tmap) {
   using K = typename KeyOf<T>::K;
   constexpr K kSent = KeyOf<T>::kSentinel;
   constexpr int SW = kBoxTW + KW - 1;
   constexpr int SHARED = (KH - 1) * KW;
   constexpr int P = pow2_at_least(SHARED > KW ? SHARED : KW);
   constexpr int V = KH * KW;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   const Geom3& g = a.g;
   const Tile& t = a.t;
   long long* maps = reinterpret_cast<long long*>(smem_raw);
   K* s = reinterpret_cast<K*>(maps + (t.SW + t.SH + g.kd));
   long long z, y0, x0;
-  tile_coords(a, blockIdx.x, z, y0, x0);
+  tile_coords(a, tile, z, y0, x0);
   const bool drop_inf = a.r.drop_inf;
   const K outside = sample_key<T>((T)a.r.cval, drop_inf);
-  if (!stage_tile(s, maps, smem_raw, in, a, &tmap, z, y0, x0, outside,
+  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, outside,
                   [&](T v) { return sample_key<T>(v, drop_inf); }))
     return;
   __syncthreads();
@@ -150,6 +152,60 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+template <typename T, int KH, int KW, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    tile_box_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
+                    const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  tile_box_body<T, KH, KW, MODE>(in, out, a, blockIdx.x, smem_raw, &tmap);
+}
+
+// Batched images (float32) of one box size and epilogue: one persistent
+// launch over the concatenated tile lists; a block finds a tile's image by
+// binary search over the images' first tiles and keeps its arguments in
+// shared memory until the image changes. Staging is the remapped path.
+struct BoxTask {
+  const float* in;
+  float* out;
+  long long first_tile;
+  TileArgs a;
+};
+
+template <int KH, int KW, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    box_family_kernel(const BoxTask* __restrict__ tasks, int ntasks, long long total_tiles) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ BoxTask task;
+  __shared__ int current, found;
+  if (threadIdx.x == 0) current = -1;
+  __syncthreads();
+  for (long long tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = ntasks - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].first_tile <= tile)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      found = lo;
+    }
+    __syncthreads();
+    const int index = found;
+    if (index != current) {
+      const long long* src = reinterpret_cast<const long long*>(tasks + index);
+      long long* dst = reinterpret_cast<long long*>(&task);
+      for (int i = threadIdx.x; i < (int)(sizeof(BoxTask) / 8); i += blockDim.x) dst[i] = src[i];
+      __syncthreads();
+      if (threadIdx.x == 0) current = index;
+    }
+    __syncthreads();
+    tile_box_body<float, KH, KW, MODE>(task.in, task.out, task.a, tile - task.first_tile, smem_raw, nullptr);
+    __syncthreads();
+  }
+}
+
 template <typename T, int KH, int KW>
 cudaError_t launch_box(const Plan& p, const T* in, T* out, cudaStream_t s) {
   const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork;
@@ -200,6 +256,55 @@ cudaError_t launch_tile_box(const Plan& p, const void* in, void* out, cudaStream
     if (kh == 5 && kw == 5) return launch_box<double, 5, 5>(p, i, o, s);
   }
   return cudaErrorInvalidValue;
+}
+
+namespace {
+
+// Variants: 2 * size index (3x3, 5x5, 7x7) + median epilogue.
+int box_family_variant(const Plan& p) {
+  if (p.algo != Algo::kTileBox || p.dtype != 0) return -1;
+  const Geom3& g = p.tile.g;
+  const int size = g.kh == 3 && g.kw == 3 ? 0 : g.kh == 5 && g.kw == 5 ? 1 : g.kh == 7 && g.kw == 7 ? 2 : -1;
+  if (size < 0) return -1;
+  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork;
+  return 2 * size + (median ? 1 : 0);
+}
+
+long long box_family_tiles(const Plan& p) { return p.tile.t.tiles; }
+
+long long box_family_slot_bytes(const Plan&) { return 0; }
+
+void box_family_write_task(const Plan& p, const void* in, void* out, long long first_tile, void* task) {
+  BoxTask t{};
+  t.in = (const float*)in;
+  t.out = (float*)out;
+  t.first_tile = first_tile;
+  t.a = p.tile;
+  t.a.r = p.r;
+  t.a.tma_bw = 0;
+  std::memcpy(task, &t, sizeof(t));
+}
+
+const void* box_family_kernel_of(int v) {
+  static const void* const table[] = {
+      (const void*)box_family_kernel<3, 3, 0>, (const void*)box_family_kernel<3, 3, 1>,
+      (const void*)box_family_kernel<5, 5, 0>, (const void*)box_family_kernel<5, 5, 1>,
+      (const void*)box_family_kernel<7, 7, 0>, (const void*)box_family_kernel<7, 7, 1>};
+  return table[v];
+}
+
+cudaError_t box_family_launch(int v, const void* d_tasks, int ntasks, long long tiles, unsigned char*, long long,
+                              size_t smem, int grid, cudaStream_t s) {
+  void* args[] = {(void*)&d_tasks, &ntasks, &tiles};
+  return cudaLaunchKernel(box_family_kernel_of(v), dim3(grid), dim3(kThreads), args, smem, s);
+}
+
+}  // namespace
+
+const FamilyOps& box_family_ops() {
+  static const FamilyOps ops{sizeof(BoxTask), box_family_variant, box_family_tiles, box_family_slot_bytes,
+                             box_family_write_task, box_family_kernel_of, box_family_launch};
+  return ops;
 }
 
 }  // namespace ndf

@@ -26,6 +26,7 @@
 //    so every half-warp's columns lie inside the tile's support.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -49,7 +50,8 @@ constexpr int kMaxSupport = 65534;
 struct HistArgs {
   Geom3 g;
   int TW, TH, SW, SH, S;
-  long long tiles_x, tiles;
+  int plane;                // SH * SW: one support plane (the support is kd planes)
+  long long tiles_x, tiles_yx, tiles;
   int cols_per_warp;        // columns walked by each half-warp segment
   int words;                // per-segment bit histogram: 32-bit words
   long long slot_bytes;     // scratch bytes per block slot
@@ -253,11 +255,11 @@ __device__ __forceinline__ V seg_bcast(V v, int src) {
   return __shfl_sync(kFull, v, src, kSeg);
 }
 
-// Parallel continuation of a walk: the t-th (1-based) set bit met when
-// walking from word wi upwards (fwd) or downwards, whole words at a time, 16
-// words per iteration. `active` false takes part for convergence only and
-// returns r unchanged.
-__device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int t, bool fwd, bool active, int r) {
+// Parallel continuation of a walk. Forward: the rem-th (0-based) set bit at
+// or above word wi. Backward: the rem-th (1-based) set bit counting down
+// from the top of word wi. `active` false takes part for convergence only
+// and returns r unchanged.
+__device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int rem, bool fwd, bool active, int r) {
   const int hl = seg_lane();
   bool found = !active;
   for (int guard = 0; guard < 8192; ++guard) {
@@ -267,17 +269,17 @@ __device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int t, boo
     const unsigned int pc = __popc(word);
     const unsigned int incl = seg_scan(pc);
     const int total = (int)seg_bcast(incl, kSeg - 1);
-    const unsigned int ball = seg_ballot((int)incl >= t);
+    const unsigned int ball = seg_ballot(fwd ? (int)incl > rem : (int)incl >= rem);
     const int L = ball ? __ffs(ball) - 1 : 0;
     const unsigned int w = seg_bcast(word, L);
     const int excl = (int)seg_bcast(incl - pc, L);
     if (!found) {
       if (ball) {
-        const int within = t - excl;  // 1-based, in walking order
-        r = ((fwd ? wi + L : wi - L) << 5) + select_in_word32(w, fwd ? within - 1 : __popc(w) - within);
+        const int within = rem - excl;
+        r = ((fwd ? wi + L : wi - L) << 5) + select_in_word32(w, fwd ? within : __popc(w) - within);
         found = true;
       } else {
-        t -= total;
+        rem -= total;
         wi = fwd ? wi + kSeg : wi - kSeg;
         if (wi < 0 || wi >= h.nwords) found = true;  // no such bit: leave r
       }
@@ -286,45 +288,54 @@ __device__ __noinline__ int seg_scan_select(const SegHist& h, int wi, int t, boo
   return r;
 }
 
-// Rank of the t-th (1-based) set bit met when walking from rank `from`
-// upwards (fwd: ranks >= from) or downwards (ranks < from). Both directions
-// run the same instructions, so the two segments of a warp never take
-// different paths; a walk longer than kSeqWords words continues in parallel.
-__device__ __forceinline__ int seg_walk(const SegHist& h, int from, int t, bool fwd, bool active) {
-  int r = 0, wi = 0;
-  bool done = !active;
-  if (active) {
-    wi = from >> 5;
-    const int bit = from & 31;
-    const int dir = fwd ? 1 : -1;
-    unsigned int w = wi < h.nwords ? h.words[wi] : 0u;
-    w &= fwd ? (~0u << bit) : ((1u << bit) - 1u);
-    int pc = __popc(w);
-#pragma unroll 1
-    for (int s = 0; t > pc && s < kSeqWords; ++s) {
-      t -= pc;
-      wi += dir;
-      w = (wi >= 0 && wi < h.nwords) ? h.words[wi] : 0u;
-      pc = __popc(w);
-    }
-    if (t <= pc) {
-      r = (wi << 5) + select_in_word32(w, fwd ? t - 1 : pc - t);
-      done = true;
-    } else {
-      t -= pc;
-      wi += dir;
-    }
-  }
-  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, t, fwd, !done, r);
-  return r;
-}
-
 // Rank of the k-th (0-based) retained sample of the segment's window; the
 // tracked rank moves to it. `active` false leaves the state untouched.
 __device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
-  const int d = k - h.lt;
-  const bool fwd = d >= 0;
-  const int r = seg_walk(h, h.m, fwd ? d + 1 : -d, fwd, active);
+  int r = 0, wi = 0, rem = 0;
+  bool fwd = true, done = !active;
+  if (active) {
+    int d = k - h.lt;
+    wi = h.m >> 5;
+    const int bit = h.m & 31;
+    if (d >= 0) {
+      unsigned int w = h.words[wi] & (~0u << bit);
+      int pc = __popc(w);
+#pragma unroll 1
+      for (int s = 0; d >= pc && s < kSeqWords; ++s) {
+        d -= pc;
+        ++wi;
+        w = wi < h.nwords ? h.words[wi] : 0u;
+        pc = __popc(w);
+      }
+      if (d < pc) {
+        r = (wi << 5) + select_in_word32(w, d);
+        done = true;
+      } else {
+        rem = d - pc;
+        ++wi;
+      }
+    } else {
+      int e = -d;
+      unsigned int w = h.words[wi] & ((1u << bit) - 1u);
+      int pc = __popc(w);
+#pragma unroll 1
+      for (int s = 0; e > pc && s < kSeqWords; ++s) {
+        e -= pc;
+        --wi;
+        w = wi >= 0 ? h.words[wi] : 0u;
+        pc = __popc(w);
+      }
+      if (e <= pc) {
+        r = (wi << 5) + select_in_word32(w, pc - e);
+        done = true;
+      } else {
+        rem = e - pc;
+        --wi;
+        fwd = false;
+      }
+    }
+  }
+  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, rem, fwd, !done, r);
   if (active) {
     h.m = r;
     h.lt = k;
@@ -334,7 +345,25 @@ __device__ __forceinline__ int seg_select(SegHist& h, int k, bool active) {
 
 // Rank of the first retained sample above `rank` (the next order statistic).
 __device__ __forceinline__ int seg_next(const SegHist& h, int rank, bool active) {
-  return seg_walk(h, rank + 1, 1, true, active);
+  int r = rank, wi = 0;
+  bool done = !active;
+  if (active) {
+    wi = rank >> 5;
+    unsigned int w = h.words[wi] & ~((2u << (rank & 31)) - 1u);
+#pragma unroll 1
+    for (int s = 0; w == 0u && s < kSeqWords; ++s) {
+      ++wi;
+      w = wi < h.nwords ? h.words[wi] : 0u;
+    }
+    if (w) {
+      r = (wi << 5) + __ffs(w) - 1;
+      done = true;
+    } else {
+      ++wi;
+    }
+  }
+  if (__any_sync(kFull, !done)) r = seg_scan_select(h, wi, 0, true, !done, r);
+  return r;
 }
 
 // Per-step bookkeeping of a lane: retained, below-m and propagated-NaN
@@ -371,42 +400,17 @@ __device__ __forceinline__ void finish_update(SegHist& h, const StepDelta& d, bo
 }
 
 // Remove the codes of one face and add those of another (n codes each,
-// `stride` apart, in shared memory; STRIDE > 0 fixes the stride at compile
-// time). Each lane takes every 16th pair of the first 16 * (n / 16); the
-// n % 16 left over pairs are spread one code per lane (lanes [0, r) remove,
-// [r, 2r) add) when they fit, so a 65-wide face costs four full iterations
-// and one single-code step instead of five pair iterations.
-template <bool PROPAGATE, int STRIDE>
+// `stride` apart, in shared memory).
+template <bool PROPAGATE>
 __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, int add_start, int n,
-                                     int stride_rt, SegHist& h) {
-  const int stride = STRIDE > 0 ? STRIDE : stride_rt;
+                                     int stride, SegHist& h) {
   const int hl = seg_lane();
   StepDelta d;
-  const int full = n / kSeg, rem = n - full * kSeg;
-  const uint16_t* rp = codes + remove_start + hl * stride;
-  const uint16_t* ap = codes + add_start + hl * stride;
-  const int jump = kSeg * stride;
-  for (int it = 0; it < full; ++it) {
-    update<PROPAGATE>(h, *rp, -1, d);
-    update<PROPAGATE>(h, *ap, +1, d);
-    rp += jump;
-    ap += jump;
-  }
-  if (rem) {
-    if (2 * rem <= kSeg) {
-      int c = kOmitted, sign = 0;
-      if (hl < rem) {
-        c = codes[remove_start + (full * kSeg + hl) * stride];
-        sign = -1;
-      } else if (hl < 2 * rem) {
-        c = codes[add_start + (full * kSeg + hl - rem) * stride];
-        sign = +1;
-      }
-      update<PROPAGATE>(h, c, sign, d);
-    } else if (hl < rem) {
-      update<PROPAGATE>(h, *rp, -1, d);
-      update<PROPAGATE>(h, *ap, +1, d);
-    }
+  for (int i = hl; i < n; i += kSeg) {
+    const int rc = codes[remove_start + i * stride];
+    const int ac = codes[add_start + i * stride];
+    update<PROPAGATE>(h, rc, -1, d);
+    update<PROPAGATE>(h, ac, +1, d);
   }
   finish_update<PROPAGATE>(h, d, n <= 8 * 1024);
 }
@@ -613,13 +617,13 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
           if (FP)
             step_lists<PROPAGATE>(codes, o, top, o + SW, bottom, a.nv, h);
           else
-            step<PROPAGATE, 1>(codes, o, o + kh * SW, kw, 1, h);
+            step<PROPAGATE>(codes, o, o + kh * SW, kw, 1, h);
           ++row;
         } else {
           if (FP)
             step_lists<PROPAGATE>(codes, o, bottom, o - SW, top, a.nv, h);
           else
-            step<PROPAGATE, 1>(codes, o + (kh - 1) * SW, o - SW, kw, 1, h);
+            step<PROPAGATE>(codes, o + (kh - 1) * SW, o - SW, kw, 1, h);
           --row;
         }
       }
@@ -629,7 +633,7 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
       if (FP)
         step_lists<PROPAGATE>(codes, o, left, o + 1, right, a.nh, h);
       else
-        step<PROPAGATE, 0>(codes, o, o + kw, kh, SW, h);
+        step<PROPAGATE>(codes, o, o + kw, kh, SW, h);
     }
     dir = -dir;
   }
@@ -637,13 +641,15 @@ __device__ __forceinline__ void walk(const uint16_t* codes, const uint16_t* list
   pipe.complete(a, out);
 }
 
+// One output tile (index `tile` of the plan's tile list) of the sliding
+// rank-histogram filter: gather the support, rank it, slide. `scratch_slot`
+// is the calling block's sort slot; `smem` the dynamic shared memory, whose
+// footprint-list region the caller has filled for FP windows.
 template <typename T, bool SDEC, bool FP>
-__global__ void __launch_bounds__(kHThreads, 1)
-    histogram_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ HistArgs a,
-                     unsigned char* scratch) {
+__device__ __forceinline__ void histogram_tile(const T* __restrict__ in, T* __restrict__ out, const HistArgs& a,
+                                               long long tile, unsigned char* scratch_slot, unsigned char* smem) {
   using K = typename KeyOf<T>::K;
   const K kSent = KeyOf<T>::kSentinel;
-  extern __shared__ __align__(16) unsigned char smem[];
   __shared__ K red_and[kHWarps], red_or[kHWarps];
   __shared__ int red_sent[kHWarps];
   const Geom3& g = a.g;
@@ -661,117 +667,182 @@ __global__ void __launch_bounds__(kHThreads, 1)
   unsigned int* table = work;
   unsigned int* totals = work + kHWarps * nd;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (FP) {
-    // Made visible by the first barrier of the tile loop.
-    const int n = a.nf + 2 * a.nv + 2 * a.nh;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) lists_s[i] = a.lists[i];
-  }
-  Slot<K> slot = slot_at<K>(scratch + (long long)blockIdx.x * a.slot_bytes, S);
+  Slot<K> slot = slot_at<K>(scratch_slot, S);
   const bool drop_inf = a.r.drop_inf;
   const K outside = sample_key<T>((T)a.r.cval, drop_inf);
+  const long long z = tile / a.tiles_yx;
+  const long long tyx = tile - z * a.tiles_yx;
+  const long long y0 = (tyx / a.tiles_x) * a.TH;
+  const long long x0 = (tyx % a.tiles_x) * a.TW;
+  // Gather the support as keys (payload = support index), mapping each
+  // coordinate through the boundary modes.
+  K k_and = kSent, k_or = 0;
+  int sent = 0;
+  for (int e = threadIdx.x; e < S; e += blockDim.x) {
+    const int sz = e / a.plane;
+    const int ep = e - sz * a.plane;
+    const int sy = ep / a.SW;
+    const int sx = ep - sy * a.SW;
+    long long mz, my, mx;
+    const bool inside = map_index(z + sz - g.az, g.D, g.mz, &mz) &&
+                        map_index(y0 + sy - g.ay, g.H, g.my, &my) &&
+                        map_index(x0 + sx - g.ax, g.W, g.mx, &mx);
+    const K key = inside ? sample_key<T>(__ldg(in + (mz * g.H + my) * g.W + mx), drop_inf) : outside;
+    slot.keys_a[e] = key;
+    slot.pay_a[e] = (uint16_t)e;
+    if (key != kSent) {
+      k_and &= key;
+      k_or |= key;
+    } else {
+      ++sent;
+    }
+  }
+  for (int o = 16; o >= 1; o >>= 1) {
+    k_and &= __shfl_xor_sync(0xffffffffu, k_and, o);
+    k_or |= __shfl_xor_sync(0xffffffffu, k_or, o);
+    sent += __shfl_xor_sync(0xffffffffu, sent, o);
+  }
+  if (lane == 0) {
+    red_and[warp] = k_and;
+    red_or[warp] = k_or;
+    red_sent[warp] = sent;
+  }
+  __syncthreads();
+  k_and = kSent;
+  k_or = 0;
+  sent = 0;
+  for (int w = 0; w < kHWarps; ++w) {
+    k_and &= red_and[w];
+    k_or |= red_or[w];
+    sent += red_sent[w];
+  }
+  // Sort keys (LSD over the bits on which the retained keys differ). The
+  // dropped samples' all-ones keys take part like any other key: an LSD
+  // sort orders the retained keys among themselves whatever lies between
+  // them, and a dropped sample's position is never set in a histogram.
+  K* src_k = slot.keys_a;
+  K* dst_k = slot.keys_b;
+  uint16_t* src_p = slot.pay_a;
+  uint16_t* dst_p = slot.pay_b;
+  const K varying = sent == S ? K(0) : (k_and ^ k_or);
+  if (varying != 0) {
+    const int bits = (int)sizeof(K) * 8;
+    const int lo = sizeof(K) == 8 ? __ffsll((long long)varying) - 1 : __ffs((int)varying) - 1;
+    const int hi = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)varying) : __clz((int)varying));
+    const K mask = (K)(nd - 1);
+    for (int shift = lo; shift <= hi; shift += a.digit_bits) {
+      radix_pass(src_k, src_p, dst_k, dst_p, S, table, totals, nd,
+                 [shift, mask](K key) { return (unsigned int)((key >> shift) & mask); });
+      K* tk = src_k;
+      src_k = dst_k;
+      dst_k = tk;
+      uint16_t* tp = src_p;
+      src_p = dst_p;
+      dst_p = tp;
+    }
+  }
+  const uint16_t dropped = a.r.omit ? kOmitted : kPropagated;
+  for (int pos = threadIdx.x; pos < S; pos += blockDim.x) {
+    const K key = src_k[pos];
+    codes_s[src_p[pos]] = key == kSent ? dropped : (uint16_t)pos;
+    if (SDEC) decode_s[pos] = key;
+  }
+  __syncthreads();
+  const K* sorted = SDEC ? decode_s : src_k;
 
-  for (long long tile = blockIdx.x; tile < a.tiles; tile += gridDim.x) {
-    const long long y0 = (tile / a.tiles_x) * a.TH;
-    const long long x0 = (tile % a.tiles_x) * a.TW;
-    // Gather the support as keys (payload = support index), mapping each
-    // coordinate through the boundary modes.
-    K k_and = kSent, k_or = 0;
-    int sent = 0;
-    for (int e = threadIdx.x; e < S; e += blockDim.x) {
-      const int sy = e / a.SW;
-      const int sx = e - sy * a.SW;
-      long long my, mx;
-      const bool inside = map_index(y0 + sy - g.ay, g.H, g.my, &my) &&
-                          map_index(x0 + sx - g.ax, g.W, g.mx, &mx);
-      const K key = inside ? sample_key<T>(__ldg(in + my * g.W + mx), drop_inf) : outside;
-      slot.keys_a[e] = key;
-      slot.pay_a[e] = (uint16_t)e;
-      if (key != kSent) {
-        k_and &= key;
-        k_or |= key;
-      } else {
-        ++sent;
-      }
-    }
-    for (int o = 16; o >= 1; o >>= 1) {
-      k_and &= __shfl_xor_sync(0xffffffffu, k_and, o);
-      k_or |= __shfl_xor_sync(0xffffffffu, k_or, o);
-      sent += __shfl_xor_sync(0xffffffffu, sent, o);
-    }
-    if (lane == 0) {
-      red_and[warp] = k_and;
-      red_or[warp] = k_or;
-      red_sent[warp] = sent;
-    }
-    __syncthreads();
-    k_and = kSent;
-    k_or = 0;
-    sent = 0;
-    for (int w = 0; w < kHWarps; ++w) {
-      k_and &= red_and[w];
-      k_or |= red_or[w];
-      sent += red_sent[w];
-    }
-    // Sort keys (LSD over the bits on which the retained keys differ). The
-    // dropped samples' all-ones keys take part like any other key: an LSD
-    // sort orders the retained keys among themselves whatever lies between
-    // them, and a dropped sample's position is never set in a histogram.
-    K* src_k = slot.keys_a;
-    K* dst_k = slot.keys_b;
-    uint16_t* src_p = slot.pay_a;
-    uint16_t* dst_p = slot.pay_b;
-    const K varying = sent == S ? K(0) : (k_and ^ k_or);
-    if (varying != 0) {
-      const int bits = (int)sizeof(K) * 8;
-      const int lo = sizeof(K) == 8 ? __ffsll((long long)varying) - 1 : __ffs((int)varying) - 1;
-      const int hi = bits - 1 - (sizeof(K) == 8 ? __clzll((long long)varying) : __clz((int)varying));
-      const K mask = (K)(nd - 1);
-      for (int shift = lo; shift <= hi; shift += a.digit_bits) {
-        radix_pass(src_k, src_p, dst_k, dst_p, S, table, totals, nd,
-                   [shift, mask](K key) { return (unsigned int)((key >> shift) & mask); });
-        K* tk = src_k;
-        src_k = dst_k;
-        dst_k = tk;
-        uint16_t* tp = src_p;
-        src_p = dst_p;
-        dst_p = tp;
-      }
-    }
-    const uint16_t dropped = a.r.omit ? kOmitted : kPropagated;
-    for (int pos = threadIdx.x; pos < S; pos += blockDim.x) {
-      const K key = src_k[pos];
-      codes_s[src_p[pos]] = key == kSent ? dropped : (uint16_t)pos;
-      if (SDEC) decode_s[pos] = key;
-    }
-    __syncthreads();
-    const K* sorted = SDEC ? decode_s : src_k;
+  // Slide: each half-warp walks its columns in boustrophedon order.
+  const int th_eff = (int)min((long long)a.TH, g.H - y0);
+  const int tw_eff = (int)min((long long)a.TW, g.W - x0);
+  const int seg = threadIdx.x / kSeg;
+  SegHist h;
+  h.words = work + seg * a.words;
+  h.nwords = a.words;
+  h.m = 0;
+  h.lt = 0;
+  h.count = 0;
+  h.nan = 0;
+  for (int i = seg_lane(); i < a.words; i += kSeg) h.words[i] = 0u;
+  __syncwarp();
+  const int kh = g.kh, kw = g.kw, SW = a.SW;
+  // Both halves of a warp have columns iff the warp's first column is in
+  // the tile's valid width; whole warps beyond it sit out.
+  const int warp_first = (threadIdx.x / 32) * 2 * a.cols_per_warp;
+  T* plane_out = out + z * g.H * g.W;
+  if (warp_first < tw_eff) {
+    if (!a.r.omit)
+      walk<T, true, FP>(codes_s, lists_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh,
+                        kw, SW, y0, x0, g, a, sorted, plane_out, h);
+    else
+      walk<T, false, FP>(codes_s, lists_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh,
+                         kw, SW, y0, x0, g, a, sorted, plane_out, h);
+  }
+  __syncthreads();
+}
 
-    // Slide: each half-warp walks its columns in boustrophedon order.
-    const int th_eff = (int)min((long long)a.TH, g.H - y0);
-    const int tw_eff = (int)min((long long)a.TW, g.W - x0);
-    const int seg = threadIdx.x / kSeg;
-    SegHist h;
-    h.words = work + seg * a.words;
-    h.nwords = a.words;
-    h.m = 0;
-    h.lt = 0;
-    h.count = 0;
-    h.nan = 0;
-    for (int i = seg_lane(); i < a.words; i += kSeg) h.words[i] = 0u;
-    __syncwarp();
-    const int kh = g.kh, kw = g.kw, SW = a.SW;
-    // Both halves of a warp have columns iff the warp's first column is in
-    // the tile's valid width; whole warps beyond it sit out.
-    const int warp_first = (threadIdx.x / 32) * 2 * a.cols_per_warp;
-    if (warp_first < tw_eff) {
-      if (!a.r.omit)
-        walk<T, true, FP>(codes_s, lists_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh,
-                          kw, SW, y0, x0, g, a, sorted, out, h);
-      else
-        walk<T, false, FP>(codes_s, lists_s, seg * a.cols_per_warp, a.cols_per_warp, tw_eff, th_eff, kh,
-                           kw, SW, y0, x0, g, a, sorted, out, h);
+// Copy a footprint window's run lists into their shared-memory region (made
+// visible by the first barrier of the next tile).
+__device__ __forceinline__ void load_lists(const HistArgs& a, unsigned char* smem) {
+  uint16_t* lists_s = reinterpret_cast<uint16_t*>(smem + align16((long long)a.S * 2));
+  const int n = a.nf + 2 * a.nv + 2 * a.nh;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) lists_s[i] = a.lists[i];
+}
+
+template <typename T, bool SDEC, bool FP>
+__global__ void __launch_bounds__(kHThreads, 1)
+    histogram_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ HistArgs a,
+                     unsigned char* scratch) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (FP) load_lists(a, smem);
+  unsigned char* slot = scratch + (long long)blockIdx.x * a.slot_bytes;
+  for (long long tile = blockIdx.x; tile < a.tiles; tile += gridDim.x)
+    histogram_tile<T, SDEC, FP>(in, out, a, tile, slot, smem);
+}
+
+// Batched images (float32): one persistent launch walks the concatenated
+// tile lists of every image of a family (same SDEC / FP variant); a block
+// finds a tile's image by binary search over the images' first tiles and
+// keeps that image's arguments in shared memory until the image changes.
+struct HistTask {
+  const float* in;
+  float* out;
+  long long first_tile;
+  HistArgs a;
+};
+
+template <bool SDEC, bool FP>
+__global__ void __launch_bounds__(kHThreads, 1)
+    histogram_family_kernel(const HistTask* __restrict__ tasks, int ntasks, long long total_tiles,
+                            unsigned char* scratch, long long slot_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ HistTask task;
+  __shared__ int current, found;
+  if (threadIdx.x == 0) current = -1;
+  __syncthreads();
+  unsigned char* slot = scratch + (long long)blockIdx.x * slot_bytes;
+  for (long long tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = ntasks - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].first_tile <= tile)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      found = lo;
     }
     __syncthreads();
+    const int index = found;
+    if (index != current) {
+      const long long* src = reinterpret_cast<const long long*>(tasks + index);
+      long long* dst = reinterpret_cast<long long*>(&task);
+      for (int i = threadIdx.x; i < (int)(sizeof(HistTask) / 8); i += blockDim.x) dst[i] = src[i];
+      __syncthreads();
+      if (FP) load_lists(task.a, smem);
+      if (threadIdx.x == 0) current = index;
+    }
+    __syncthreads();
+    histogram_tile<float, SDEC, FP>(task.in, task.out, task.a, tile - task.first_tile, slot, smem);
   }
 }
 
@@ -809,18 +880,20 @@ size_t smem_bytes_for(int S, bool sdec, size_t key_bytes, int list_entries) {
   return codes + lists + decode + work_bytes_for(S);
 }
 
-// Count the taps and the vertical and horizontal runs of a kh x kw
-// footprint mask (row-major).
-Runs count_runs(const std::vector<uint8_t>& mask, int kh, int kw) {
+// Count the taps and the vertical and horizontal runs (within each plane)
+// of a kd x kh x kw footprint mask (row-major).
+Runs count_runs(const std::vector<uint8_t>& mask, int kd, int kh, int kw) {
   Runs r;
   r.footprint = true;
-  for (int y = 0; y < kh; ++y)
-    for (int x = 0; x < kw; ++x) {
-      if (!mask[(size_t)y * kw + x]) continue;
-      ++r.nf;
-      if (y == 0 || !mask[(size_t)(y - 1) * kw + x]) ++r.nv;
-      if (x == 0 || !mask[(size_t)y * kw + x - 1]) ++r.nh;
-    }
+  for (int zz = 0; zz < kd; ++zz)
+    for (int y = 0; y < kh; ++y)
+      for (int x = 0; x < kw; ++x) {
+        const size_t at = ((size_t)zz * kh + y) * kw + x;
+        if (!mask[at]) continue;
+        ++r.nf;
+        if (y == 0 || !mask[at - kw]) ++r.nv;
+        if (x == 0 || !mask[at - 1]) ++r.nh;
+      }
   return r;
 }
 
@@ -830,11 +903,14 @@ Runs count_runs(const std::vector<uint8_t>& mask, int kh, int kw) {
 // global decode when the sorted keys do not fit in shared memory.
 HistChoice choose_tile(const Geom3& g, size_t key_bytes, const Runs& runs = Runs{}) {
   HistChoice best;
-  if (g.kd != 1 || g.D != 1) return best;
-  if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport) return best;
+  if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport || (long long)g.kd > kMaxSupport)
+    return best;
+  // Windows deeper than one plane walk their (kd-plane) faces through the
+  // run lists.
+  if (g.kd > 1 && !runs.footprint) return best;
   double best_cost = 1e300;
   auto consider = [&](int tw, int th) {
-    long long S = (long long)(tw + g.kw - 1) * (th + g.kh - 1);
+    long long S = (long long)g.kd * (tw + g.kw - 1) * (th + g.kh - 1);
     if (S > kMaxSupport) return;
     for (int sdec = 1; sdec >= 0; --sdec) {
       size_t smem = smem_bytes_for((int)S, sdec != 0, key_bytes, runs.entries());
@@ -879,9 +955,11 @@ HistArgs make_args_core(const Geom3& g, int TW, int TH, int dtype, const Reduce&
   a.TH = TH;
   a.SW = a.TW + a.g.kw - 1;
   a.SH = a.TH + a.g.kh - 1;
-  a.S = a.SW * a.SH;
+  a.plane = a.SW * a.SH;
+  a.S = a.g.kd * a.plane;
   a.tiles_x = (a.g.W + a.TW - 1) / a.TW;
-  a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
+  a.tiles_yx = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
+  a.tiles = a.tiles_yx * a.g.D;
   a.cols_per_warp = (a.TW + kSegs - 1) / kSegs;  // columns per half-warp segment
   a.words = (a.S + 31) / 32;
   a.slot_bytes = dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
@@ -901,9 +979,11 @@ HistArgs make_args(const Plan& p) {
   a.TH = p.hist_block_h;
   a.SW = a.TW + a.g.kw - 1;
   a.SH = a.TH + a.g.kh - 1;
-  a.S = a.SW * a.SH;
+  a.plane = a.SW * a.SH;
+  a.S = a.g.kd * a.plane;
   a.tiles_x = (a.g.W + a.TW - 1) / a.TW;
-  a.tiles = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
+  a.tiles_yx = a.tiles_x * ((a.g.H + a.TH - 1) / a.TH);
+  a.tiles = a.tiles_yx * a.g.D;
   a.cols_per_warp = (a.TW + kSegs - 1) / kSegs;  // columns per half-warp segment
   a.words = (a.S + 31) / 32;
   a.slot_bytes = p.dtype == 0 ? slot_bytes_for<uint32_t>(a.S) : slot_bytes_for<unsigned long long>(a.S);
@@ -955,27 +1035,31 @@ cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
 
 namespace {
 
-// The footprint of a 1-D/2-D plan as a kh x kw mask in the tile's (y, x)
-// orientation, from the taps' box positions.
+// The footprint of a plan as a kd x kh x kw mask in the tile's (z, y, x)
+// orientation, from the taps' box positions (all ones for a box).
 std::vector<uint8_t> footprint_mask(const Plan& p) {
   const Geom3& g = p.tile.g;
-  std::vector<uint8_t> mask((size_t)g.kh * g.kw, 0);
+  std::vector<uint8_t> mask((size_t)g.kd * g.kh * g.kw, 0);
   for (int i = 0; i < p.r.count; ++i) {
     const int* bt = &p.box_taps[(size_t)i * 3];
-    mask[(size_t)bt[1] * g.kw + bt[2]] = 1;
+    mask[((size_t)bt[0] * g.kh + bt[1]) * g.kw + bt[2]] = 1;
   }
   return mask;
 }
 
+// Run lists for footprint windows and for every window deeper than one
+// plane (a 3-D box is walked as a footprint); none for 1-D/2-D boxes.
 Runs runs_of(const Plan& p) {
-  if (p.footprint.empty()) return Runs{};
-  return count_runs(footprint_mask(p), p.tile.g.kh, p.tile.g.kw);
+  const Geom3& g = p.tile.g;
+  if (p.footprint.empty() && g.kd == 1) return Runs{};
+  if ((long long)g.kd * g.kh * g.kw > (1ll << 24)) return Runs{};  // too large to list
+  return count_runs(footprint_mask(p), g.kd, g.kh, g.kw);
 }
 
 }  // namespace
 
 bool histogram_supported(const Plan& p) {
-  if (p.ndim > 2 || p.r.count < 1) return false;
+  if (p.ndim > 3 || p.r.count < 1) return false;
   const int k = p.r.kind;
   if (k != kMedian && k != kMedianNetwork && k != kMedianHistogram && k != kRank &&
       k != kRankHistogram && k != kMin && k != kMax && k != kPercentile)
@@ -995,25 +1079,28 @@ void histogram_configure(Plan& p) {
   p.hist_nv = runs.nv;
   p.hist_nh = runs.nh;
   p.hist_lists.clear();
-  if (runs.footprint) {
-    // Support-linear offsets (y * SW + x) of the taps and of the run ends.
+  if (runs.footprint && c.TW > 0) {
+    // Support-linear offsets (zz * plane + y * SW + x) of the taps and of
+    // the run ends; below the support size, so they fit 16 bits.
     const Geom3& g = p.tile.g;
     const int SW = c.TW + g.kw - 1;
+    const int plane = SW * (c.TH + g.kh - 1);
     const std::vector<uint8_t> mask = footprint_mask(p);
-    auto at = [&](int y, int x) {
-      return y >= 0 && y < g.kh && x >= 0 && x < g.kw && mask[(size_t)y * g.kw + x] != 0;
+    auto at = [&](int zz, int y, int x) {
+      return y >= 0 && y < g.kh && x >= 0 && x < g.kw && mask[((size_t)zz * g.kh + y) * g.kw + x] != 0;
     };
     std::vector<uint16_t> taps, top, bottom, left, right;
-    for (int y = 0; y < g.kh; ++y)
-      for (int x = 0; x < g.kw; ++x) {
-        if (!at(y, x)) continue;
-        const uint16_t off = (uint16_t)(y * SW + x);
-        taps.push_back(off);
-        if (!at(y - 1, x)) top.push_back(off);
-        if (!at(y + 1, x)) bottom.push_back(off);
-        if (!at(y, x - 1)) left.push_back(off);
-        if (!at(y, x + 1)) right.push_back(off);
-      }
+    for (int zz = 0; zz < g.kd; ++zz)
+      for (int y = 0; y < g.kh; ++y)
+        for (int x = 0; x < g.kw; ++x) {
+          if (!at(zz, y, x)) continue;
+          const uint16_t off = (uint16_t)(zz * plane + y * SW + x);
+          taps.push_back(off);
+          if (!at(zz, y - 1, x)) top.push_back(off);
+          if (!at(zz, y + 1, x)) bottom.push_back(off);
+          if (!at(zz, y, x - 1)) left.push_back(off);
+          if (!at(zz, y, x + 1)) right.push_back(off);
+        }
     // A step removes one list and adds the other; the pairing of entries
     // does not matter, only that both lists of an axis have one entry per run.
     p.hist_lists = taps;
@@ -1053,6 +1140,49 @@ cudaError_t histogram_allocate(Plan& p) {
   long long slots = std::min<long long>(a.tiles, (long long)std::max(per_sm, 1) * p.sm_count);
   p.scratch_bytes = (size_t)slots * (size_t)a.slot_bytes;
   return cudaMalloc(&p.d_scratch, p.scratch_bytes);
+}
+
+namespace {
+
+int hist_family_variant(const Plan& p) {
+  if (p.algo != Algo::kHistogram || p.dtype != 0) return -1;
+  return (p.hist_sdec ? 1 : 0) + (p.hist_footprint ? 2 : 0);
+}
+
+long long hist_family_tiles(const Plan& p) { return make_args(p).tiles; }
+
+long long hist_family_slot_bytes(const Plan& p) { return make_args(p).slot_bytes; }
+
+void hist_family_write_task(const Plan& p, const void* in, void* out, long long first_tile, void* task) {
+  HistTask t{};
+  t.in = (const float*)in;
+  t.out = (float*)out;
+  t.first_tile = first_tile;
+  t.a = make_args(p);
+  std::memcpy(task, &t, sizeof(t));
+}
+
+const void* hist_family_kernel(int v) {
+  switch (v) {
+    case 0: return (const void*)histogram_family_kernel<false, false>;
+    case 1: return (const void*)histogram_family_kernel<true, false>;
+    case 2: return (const void*)histogram_family_kernel<false, true>;
+    default: return (const void*)histogram_family_kernel<true, true>;
+  }
+}
+
+cudaError_t hist_family_launch(int v, const void* d_tasks, int ntasks, long long tiles, unsigned char* scratch,
+                               long long slot_bytes, size_t smem, int grid, cudaStream_t s) {
+  void* args[] = {(void*)&d_tasks, &ntasks, &tiles, &scratch, &slot_bytes};
+  return cudaLaunchKernel(hist_family_kernel(v), dim3(grid), dim3(kHThreads), args, smem, s);
+}
+
+}  // namespace
+
+const FamilyOps& histogram_family_ops() {
+  static const FamilyOps ops{sizeof(HistTask), hist_family_variant, hist_family_tiles, hist_family_slot_bytes,
+                             hist_family_write_task, hist_family_kernel, hist_family_launch};
+  return ops;
 }
 
 cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStream_t s) {

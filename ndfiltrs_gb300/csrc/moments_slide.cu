@@ -21,6 +21,7 @@
 //    widths compute their outputs with the reference's float64 arithmetic.
 #include <algorithm>
 #include <climits>
+#include <cstring>
 
 #include "exact.cuh"
 #include "fixed_moments.cuh"
@@ -41,11 +42,12 @@ struct SlideArgs {
   int count_bits;  // bit length of (window volume + 1)
 };
 
+// One output tile (index `tile`) of the sliding moments kernel; `tmap` is
+// the launch's tensor map (nullptr: remapped staging only).
 template <typename T>
-__global__ void __launch_bounds__(kSThreads)
-    moments_slide_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
-                         const __grid_constant__ SlideArgs sa, const __grid_constant__ CUtensorMap tmap) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* __restrict__ out,
+                                                   const TileArgs& a, const SlideArgs& sa, long long tile,
+                                                   unsigned char* smem_raw, const CUtensorMap* tmap) {
   constexpr int E0 = sizeof(T) == 4 ? -149 : -1074;
   const Geom3& g = a.g;
   const Tile& t = a.t;
@@ -61,8 +63,8 @@ __global__ void __launch_bounds__(kSThreads)
   u128* h2 = reinterpret_cast<u128*>(h1 + (size_t)t.SH * t.TW);
   unsigned long long* hc = reinterpret_cast<unsigned long long*>(h2 + (size_t)t.SH * t.TW);
   long long z, y0, x0;
-  net::tile_coords(a, blockIdx.x, z, y0, x0);
-  if (!stage_tile(s, maps, smem_raw, in, a, &tmap, z, y0, x0, (T)r.cval, [](T v) { return v; })) return;
+  net::tile_coords(a, tile, z, y0, x0);
+  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, (T)r.cval, [](T v) { return v; })) return;
   __syncthreads();
   const int support = t.SH * t.SW;
   const Span<T> sp = tile_span<T, kSThreads>(s, support);
@@ -161,6 +163,61 @@ __global__ void __launch_bounds__(kSThreads)
 }
 
 template <typename T>
+__global__ void __launch_bounds__(kSThreads)
+    moments_slide_kernel(const T* __restrict__ in, T* __restrict__ out, const __grid_constant__ TileArgs a,
+                         const __grid_constant__ SlideArgs sa, const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  moments_slide_body<T>(in, out, a, sa, blockIdx.x, smem_raw, &tmap);
+}
+
+// Batched float32 images: one persistent launch over the concatenated tile
+// lists; a block finds a tile's image by binary search over the images'
+// first tiles and keeps its arguments in shared memory until the image
+// changes. Staging is the remapped path.
+struct SlideTask {
+  const float* in;
+  float* out;
+  long long first_tile;
+  TileArgs a;
+  SlideArgs sa;
+  int pad;
+};
+
+__global__ void __launch_bounds__(kSThreads)
+    slide_family_kernel(const SlideTask* __restrict__ tasks, int ntasks, long long total_tiles) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ SlideTask task;
+  __shared__ int current, found;
+  if (threadIdx.x == 0) current = -1;
+  __syncthreads();
+  for (long long tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = ntasks - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].first_tile <= tile)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      found = lo;
+    }
+    __syncthreads();
+    const int index = found;
+    if (index != current) {
+      const long long* src = reinterpret_cast<const long long*>(tasks + index);
+      long long* dst = reinterpret_cast<long long*>(&task);
+      for (int i = threadIdx.x; i < (int)(sizeof(SlideTask) / 8); i += blockDim.x) dst[i] = src[i];
+      __syncthreads();
+      if (threadIdx.x == 0) current = index;
+    }
+    __syncthreads();
+    moments_slide_body<float>(task.in, task.out, task.a, task.sa, tile - task.first_tile, smem_raw, nullptr);
+    __syncthreads();
+  }
+}
+
+template <typename T>
 size_t tile_smem(const Tile& t, int kd) {
   const size_t sums_offset = ((size_t)(t.SW + t.SH + kd) * 8 + (size_t)t.SH * t.SW * sizeof(T) + 15) & ~(size_t)15;
   return sums_offset + (size_t)t.SH * t.TW * (16 + 16 + 8);
@@ -228,6 +285,42 @@ bool moments_slide_configure(Plan& p, int smem_limit) {
 cudaError_t launch_moments_slide(const Plan& p, const void* in, void* out, cudaStream_t s) {
   if (p.dtype == 0) return launch_t<float>(p, (const float*)in, (float*)out, s);
   return launch_t<double>(p, (const double*)in, (double*)out, s);
+}
+
+namespace {
+
+int slide_family_variant(const Plan& p) { return p.algo == Algo::kMomentsSlide && p.dtype == 0 ? 0 : -1; }
+
+long long slide_family_tiles(const Plan& p) { return p.tile.t.tiles; }
+
+long long slide_family_slot_bytes(const Plan&) { return 0; }
+
+void slide_family_write_task(const Plan& p, const void* in, void* out, long long first_tile, void* task) {
+  SlideTask t{};
+  t.in = (const float*)in;
+  t.out = (float*)out;
+  t.first_tile = first_tile;
+  t.a = p.tile;
+  t.a.r = p.r;
+  t.a.tma_bw = 0;
+  t.sa.count_bits = 64 - __builtin_clzll((unsigned long long)p.r.count + 1);
+  std::memcpy(task, &t, sizeof(t));
+}
+
+const void* slide_family_kernel_of(int) { return (const void*)slide_family_kernel; }
+
+cudaError_t slide_family_launch(int, const void* d_tasks, int ntasks, long long tiles, unsigned char*, long long,
+                                size_t smem, int grid, cudaStream_t s) {
+  void* args[] = {(void*)&d_tasks, &ntasks, &tiles};
+  return cudaLaunchKernel((const void*)slide_family_kernel, dim3(grid), dim3(kSThreads), args, smem, s);
+}
+
+}  // namespace
+
+const FamilyOps& slide_family_ops() {
+  static const FamilyOps ops{sizeof(SlideTask), slide_family_variant, slide_family_tiles, slide_family_slot_bytes,
+                             slide_family_write_task, slide_family_kernel_of, slide_family_launch};
+  return ops;
 }
 
 }  // namespace ndf

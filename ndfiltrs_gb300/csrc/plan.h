@@ -253,4 +253,23 @@ int network_width_for(int dtype, int count);
 bool box_supported(int dtype, int kh, int kw);
 Tile box_tile(const Geom3& g);
 
+// A kernel family of the batched path (float32 images): one persistent
+// launch walks the concatenated tile lists of several images, each described
+// by a task of `task_bytes` (written by write_task with the image's buffers
+// and its first tile in the family's list). `variant` picks the kernel
+// instantiation a plan needs (-1: the plan's kernel is not of this family).
+struct FamilyOps {
+  size_t task_bytes;
+  int (*variant)(const Plan& p);
+  long long (*tiles)(const Plan& p);
+  long long (*slot_bytes)(const Plan& p);  // per-block scratch bytes (0: none)
+  void (*write_task)(const Plan& p, const void* in, void* out, long long first_tile, void* task);
+  const void* (*kernel)(int variant);
+  cudaError_t (*launch)(int variant, const void* d_tasks, int ntasks, long long tiles, unsigned char* scratch,
+                        long long slot_bytes, size_t smem, int grid, cudaStream_t s);
+};
+const FamilyOps& histogram_family_ops();  // sliding histogram (histogram.cu), 4 variants
+const FamilyOps& box_family_ops();        // box pair 3x3 / 5x5 / 7x7 (box.cu), 6 variants
+const FamilyOps& slide_family_ops();      // sliding exact moments (moments_slide.cu), 1 variant
+
 }  // namespace ndf

@@ -151,3 +151,46 @@ def test_batch_with_rolling_means_extrema_and_robust_kinds(gpu) -> None:
         np.testing.assert_array_equal(bits(out.cpu().numpy()), bits(want), err_msg=spec["kind"])
         np.testing.assert_array_equal(bits(host), bits(want), err_msg=spec["kind"])
     batch.close()
+
+
+def test_specialised_kernels_run_as_one_persistent_launch_per_family(gpu) -> None:
+    """Images whose plans take the box-pair kernel, the sliding histogram or
+    the sliding exact moments join one persistent launch per family (kernel
+    and variant) instead of launching per image; results equal per-image
+    plans bit for bit."""
+    import torch
+
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(11)
+    specs, images = [], []
+    families = [("median", (5, 5)), ("median_histogram", (33, 31)), ("std", (9, 9))]
+    for i in range(12):
+        kind, size = families[i % 3]
+        image = rng.normal(1000, 10, size=(int(rng.integers(60, 260)), int(rng.integers(60, 260))))
+        image = image.astype(np.float32)
+        image[rng.random(image.shape) < 0.02] = np.nan
+        specs.append(dict(shape=image.shape, kind=kind, size=size, footprint=None, omit_nan=True,
+                          ignore_inf=kind == "std", min_count=1, parameter=1 if kind == "std" else 0,
+                          percentile=50.0, mode=["reflect", "nearest", "wrap"][i % 3]))
+        images.append(image)
+    expected_algorithms = {"median": "tile_box", "median_histogram": "histogram", "std": "moments_slide"}
+    wants = []
+    for spec, image in zip(specs, images):
+        with _core.Plan(image.shape, np.float32, spec["kind"], spec["size"], mode=[spec["mode"]] * 2,
+                        omit_nan=True, ignore_inf=spec["ignore_inf"], parameter=spec["parameter"]) as plan:
+            assert plan.algorithm == expected_algorithms[spec["kind"]], spec["kind"]
+            wants.append(plan.run_host(image))
+    batch = _core.Batch(specs)
+    d_in = [torch.from_numpy(im).cuda() for im in images]
+    d_out = [torch.full_like(t, 3.0) for t in d_in]
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):
+        batch.run_device([t.data_ptr() for t in d_in], [t.data_ptr() for t in d_out], stream)
+    torch.cuda.synchronize()
+    assert batch.launches == 3
+    for spec, out, want in zip(specs, d_out, wants):
+        np.testing.assert_array_equal(bits(out.cpu().numpy()), bits(want), err_msg=spec["kind"])
+    hosts = batch.run_host(images)
+    for spec, host, want in zip(specs, hosts, wants):
+        np.testing.assert_array_equal(bits(host), bits(want), err_msg=spec["kind"])

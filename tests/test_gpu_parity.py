@@ -422,3 +422,64 @@ def test_separable_extrema(gpu, oracle, dtype, family, algorithm) -> None:
                         _assert_bits(actual, _oracle(oracle, *args), (size, mode, kind, omit, ignore_inf, cval))
     finally:
         _core.pin_kernel(None)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_histogram_3d_windows(gpu, oracle, dtype) -> None:
+    """3-D windows slide the rank histogram over supports of kd planes: boxes
+    (walked through their run lists, as the reference's N-D histogram walks
+    any rank, src/histogram.rs:494-566) and 3-D footprints (with the kernel
+    family pinned), every boundary mode on every axis, shifted origins, both
+    NaN policies, every order statistic; against the oracle bit for bit."""
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(33)
+    values = _special_values((11, 45, 38), dtype, seed=9, fraction=0.08)
+    footprint = rng.random((3, 7, 9)) < 0.7
+    footprint[1, 3, 4] = True
+    boxes = (((3, 5, 4), (0, 1, -1)), ((5, 9, 9), (-2, 0, 4)), ((4, 1, 6), (1, 0, 0)), ((2, 3, 1), (0, 1, 0)))
+    for size, origin in boxes:
+        with _core.Plan(values.shape, dtype, "median_histogram", size, origin=origin, omit_nan=True) as plan:
+            assert plan.algorithm == "histogram", size
+        for mode in MODES:
+            modes = (mode, MODES[(MODES.index(mode) + 1) % 5], MODES[(MODES.index(mode) + 3) % 5])
+            volume = int(np.prod(size))
+            for omit, ignore_inf, min_count in ((False, False, 1), (True, True, max(1, volume // 3))):
+                for kind, parameter in (("median_histogram", 0), ("rank_histogram", volume // 4)):
+                    args = (kind, values, size, None, origin, modes, -1.25, omit, ignore_inf, min_count,
+                            parameter)
+                    base = "median" if kind == "median_histogram" else "rank"
+                    _assert_bits(_gpu(*args), _oracle(oracle, base, *args[1:]), (size, modes, omit, kind))
+    _core.pin_kernel("histogram")
+    try:
+        with _core.Plan(values.shape, dtype, "median", footprint.shape, footprint=footprint,
+                        omit_nan=True) as plan:
+            assert plan.algorithm == "histogram"
+        for mode in MODES:
+            for omit, ignore_inf, min_count in ((False, False, 1), (True, False, 9)):
+                for kind, parameter, q in (("median", 0, 50.0), ("rank", 5, 50.0), ("min", 0, 50.0),
+                                           ("max", 0, 50.0), ("percentile", 0, 16.0)):
+                    args = (kind, values, None, footprint, (1, -2, 3), (mode,) * 3, 0.5, omit, ignore_inf,
+                            min_count, parameter, q)
+                    _assert_bits(_gpu(*args), _oracle(oracle, *args), ("footprint", mode, omit, kind))
+    finally:
+        _core.pin_kernel(None)
+
+
+def test_histogram_3d_large_window(gpu, oracle) -> None:
+    """A (9, 33, 33) window (9,801 taps) on a 12 x 100 x 90 cube: the sliding
+    histogram against the oracle's direct selection, nearest and reflect."""
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(4)
+    cube = (500 + rng.normal(size=(12, 100, 90)) * 20).astype(np.float32)
+    cube[rng.random(cube.shape) < 0.01] = np.nan
+    cube[:, :, 31] = np.nan
+    size = (9, 33, 33)
+    with _core.Plan(cube.shape, np.float32, "median_histogram", size, omit_nan=True) as plan:
+        assert plan.algorithm == "histogram"
+    for mode in ("nearest", "reflect"):
+        for kind, parameter in (("median_histogram", 0), ("rank_histogram", 1234)):
+            args = (kind, cube, size, None, (0, 0, 0), (mode,) * 3, 0.0, True, False, 1, parameter)
+            base = "median" if kind == "median_histogram" else "rank"
+            _assert_bits(_gpu(*args), _oracle(oracle, base, *args[1:]), (mode, kind))
