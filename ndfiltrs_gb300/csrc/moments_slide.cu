@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <type_traits>
 
 #include "exact.cuh"
 #include "fixed_moments.cuh"
@@ -42,53 +43,42 @@ struct SlideArgs {
   int count_bits;  // bit length of (window volume + 1)
 };
 
-// One output tile (index `tile`) of the sliding moments kernel; `tmap` is
-// the launch's tensor map (nullptr: remapped staging only).
-template <typename T>
-__device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* __restrict__ out,
-                                                   const TileArgs& a, const SlideArgs& sa, long long tile,
-                                                   unsigned char* smem_raw, const CUtensorMap* tmap) {
+// The exact sliding sums of one tile and its outputs: horizontal sums of X,
+// X^2 and the sample counts along every support row (8 outputs per work
+// item), then vertical sums down each output column (L rows per thread) and
+// the combine. NARROW keeps S1 and S2 in 64-bit words (the caller has checked
+// that every window's sums fit), otherwise 128-bit words; the row sums live
+// in shared memory at `sums`.
+template <typename T, bool NARROW>
+__device__ __forceinline__ void slide_sums(const T* s, const TileArgs& a, const Span<T>& sp, i128 P,
+                                           const SlideArgs& sa, unsigned char* sums, long long z, long long y0,
+                                           long long x0, T* __restrict__ out) {
+  using S1 = typename std::conditional<NARROW, long long, i128>::type;
+  using S2 = typename std::conditional<NARROW, unsigned long long, u128>::type;
   constexpr int E0 = sizeof(T) == 4 ? -149 : -1074;
   const Geom3& g = a.g;
   const Tile& t = a.t;
   const Reduce& r = a.r;
-  // Layout (offsets from the 16-byte aligned base, each region 16-byte
-  // aligned for the 128-bit sums): remap tables | staged samples | row sums
-  // of X (i128) | row sums of X^2 (u128) | row counts (u64).
-  long long* maps = reinterpret_cast<long long*>(smem_raw);
-  T* s = reinterpret_cast<T*>(maps + (t.SW + t.SH + g.kd));
-  const size_t sums_offset =
-      ((size_t)(t.SW + t.SH + g.kd) * 8 + (size_t)t.SH * t.SW * sizeof(T) + 15) & ~(size_t)15;
-  i128* h1 = reinterpret_cast<i128*>(smem_raw + sums_offset);
-  u128* h2 = reinterpret_cast<u128*>(h1 + (size_t)t.SH * t.TW);
-  unsigned long long* hc = reinterpret_cast<unsigned long long*>(h2 + (size_t)t.SH * t.TW);
-  long long z, y0, x0;
-  net::tile_coords(a, tile, z, y0, x0);
-  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, (T)r.cval, [](T v) { return v; })) return;
-  __syncthreads();
-  const int support = t.SH * t.SW;
-  const Span<T> sp = tile_span<T, kSThreads>(s, support);
-  const T pivot = sp.pivot;
-  const int lo = sp.lo;
-  const bool fits = span_fits(sp, sa.count_bits);
-
   const int kw = g.kw, kh = g.kh, TW = t.TW, SW = t.SW;
   const bool omit = r.omit, drop_inf = r.drop_inf;
-  if (!fits) {
-    // A value range too wide for the integer widths: the reference's float64
-    // arithmetic per window (bit-identical to it) over the staged support.
-    const int tx = threadIdx.x % TW;
-    const int nseg_rows = kSThreads / TW;
-    for (int ty = threadIdx.x / TW; ty < t.TH; ty += nseg_rows) {
-      const long long gy = y0 + ty, gx = x0 + tx;
-      if (gy >= g.H || gx >= g.W) continue;
-      const int base = ty * SW + tx;
-      auto fetch64 = [&](int i) -> double { return (double)s[base + (i / kw) * SW + i % kw]; };
-      out[(z * g.H + gy) * g.W + gx] = canonical(from_f64<T>(mom::moments_exact(fetch64, r)));
+  const int lo = sp.lo;
+  S1* h1 = reinterpret_cast<S1*>(sums);
+  S2* h2 = reinterpret_cast<S2*>(h1 + (size_t)t.SH * t.TW);
+  unsigned long long* hc = reinterpret_cast<unsigned long long*>(h2 + (size_t)t.SH * t.TW);
+  const long long P64 = (long long)P;
+  // X = x - P in units of 2^(E0 + lo); zero for non-finite samples.
+  auto deviation = [&](T v) -> long long {
+    if constexpr (NARROW) {
+      unsigned long long m;
+      int pos;
+      bool neg;
+      if (!decompose(v, m, pos, neg)) return isfinite(v) ? -P64 : 0ll;  // zero, or not finite
+      const long long f = (long long)(m << (pos - lo));
+      return (neg ? -f : f) - P64;
+    } else {
+      return isfinite(v) ? (long long)(fixed(v, lo) - P) : 0ll;
     }
-    return;
-  }
-  const i128 P = fixed(pivot, lo);
+  };
 
   // Horizontal sums of every support row, 8 outputs per work item.
   const int nseg = TW / 8;
@@ -96,12 +86,16 @@ __device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* 
     const int y = item / nseg;
     const int xs = (item - y * nseg) * 8;
     const T* row = s + (size_t)y * SW + xs;
-    i128 s1 = 0;
-    u128 s2 = 0;
+    S1 s1 = 0;
+    S2 s2 = 0;
     unsigned long long cnt = 0;
     auto add = [&](T v, int sign) {
-      const long long X = isfinite(v) ? (long long)(fixed(v, lo) - P) : 0ll;
-      const u128 sq = (u128)((i128)X * X);
+      const long long X = deviation(v);
+      S2 sq;
+      if constexpr (NARROW)
+        sq = (unsigned long long)(X * X);
+      else
+        sq = (u128)((i128)X * X);
       if (sign > 0) {
         s1 += X;
         s2 += sq;
@@ -132,8 +126,8 @@ __device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* 
   const int L = t.TH / nsegs;
   const int r0 = (threadIdx.x / TW) * L;
   const long long gx = x0 + x;
-  i128 s1 = 0;
-  u128 s2 = 0;
+  S1 s1 = 0;
+  S2 s2 = 0;
   unsigned long long cnt = 0;
   for (int k = 0; k < kh; ++k) {
     s1 += h1[(size_t)(r0 + k) * TW + x];
@@ -151,7 +145,8 @@ __device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* 
       if (mom::decide_special(r, (long long)finite + pos + neg, nanc != 0, pos != 0, neg != 0, &result))
         out[(z * g.H + gy) * g.W + gx] = canonical(from_f64<T>(result));
       else
-        out[(z * g.H + gy) * g.W + gx] = canonical(fixed_combine<T>(r.kind, r.param, s1, s2, finite, P, quantum));
+        out[(z * g.H + gy) * g.W + gx] =
+            canonical(fixed_combine<T>(r.kind, r.param, (i128)s1, (u128)s2, finite, P, quantum));
     }
     if (rr + 1 < L) {
       const size_t add = (size_t)(row + kh) * TW + x, sub = (size_t)row * TW + x;
@@ -160,6 +155,59 @@ __device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* 
       cnt += hc[add] - hc[sub];
     }
   }
+}
+
+// One output tile (index `tile`) of the sliding moments kernel; `tmap` is
+// the launch's tensor map (nullptr: remapped staging only).
+template <typename T>
+__device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* __restrict__ out,
+                                                   const TileArgs& a, const SlideArgs& sa, long long tile,
+                                                   unsigned char* smem_raw, const CUtensorMap* tmap) {
+  const Geom3& g = a.g;
+  const Tile& t = a.t;
+  const Reduce& r = a.r;
+  // Layout (offsets from the 16-byte aligned base, each region 16-byte
+  // aligned for the 128-bit sums): remap tables | staged samples | row sums
+  // of X | row sums of X^2 | row counts (u64), the sums 128-bit (wide tiles)
+  // or 64-bit (narrow tiles) each.
+  long long* maps = reinterpret_cast<long long*>(smem_raw);
+  T* s = reinterpret_cast<T*>(maps + (t.SW + t.SH + g.kd));
+  const size_t sums_offset =
+      ((size_t)(t.SW + t.SH + g.kd) * 8 + (size_t)t.SH * t.SW * sizeof(T) + 15) & ~(size_t)15;
+  long long z, y0, x0;
+  net::tile_coords(a, tile, z, y0, x0);
+  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, (T)r.cval, [](T v) { return v; })) return;
+  __syncthreads();
+  const int support = t.SH * t.SW;
+  const Span<T> sp = tile_span<T, kSThreads>(s, support);
+  const T pivot = sp.pivot;
+  const int lo = sp.lo;
+  const bool fits = span_fits(sp, sa.count_bits);
+
+  const int kw = g.kw, TW = t.TW, SW = t.SW;
+  if (!fits) {
+    // A value range too wide for the integer widths: the reference's float64
+    // arithmetic per window (bit-identical to it) over the staged support.
+    const int tx = threadIdx.x % TW;
+    const int nseg_rows = kSThreads / TW;
+    for (int ty = threadIdx.x / TW; ty < t.TH; ty += nseg_rows) {
+      const long long gy = y0 + ty, gx = x0 + tx;
+      if (gy >= g.H || gx >= g.W) continue;
+      const int base = ty * SW + tx;
+      auto fetch64 = [&](int i) -> double { return (double)s[base + (i / kw) * SW + i % kw]; };
+      out[(z * g.H + gy) * g.W + gx] = canonical(from_f64<T>(mom::moments_exact(fetch64, r)));
+    }
+    return;
+  }
+  const i128 P = fixed(pivot, lo);
+  // Narrow tiles (deviations within 31 bits and their window sums within 64
+  // bits, the usual case for float32 data of moderate range) keep every sum
+  // in 64-bit words; wide tiles in 128-bit words. Both are exact.
+  const int bits = deviation_bits(sp);
+  if (sp.top - lo <= 62 && bits <= 31 && 2 * bits + sa.count_bits <= 63)
+    slide_sums<T, true>(s, a, sp, P, sa, smem_raw + sums_offset, z, y0, x0, out);
+  else
+    slide_sums<T, false>(s, a, sp, P, sa, smem_raw + sums_offset, z, y0, x0, out);
 }
 
 template <typename T>
