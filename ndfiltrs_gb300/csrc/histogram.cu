@@ -375,7 +375,10 @@ struct StepDelta {
 template <bool PROPAGATE>
 __device__ __forceinline__ void update(const SegHist& h, int c, int sign, StepDelta& d) {
   const bool valid = c < (int)kPropagated;
-  if (valid) atomicXor(&h.words[c >> 5], 1u << (c & 31));
+  // Unconditional: a dropped code XORs zero into a word of the segment's own
+  // bitset (the lane's, within its bounds), so the update has no branch (and
+  // no reconvergence) around its atomic.
+  atomicXor(&h.words[valid ? (c >> 5) : min(seg_lane(), h.nwords - 1)], valid ? 1u << (c & 31) : 0u);
   d.kept += valid ? sign : 0;
   d.below += c < h.m ? sign : 0;  // codes below m are retained (dropped codes are the largest)
   if (PROPAGATE) d.nans += c == (int)kPropagated ? sign : 0;

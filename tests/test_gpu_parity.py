@@ -483,3 +483,40 @@ def test_histogram_3d_large_window(gpu, oracle) -> None:
             args = (kind, cube, size, None, (0, 0, 0), (mode,) * 3, 0.0, True, False, 1, parameter)
             base = "median" if kind == "median_histogram" else "rank"
             _assert_bits(_gpu(*args), _oracle(oracle, base, *args[1:]), (mode, kind))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_fp32c_moments_are_exact_sums_rounded(gpu, oracle, dtype) -> None:
+    """The default moments path sums exactly (fixed-point window sums), so on
+    zero-centred data, where a compensated floating-point sum cancels, its
+    results stay within 1 ulp (float32) / 1e-15 relative (float64) of the
+    exact window moments, for boxes (sliding kernel) and footprints (tile
+    kernel), every kind, with NaN / infinity handling and ddof."""
+    from ndfiltrs_gb300 import kernels
+
+    rng = np.random.default_rng(17)
+    values = rng.normal(size=(61, 83)).astype(dtype)
+    values[rng.random(values.shape) < 0.03] = np.nan
+    values[rng.random(values.shape) < 0.01] = np.inf
+    values[:, 7] *= dtype(1e-6)  # a column of tiny values widens the tiles' bit span
+    ring = kernels.ring(2, 4, 2) != 0
+    for size, footprint in (((9, 9), None), ((1, 31), None), (None, ring), (None, kernels.tophat(3, 2) != 0)):
+        for kind in ("mean", "var", "std"):
+            for ignore_inf, min_count, ddof in ((True, 1, 0), (True, 5, 1), (False, 1, 1)):
+                args = (kind, values, size, footprint, (0, 0), ("reflect", "wrap"), 0.0, True, ignore_inf,
+                        min_count, ddof)
+                exact = oracle.exact_moments(values, kind, size, footprint=footprint, mode=("reflect", "wrap"),
+                                             omit_nan=True, ignore_inf=ignore_inf, min_count=min_count, ddof=ddof)
+                fast = _gpu(*args, moments="fp32c")
+                context = (kind, size, None if footprint is None else int(footprint.sum()), ignore_inf, ddof)
+                np.testing.assert_array_equal(np.isnan(fast), np.isnan(exact), err_msg=str(context))
+                finite = np.isfinite(exact) & (np.abs(exact) > np.finfo(dtype).tiny * 1e6)
+                np.testing.assert_array_equal(fast[np.isinf(exact)], exact[np.isinf(exact)].astype(dtype))
+                a = fast[finite].astype(np.float64)
+                e = exact[finite]
+                if dtype == np.float32:
+                    ulp = np.spacing(np.abs(e.astype(np.float32))).astype(np.float64)
+                    assert np.all(np.abs(a - e) <= ulp), (context, float((np.abs(a - e) / ulp).max(initial=0)))
+                else:
+                    rel = np.abs(a - e) / np.abs(e)
+                    assert np.all(rel <= 1e-15), (context, float(rel.max(initial=0)))
