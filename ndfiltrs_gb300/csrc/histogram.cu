@@ -95,6 +95,41 @@ __device__ inline Slot<K> slot_at(unsigned char* base, int S) {
   return s;
 }
 
+// Accesses to the sort slots in global memory with an L2 evict-last policy.
+// A block rewrites its slot on every radix pass; together the slots hold
+// (grid) x S x 12 bytes (67 MB for 152 blocks of 36,864 samples), which fits
+// in the 126 MB L2, and the hint keeps them there against the input stream
+// (read with evict-first loads), so the ping-pong does not reach DRAM.
+__device__ __forceinline__ unsigned long long keep_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_keep(uint32_t* a, uint32_t v, unsigned long long p) {
+  asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(p) : "memory");
+}
+__device__ __forceinline__ void st_keep(unsigned long long* a, unsigned long long v, unsigned long long p) {
+  asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(a), "l"(v), "l"(p) : "memory");
+}
+__device__ __forceinline__ void st_keep(uint16_t* a, uint16_t v, unsigned long long p) {
+  asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(a), "h"(v), "l"(p) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_keep(const uint32_t* a, unsigned long long p) {
+  uint32_t v;
+  asm volatile("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_keep(const unsigned long long* a, unsigned long long p) {
+  unsigned long long v;
+  asm volatile("ld.global.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint16_t ld_keep(const uint16_t* a, unsigned long long p) {
+  uint16_t v;
+  asm volatile("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(p) : "memory");
+  return v;
+}
+
 // Shared-memory words of the sort's counter tables for `nd` digits: one
 // table of nd counters per warp plus the nd digit totals.
 __host__ __device__ inline long long sort_table_words(int nd) { return (long long)(kHWarps + 1) * nd; }
@@ -108,7 +143,8 @@ constexpr int kBatch = 16;
 
 template <typename K, typename Digit>
 __device__ void radix_pass(const K* src_k, const uint16_t* src_p, K* dst_k, uint16_t* dst_p, int S,
-                           unsigned int* table, unsigned int* totals, int nd, Digit digit) {
+                           unsigned int* table, unsigned int* totals, int nd, Digit digit,
+                           unsigned long long keep) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < kHWarps * nd; i += blockDim.x) table[i] = 0;
   __syncthreads();
@@ -121,7 +157,7 @@ __device__ void radix_pass(const K* src_k, const uint16_t* src_p, K* dst_k, uint
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int i = b + j * 32 + lane;
-      keys[j] = i < end ? src_k[i] : K(0);
+      keys[j] = i < end ? ld_keep(src_k + i, keep) : K(0);
     }
 #pragma unroll
     for (int j = 0; j < kBatch; ++j)
@@ -167,8 +203,8 @@ __device__ void radix_pass(const K* src_k, const uint16_t* src_p, K* dst_k, uint
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int i = b + j * 32 + lane;
-      keys[j] = i < end ? src_k[i] : K(0);
-      pays[j] = i < end ? src_p[i] : uint16_t(0);
+      keys[j] = i < end ? ld_keep(src_k + i, keep) : K(0);
+      pays[j] = i < end ? ld_keep(src_p + i, keep) : uint16_t(0);
     }
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
@@ -182,8 +218,8 @@ __device__ void radix_pass(const K* src_k, const uint16_t* src_p, K* dst_k, uint
       if (valid && lane == 31 - __clz(peers)) wt[d] += __popc(peers);
       __syncwarp();
       if (valid) {
-        dst_k[pos] = keys[j];
-        dst_p[pos] = pays[j];
+        st_keep(dst_k + pos, keys[j], keep);
+        st_keep(dst_p + pos, pays[j], keep);
       }
     }
   }
@@ -409,9 +445,13 @@ __device__ __forceinline__ void step(const uint16_t* codes, int remove_start, in
                                      int stride, SegHist& h) {
   const int hl = seg_lane();
   StepDelta d;
-  for (int i = hl; i < n; i += kSeg) {
-    const int rc = codes[remove_start + i * stride];
-    const int ac = codes[add_start + i * stride];
+  // The same trip count in every lane (lanes past the face's end update a
+  // dropped code, a no-op), so the loop never diverges.
+  const int iters = (n + kSeg - 1) / kSeg;
+  for (int it = 0, i = hl; it < iters; ++it, i += kSeg) {
+    const bool in = i < n;
+    const int rc = in ? codes[remove_start + i * stride] : (int)kOmitted;
+    const int ac = in ? codes[add_start + i * stride] : (int)kOmitted;
     update<PROPAGATE>(h, rc, -1, d);
     update<PROPAGATE>(h, ac, +1, d);
   }
@@ -437,9 +477,11 @@ __device__ __forceinline__ void step_lists(const uint16_t* codes, int rbase, con
                                            int abase, const uint16_t* alist, int n, SegHist& h) {
   const int hl = seg_lane();
   StepDelta d;
-  for (int i = hl; i < n; i += kSeg) {
-    const int rc = codes[rbase + rlist[i]];
-    const int ac = codes[abase + alist[i]];
+  const int iters = (n + kSeg - 1) / kSeg;
+  for (int it = 0, i = hl; it < iters; ++it, i += kSeg) {
+    const bool in = i < n;
+    const int rc = in ? codes[rbase + rlist[i]] : (int)kOmitted;
+    const int ac = in ? codes[abase + alist[i]] : (int)kOmitted;
     update<PROPAGATE>(h, rc, -1, d);
     update<PROPAGATE>(h, ac, +1, d);
   }
@@ -671,6 +713,7 @@ __device__ __forceinline__ void histogram_tile(const T* __restrict__ in, T* __re
   unsigned int* totals = work + kHWarps * nd;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Slot<K> slot = slot_at<K>(scratch_slot, S);
+  const unsigned long long keep = keep_policy();
   const bool drop_inf = a.r.drop_inf;
   const K outside = sample_key<T>((T)a.r.cval, drop_inf);
   const long long z = tile / a.tiles_yx;
@@ -690,9 +733,9 @@ __device__ __forceinline__ void histogram_tile(const T* __restrict__ in, T* __re
     const bool inside = map_index(z + sz - g.az, g.D, g.mz, &mz) &&
                         map_index(y0 + sy - g.ay, g.H, g.my, &my) &&
                         map_index(x0 + sx - g.ax, g.W, g.mx, &mx);
-    const K key = inside ? sample_key<T>(__ldg(in + (mz * g.H + my) * g.W + mx), drop_inf) : outside;
-    slot.keys_a[e] = key;
-    slot.pay_a[e] = (uint16_t)e;
+    const K key = inside ? sample_key<T>(__ldcs(in + (mz * g.H + my) * g.W + mx), drop_inf) : outside;
+    st_keep(slot.keys_a + e, key, keep);
+    st_keep(slot.pay_a + e, (uint16_t)e, keep);
     if (key != kSent) {
       k_and &= key;
       k_or |= key;
@@ -735,7 +778,7 @@ __device__ __forceinline__ void histogram_tile(const T* __restrict__ in, T* __re
     const K mask = (K)(nd - 1);
     for (int shift = lo; shift <= hi; shift += a.digit_bits) {
       radix_pass(src_k, src_p, dst_k, dst_p, S, table, totals, nd,
-                 [shift, mask](K key) { return (unsigned int)((key >> shift) & mask); });
+                 [shift, mask](K key) { return (unsigned int)((key >> shift) & mask); }, keep);
       K* tk = src_k;
       src_k = dst_k;
       dst_k = tk;
@@ -746,8 +789,8 @@ __device__ __forceinline__ void histogram_tile(const T* __restrict__ in, T* __re
   }
   const uint16_t dropped = a.r.omit ? kOmitted : kPropagated;
   for (int pos = threadIdx.x; pos < S; pos += blockDim.x) {
-    const K key = src_k[pos];
-    codes_s[src_p[pos]] = key == kSent ? dropped : (uint16_t)pos;
+    const K key = ld_keep(src_k + pos, keep);
+    codes_s[ld_keep(src_p + pos, keep)] = key == kSent ? dropped : (uint16_t)pos;
     if (SDEC) decode_s[pos] = key;
   }
   __syncthreads();
