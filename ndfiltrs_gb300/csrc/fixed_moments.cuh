@@ -210,12 +210,14 @@ __device__ __forceinline__ float combine_f32(i128 s1, u128 s2, unsigned int fini
 
 // The value range of a tile's staged support: its pivot (first finite
 // sample), the lowest and highest set bits of its finite samples (units of
-// 2^E0), a bound on the exponent of |x - P|, and whether every sample is
-// finite. Every thread of the block calls it and gets the same result.
+// 2^E0), a bound on the exponent of |x - P|, the classes of non-finite
+// samples present (bit 0 NaN, bit 1 +inf, bit 2 -inf) and whether every
+// sample is finite. Every thread of the block calls it and gets the same
+// result.
 template <typename T>
 struct Span {
   T pivot;
-  int lo, top, dev;
+  int lo, top, dev, classes;
   bool all_finite;
   __device__ int e0() const { return sizeof(T) == 4 ? -149 : -1074; }
 };
@@ -271,7 +273,7 @@ __device__ Span<T> tile_span(const T* s, int support) {
       else
         dev = max(dev, exponent_of(__dsub_rn((double)v, (double)sp.pivot)));
     } else {
-      nonfinite = 1;
+      nonfinite |= isnan(v) ? 1 : (v > (T)0 ? 2 : 4);
     }
   }
   for (int o = 16; o >= 1; o >>= 1) {
@@ -302,6 +304,7 @@ __device__ Span<T> tile_span(const T* s, int support) {
   sp.lo = lo == INT_MAX ? 0 : lo;
   sp.top = top;
   sp.dev = dev;
+  sp.classes = nonfinite;
   sp.all_finite = nonfinite == 0;
   (void)E0;
   return sp;

@@ -389,6 +389,78 @@ def test_sliding_moments_against_exact_oracle(gpu, oracle, dtype) -> None:
                         assert np.all(close), context
 
 
+def _slide_path_images(rng, dtype):
+    """Images that steer the sliding moments kernel's tiles into each of its
+    arithmetic paths (name, array)."""
+    shape = (150, 170)
+    base = 1e4 + rng.normal(size=shape)
+    images = [("finite", base)]
+    for name, value in (("nan_only", np.nan), ("pinf_only", np.inf), ("ninf_only", -np.inf)):
+        image = base.copy()
+        image[rng.random(shape) < 0.02] = value
+        image[40:47, 60:70] = value  # windows with many of them
+        images.append((name, image))
+    mixed = base.copy()
+    mixed[rng.random(shape) < 0.02] = np.nan
+    mixed[rng.random(shape) < 0.01] = np.inf
+    mixed[rng.random(shape) < 0.01] = -np.inf
+    images.append(("mixed", mixed))
+    # Multiples of 1/8 up to 2^24: deviations of about 28 bits, whose window
+    # sums of squares need 128 bits.
+    images.append(("eighths", np.round(rng.uniform(-2.0**24, 2.0**24, size=shape) * 8) / 8))
+    # A column of tiny values: deviations beyond 30 (float32) bits.
+    tiny = base.copy()
+    tiny[:, 33] *= 1e-7
+    tiny[rng.random(shape) < 0.01] = np.nan
+    images.append(("tiny_column", tiny))
+    # Small integers: narrow sums for float64 too.
+    integers = np.floor(rng.normal(100.0, 20.0, size=shape))
+    integers[rng.random(shape) < 0.02] = np.nan
+    images.append(("integers", integers))
+    return [(name, image.astype(dtype)) for name, image in images]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_sliding_moments_every_path_is_exact(gpu, oracle, dtype) -> None:
+    """The sliding moments kernel keeps 64- or 128-bit column sums, packs the
+    count of a single non-finite class above the sum of deviations or keeps
+    every class's counts, and holds deviations in place of the samples or
+    recomputes them; every combination (steered by the images' value
+    ranges and non-finite classes) stays within 1 ulp (float32) / 1e-15
+    relative (float64) of the exact window moments, with the reference's
+    NaN / infinity classification, under both NaN policies, both infinity
+    policies, ddof, min_count and boundary modes, on tiles cut by the array
+    edges."""
+    from ndfiltrs_gb300 import _core
+
+    rng = np.random.default_rng(23)
+    for name, values in _slide_path_images(rng, dtype):
+        for size, mode in (((7, 9), "reflect"), ((31, 31), "nearest"), ((3, 45), "wrap"), ((33, 2), "constant")):
+            for kind in ("mean", "var", "std"):
+                for omit, ignore_inf, min_count, ddof in ((True, True, 5, 1), (False, False, 1, 0),
+                                                          (True, False, 1, 2)):
+                    parameter = ddof if kind != "mean" else 0
+                    with _core.Plan(values.shape, dtype, kind, size, mode=[mode] * 2, cval=2.5, omit_nan=omit,
+                                    ignore_inf=ignore_inf, min_count=min_count, parameter=parameter) as plan:
+                        assert plan.algorithm == "moments_slide"
+                        actual = plan.run_host(values)
+                    exact = oracle.exact_moments(values, kind, size, mode=mode, cval=2.5, omit_nan=omit,
+                                                 ignore_inf=ignore_inf, min_count=min_count, ddof=parameter)
+                    context = (name, size, mode, kind, omit, ignore_inf, ddof)
+                    np.testing.assert_array_equal(np.isnan(actual), np.isnan(exact), err_msg=str(context))
+                    np.testing.assert_array_equal(actual[np.isinf(exact)], exact[np.isinf(exact)].astype(dtype),
+                                                  err_msg=str(context))
+                    finite = np.isfinite(exact) & (np.abs(exact) > np.finfo(dtype).tiny * 1e6)
+                    a, e = actual[finite].astype(np.float64), exact[finite]
+                    if dtype == np.float32:
+                        ulp = np.spacing(np.abs(e.astype(np.float32))).astype(np.float64)
+                        worst = float((np.abs(a - e) / ulp).max(initial=0))
+                        assert worst <= 1, (context, worst)
+                    else:
+                        worst = float((np.abs(a - e) / np.abs(e)).max(initial=0))
+                        assert worst <= 1e-15, (context, worst)
+
+
 @pytest.mark.parametrize("family,algorithm", [("passes", "extrema_passes"), ("extrema", "extrema_tile")])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_separable_extrema(gpu, oracle, dtype, family, algorithm) -> None:
