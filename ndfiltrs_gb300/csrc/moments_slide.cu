@@ -50,15 +50,15 @@ constexpr int kSThreads = 256;
 
 struct SlideArgs {
   int count_bits;  // bit length of (window volume + 1)
-  int pad;
+  int rows;        // output rows per chunk (64-bit sums; 128-bit sums take half)
 };
 
-// Output rows per chunk (64-bit sums; 128-bit sums take half as many) and
-// outputs per row work item of a tile: a chunk holds 1024 column sums of
-// each kind, so every chunk has exactly kSThreads row items.
-__host__ __device__ inline int slide_rows(const Tile& t) { return t.TH < 1024 / t.TW ? t.TH : 1024 / t.TW; }
-__host__ __device__ inline int slide_wide_rows(const Tile& t) { return slide_rows(t) > 1 ? slide_rows(t) / 2 : 1; }
-__host__ __device__ inline int slide_seg(const Tile& t) { return t.TW * slide_rows(t) / kSThreads > 0 ? t.TW * slide_rows(t) / kSThreads : 1; }
+// Outputs per row work item: as many as make rows x TW / seg = kSThreads
+// items (one per thread), at least one. TW and rows are powers of two.
+__host__ __device__ inline int slide_seg(int tw, int rows) {
+  return tw * rows / kSThreads > 0 ? tw * rows / kSThreads : 1;
+}
+__host__ __device__ inline int slide_wide_rows(int rows) { return rows > 1 ? rows / 2 : 1; }
 
 __host__ __device__ inline size_t round16(size_t v) { return (v + 15) & ~(size_t)15; }
 
@@ -74,9 +74,9 @@ struct SlideLayout {
   int pitch;
 };
 
-__host__ __device__ inline SlideLayout slide_layout(const Tile& t, int kd, int elem) {
+__host__ __device__ inline SlideLayout slide_layout(const Tile& t, int kd, int elem, int rows) {
   SlideLayout l;
-  const int rows = slide_rows(t), wide_rows = slide_wide_rows(t);
+  const int wide_rows = slide_wide_rows(rows);
   l.pitch = t.SW + t.SW / 8 + 1;
   l.s = round16((size_t)(t.SW + t.SH + kd) * 8);
   l.state = round16(l.s + (size_t)t.SH * t.SW * elem);
@@ -119,8 +119,9 @@ __device__ __forceinline__ void column_walk(unsigned char* base, const SlideLayo
   const Tile& t = a.t;
   const Reduce& r = a.r;
   const int kh = g.kh, kw = g.kw, SW = t.SW, TW = t.TW, TH = t.TH;
-  const int rows = NARROW ? slide_rows(t) : slide_wide_rows(t);
-  const int seg = NARROW ? slide_seg(t) : (slide_seg(t) > 1 ? slide_seg(t) / 2 : 1);
+  const int rows = NARROW ? sa.rows : slide_wide_rows(sa.rows);
+  const int seg0 = slide_seg(TW, sa.rows);
+  const int seg = NARROW ? seg0 : (seg0 > 1 ? seg0 / 2 : 1);
   const int pitch = L.pitch;
   S1* st1 = reinterpret_cast<S1*>(base + L.state);
   S2* st2 = reinterpret_cast<S2*>(base + L.state + (size_t)SW * 16);
@@ -323,7 +324,7 @@ __device__ __forceinline__ void moments_slide_body(const T* __restrict__ in, T* 
   const Geom3& g = a.g;
   const Tile& t = a.t;
   const Reduce& r = a.r;
-  const SlideLayout L = slide_layout(t, g.kd, (int)sizeof(T));
+  const SlideLayout L = slide_layout(t, g.kd, (int)sizeof(T), sa.rows);
   long long* maps = reinterpret_cast<long long*>(smem_raw);
   T* s = reinterpret_cast<T*>(smem_raw + L.s);
   long long z, y0, x0;
@@ -451,11 +452,11 @@ cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
   auto kernel = moments_slide_kernel<T>;
   cudaError_t e = allow_max_smem((const void*)kernel);
   if (e != cudaSuccess) return e;
-  SlideArgs sa{count_bits_of(p), 0};
+  SlideArgs sa{count_bits_of(p), p.slide_rows};
   TileArgs args = p.tile;
   CUtensorMap map{};
   // The TMA staging area overlays the chunk buffers (see SlideLayout).
-  size_t smem = slide_layout(p.tile.t, p.tile.g.kd, (int)sizeof(T)).vbuf;
+  size_t smem = slide_layout(p.tile.t, p.tile.g.kd, (int)sizeof(T), p.slide_rows).vbuf;
   if (tma_prepare(p, p.tile.t, in, &map, &args, &smem))
     smem = std::max(smem, p.smem_bytes);
   else
@@ -466,17 +467,23 @@ cudaError_t launch_t(const Plan& p, const T* in, T* out, cudaStream_t s) {
 
 }  // namespace
 
-// Tile shape of the sliding moments kernel: 64 x 64 outputs (chunks of 16
-// rows), else 32 x 128, 64 x 32, 32 x 64 / 32 / 16 / 8 (chunks of up to 32
-// rows): the first within 112 KB of shared memory (two blocks per SM), else
-// the first within the device limit; 1024 x 1 for single-row arrays. False
-// when the window or the array does not suit it (footprints, rank 3, counts
-// beyond 16 bits, supports beyond shared memory).
+// Tile shape and chunk rows of the sliding moments kernel, in the order
+// measured fastest on the GB300 (4096^2 float32 / float64): 64 x 32 outputs
+// in chunks of 16 rows for most windows (31 x 31: 0.53 ms; 9 x 9: 0.36 ms;
+// 31 x 31 float64: 1.87 ms); 128 x 16 in chunks of 8 for flat windows whose
+// width is at least four times their height (7 x 51: 0.48 ms; 1 x 31:
+// 0.35 ms); 128 x 64 / 64 x 64 in chunks of 16 for windows of 48 rows and
+// columns or more (65 x 65: 1.02 ms; 101 x 101: 1.88 ms); then smaller
+// tiles down to 32 x 8 when shared memory is short. Single-row arrays take
+// 1024 x 1 tiles. False when the window or the array does not suit the
+// kernel (footprints, rank 3, counts beyond 16 bits, supports beyond shared
+// memory).
 bool moments_slide_configure(Plan& p, int smem_limit) {
   const Geom3& g = p.tile.g;
   if (p.ndim > 2 || g.D != 1 || !p.footprint.empty()) return false;
   const long long volume = (long long)g.kh * g.kw;
   if (volume + g.kw + g.kh >= 65535) return false;
+  const int elem = p.dtype == 0 ? 4 : 8;
   auto shape = [&](int tw, int th) {
     Tile t = p.tile.t;
     t.TW = tw;
@@ -488,26 +495,22 @@ bool moments_slide_configure(Plan& p, int smem_limit) {
     t.tiles = t.tiles_x * t.tiles_y * g.D;
     return t;
   };
-  auto bytes = [&](const Tile& t) { return slide_layout(t, g.kd, p.dtype == 0 ? 4 : 8).total; };
-  if (g.H == 1 && g.kh == 1) {
-    Tile t = shape(1024, 1);
-    if (bytes(t) > (size_t)smem_limit) return false;
+  auto take = [&](int tw, int th, int rows) {
+    const Tile t = shape(tw, th);
+    const size_t bytes = slide_layout(t, g.kd, elem, rows).total;
+    if (bytes > (size_t)smem_limit) return false;
     p.tile.t = t;
-    p.smem_bytes = bytes(t);
+    p.slide_rows = rows;
+    p.smem_bytes = bytes;
     return true;
-  }
-  static const int shapes[][2] = {{64, 64}, {32, 128}, {64, 32}, {32, 64}, {32, 32}, {32, 16}, {32, 8}};
-  const size_t budget = std::min<size_t>(112 * 1024, (size_t)smem_limit);
-  for (size_t limit : {budget, (size_t)smem_limit}) {
-    for (const auto& sh : shapes) {
-      const Tile t = shape(sh[0], sh[1]);
-      if (bytes(t) <= limit) {
-        p.tile.t = t;
-        p.smem_bytes = bytes(t);
-        return true;
-      }
-    }
-  }
+  };
+  if (g.H == 1 && g.kh == 1) return take(1024, 1, 1);
+  if (g.kw >= 4 * g.kh && g.kh <= 16 && take(128, 16, 8)) return true;
+  if (g.kh >= 48 && g.kw >= 48 && (take(128, 64, 16) || take(64, 64, 16))) return true;
+  static const int order[][3] = {{64, 32, 16}, {64, 64, 16}, {128, 32, 8}, {32, 64, 32},
+                                 {32, 32, 32}, {32, 16, 16}, {32, 8, 8}};
+  for (const auto& o : order)
+    if (take(o[0], o[1], o[2])) return true;
   return false;
 }
 
@@ -533,6 +536,7 @@ void slide_family_write_task(const Plan& p, const void* in, void* out, long long
   t.a.r = p.r;
   t.a.tma_bw = 0;
   t.sa.count_bits = count_bits_of(p);
+  t.sa.rows = p.slide_rows;
   std::memcpy(task, &t, sizeof(t));
 }
 

@@ -181,6 +181,7 @@ struct Plan {
   // Kernel choice: measure candidates not in the autotune cache (batches).
   bool may_tune = false;
   int ext_rows[2] = {0, 0};  // rows per block of the two extrema column passes
+  int slide_rows = 0;        // output rows per chunk of the sliding moments kernel
   RobustArgs robust{};       // robust estimator parameters
   long long robust_threads = 0;  // threads of the scratch-backed robust kernel
 
