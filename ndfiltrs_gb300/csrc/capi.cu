@@ -855,8 +855,9 @@ int plan_apply(Plan& p, const Candidate& c, int smem_limit) { return apply_candi
 // lies inside its band's real rows except at the array's own first and last
 // rows, where the band's edge is the array's edge, so boundary modes behave
 // as for the whole array. Not used for the wrap mode along the first axis
-// (its windows reach the far edge), for float32-compensated moments (their
-// per-tile pivots make the last bits depend on the tiling), for robust
+// (its windows reach the far edge), for float32-compensated moments other
+// than the sliding kernel's float32 outputs (elsewhere the last bits depend
+// on the tiling), for robust
 // windows beyond 256 samples (their per-plan scratch), or for small arrays.
 // Bands pay for recomputing their overlaps and for smaller launches, which
 // costs more than it saves for kernels slower than the copies (wide
@@ -895,7 +896,13 @@ constexpr size_t kBandMinBytes = 16u << 20;
 int build_strips(Plan& p) {
   p.strips_tried = true;
   if (p.algo == Algo::kEmpty || p.ndim < 1 || p.modes[0] == NDF_MODE_WRAP) return NDF_OK;
-  if (is_moment(p.r.kind) && p.r.moments == 0) return NDF_OK;
+  // Float32-compensated moments: only the sliding kernel with float32
+  // output, whose exact-integer combine depends on the window's samples
+  // alone (not on its tile's pivot or lowest bit), so bands give the whole
+  // array's bits; float64 outputs convert the exact numerator word by word,
+  // and the footprint kernel is not banded either.
+  const bool fp32c = is_moment(p.r.kind) && p.r.moments == 0;
+  if (fp32c && !(p.algo == Algo::kMomentsSlide && p.dtype == 0)) return NDF_OK;
   if (p.robust_threads > 0) return NDF_OK;  // per-thread scratch of up to 1 GiB per plan
   const size_t bytes = (size_t)p.n_out * element_bytes(p);
   if (bytes < kBandMinBytes) return NDF_OK;
@@ -943,6 +950,7 @@ int build_strips(Plan& p) {
     q.sm_count = sm_count;
     rc = choose_algorithm(q, smem_limit);
     if (rc != NDF_OK) return rc;
+    if (fp32c && q.algo != Algo::kMomentsSlide) return NDF_OK;
     b.out_offset = total;
     total += (size_t)q.n_out;
   }

@@ -148,6 +148,35 @@ __device__ __forceinline__ void ff_div(float hi, float lo, float dh, float dl, f
   ql = __fsub_rn(q2, __fsub_rn(qh, q1));
 }
 
+// Variance / standard deviation of float32 output from the exact numerator
+// n S2 - S1^2 (192-bit, d2:d1:d0, in units of 2^(2 quantum)).
+template <int KIND>
+__device__ __forceinline__ float spread_f32(unsigned long long d2, unsigned long long d1, unsigned long long d0,
+                                            unsigned int finite, long long ddof, int quantum) {
+  float hi, lo;
+  int e;
+  top48(d2, d1, d0, hi, lo, e);
+  const unsigned long long den = (unsigned long long)finite * (unsigned long long)(finite - ddof);
+  const float dh = (float)den;
+  const float dl = (float)((long long)den - (long long)dh);
+  float qh, ql;
+  ff_div(hi, lo, dh, dl, qh, ql);
+  if (KIND == kVar) return scalbnf(__fadd_rn(qh, ql), e + 2 * quantum);
+  // sqrt((qh + ql) 2^e) 2^quantum with an even power of two under the root.
+  if (e & 1) {
+    qh = __fmul_rn(qh, 2.0f);
+    ql = __fmul_rn(ql, 2.0f);
+    e -= 1;
+  }
+  const float r0 = __fsqrt_rn(qh);
+  float root = r0;
+  if (r0 > 0.0f) {
+    const float resid = __fadd_rn(fmaf(-r0, r0, qh), ql);
+    root = __fadd_rn(r0, __fdiv_rn(resid, __fmul_rn(2.0f, r0)));
+  }
+  return scalbnf(root, e / 2 + quantum);
+}
+
 template <int KIND>
 __device__ __forceinline__ float combine_f32(i128 s1, u128 s2, unsigned int finite, long long ddof, float pivot,
                                              int quantum) {
@@ -184,28 +213,7 @@ __device__ __forceinline__ float combine_f32(i128 s1, u128 s2, unsigned int fini
   const unsigned long long d0 = n0 - b0, br0 = n0 < b0;
   const unsigned long long t1 = n1 - b1, d1 = t1 - br0, br1 = (n1 < b1) | (t1 < br0);
   const unsigned long long d2 = n2 - b2 - br1;
-  float hi, lo;
-  int e;
-  top48(d2, d1, d0, hi, lo, e);
-  const unsigned long long den = (unsigned long long)finite * (unsigned long long)(finite - ddof);
-  const float dh = (float)den;
-  const float dl = (float)((long long)den - (long long)dh);
-  float qh, ql;
-  ff_div(hi, lo, dh, dl, qh, ql);
-  if (KIND == kVar) return scalbnf(__fadd_rn(qh, ql), e + 2 * quantum);
-  // sqrt((qh + ql) 2^e) 2^quantum with an even power of two under the root.
-  if (e & 1) {
-    qh = __fmul_rn(qh, 2.0f);
-    ql = __fmul_rn(ql, 2.0f);
-    e -= 1;
-  }
-  const float r0 = __fsqrt_rn(qh);
-  float root = r0;
-  if (r0 > 0.0f) {
-    const float resid = __fadd_rn(fmaf(-r0, r0, qh), ql);
-    root = __fadd_rn(r0, __fdiv_rn(resid, __fmul_rn(2.0f, r0)));
-  }
-  return scalbnf(root, e / 2 + quantum);
+  return spread_f32<KIND>(d2, d1, d0, finite, ddof, quantum);
 }
 
 // The value range of a tile's staged support: its pivot (first finite
@@ -344,6 +352,29 @@ __device__ __forceinline__ T fixed_combine(int kind, long long ddof, i128 s1, u1
     const double unscaled = __ddiv_rn(num, __dmul_rn(n, (double)((long long)finite - ddof)));
     // Scale after the square root so that a finite deviation never
     // overflows through its square.
+    return kind == kStd ? __dmul_rn(__dsqrt_rn(unscaled), scale) : __dmul_rn(__dmul_rn(unscaled, scale), scale);
+  }
+}
+
+// fixed_combine for sums held in 64-bit words (|S1| < 2^63, S2 < 2^64): the
+// numerator n S2 - S1^2 fits 128 bits, so its upper word is zero and the
+// same arithmetic runs on fewer words. Results equal fixed_combine's.
+template <typename T>
+__device__ __forceinline__ T fixed_combine_narrow(int kind, long long ddof, long long s1, unsigned long long s2,
+                                                 unsigned int finite, i128 P, int quantum) {
+  if (kind == kMean) return fixed_combine<T>(kind, ddof, (i128)s1, (u128)s2, finite, P, quantum);
+  const unsigned long long a = s1 < 0 ? 0ull - (unsigned long long)s1 : (unsigned long long)s1;
+  const u128 d = (u128)s2 * finite - (u128)a * a;  // >= 0 (Cauchy-Schwarz)
+  const unsigned long long d1 = (unsigned long long)(d >> 64), d0 = (unsigned long long)d;
+  if constexpr (sizeof(T) == 4) {
+    return kind == kVar ? spread_f32<kVar>(0ull, d1, d0, finite, ddof, quantum)
+                        : spread_f32<kStd>(0ull, d1, d0, finite, ddof, quantum);
+  } else {
+    const double n = (double)finite;
+    const double scale = pow2(quantum);
+    const double num = (double)0ull * 340282366920938463463374607431768211456.0 + (double)d1 * 18446744073709551616.0 +
+                       (double)d0;
+    const double unscaled = __ddiv_rn(num, __dmul_rn(n, (double)((long long)finite - ddof)));
     return kind == kStd ? __dmul_rn(__dsqrt_rn(unscaled), scale) : __dmul_rn(__dmul_rn(unscaled, scale), scale);
   }
 }

@@ -197,7 +197,10 @@ __device__ __forceinline__ void column_walk(unsigned char* base, const SlideLayo
     double result;
     if (mom::decide_special(r, (long long)finite + pos + neg, nanc != 0, pos != 0, neg != 0, &result))
       return canonical(from_f64<T>(result));
-    return canonical(fixed_combine<T>(r.kind, r.param, (i128)a1, (u128)a2, finite, P, quantum));
+    if constexpr (NARROW)
+      return canonical(fixed_combine_narrow<T>(r.kind, r.param, a1, a2, finite, P, quantum));
+    else
+      return canonical(fixed_combine<T>(r.kind, r.param, (i128)a1, (u128)a2, finite, P, quantum));
   };
 
   const int chunks = (TH + rows - 1) / rows;

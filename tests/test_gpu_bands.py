@@ -41,10 +41,17 @@ CASES = [
     ((1 << 23,), np.float32, dict(kind="median", size=(9,), origin=(2,), mode=("mirror",), omit_nan=True), True),
     ((512, 96, 96), np.float32, dict(kind="median", size=(3, 5, 5), mode=("nearest", "reflect", "wrap"),
                                      omit_nan=True), True),
-    # Not banded: wrap along the first axis, float32-compensated moments,
-    # arrays below 16 MiB.
+    # Float32-compensated moments of float32 arrays (sliding kernel).
+    ((2048, 2048), np.float32, dict(kind="std", size=(9, 9), omit_nan=True, moments="fp32c"), True),
+    ((2048, 2048), np.float32, dict(kind="mean", size=(31, 31), mode=("nearest", "mirror"), omit_nan=True,
+                                    ignore_inf=True, moments="fp32c"), True),
+    ((2048, 2048), np.float32, dict(kind="var", size=(7, 51), origin=(2, -5), omit_nan=False,
+                                    moments="fp32c"), True),
+    # Not banded: wrap along the first axis, float32-compensated moments of
+    # float64 arrays or footprints, arrays below 16 MiB.
     ((2048, 2048), np.float32, dict(kind="median", size=(5, 5), mode=("wrap", "reflect"), omit_nan=True), False),
-    ((2048, 2048), np.float32, dict(kind="std", size=(9, 9), omit_nan=True, moments="fp32c"), False),
+    ((1500, 1400), np.float64, dict(kind="std", size=(9, 9), omit_nan=True, moments="fp32c"), False),
+    ((2048, 2048), np.float32, dict(kind="std", size=(9, 9), footprint=RING, omit_nan=True, moments="fp32c"), False),
     ((1024, 1024), np.float32, dict(kind="median", size=(5, 5), omit_nan=True), False),
 ]
 
