@@ -913,7 +913,8 @@ def autotune_entries() -> int:
 
 def pin_kernel(family: str | None) -> None:
     """Make plans take kernel ``family`` ("histogram", "box", "network",
-    "radix", "moments", "slide", "extrema", "passes", "boxcar", "band")
+    "ranked", "radix", "moments", "slide", "extrema", "passes", "boxcar",
+    "band")
     whenever it is one of their candidates; None unpins. Results never
     depend on it."""
     lib, _ = _load()

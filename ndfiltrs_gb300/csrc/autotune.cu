@@ -86,6 +86,8 @@ const char* algo_token(Algo a) {
       return "box";
     case Algo::kTileNetwork:
       return "network";
+    case Algo::kTileRank:
+      return "ranked";
     case Algo::kTileRadix:
       return "radix";
     case Algo::kMomentsTile:
@@ -109,6 +111,7 @@ bool parse_algo(const std::string& t, Algo* a) {
   static const std::pair<const char*, Algo> names[] = {{"histogram", Algo::kHistogram},
                                                        {"box", Algo::kTileBox},
                                                        {"network", Algo::kTileNetwork},
+                                                       {"ranked", Algo::kTileRank},
                                                        {"radix", Algo::kTileRadix},
                                                        {"moments", Algo::kMomentsTile},
                                                        {"slide", Algo::kMomentsSlide},

@@ -66,6 +66,8 @@ const char* algo_name(Algo a) {
       return "robust";
     case Algo::kMomentsSlide:
       return "moments_slide";
+    case Algo::kTileRank:
+      return "rank_network";
     case Algo::kExtremaTile:
       return "extrema_tile";
   }
@@ -550,6 +552,12 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
     Tile bt = box_tile(g);
     if (tile_select_smem(p, bt) <= (size_t)smem_limit) out.push_back({Algo::kTileBox, bt.TW, bt.TH});
   }
+  if (width >= 48 && !line) {
+    // Float32 networks of 48 wires or more: rank codes, two windows per thread.
+    Plan probe = p;
+    if (rank_network_configure(probe, smem_limit))
+      out.push_back({Algo::kTileRank, probe.tile.t.TW, probe.tile.t.TH});
+  }
   for (auto [tw, th] : tiles) {
     if (!fits_tile(tw, th, false)) continue;
     if (width > 0)
@@ -587,6 +595,9 @@ int apply_candidate_impl(Plan& p, const Candidate& c, int smem_limit) {
       set_tile(p, c.tw, c.th);
       p.smem_bytes = tile_select_smem(p, p.tile.t);
       p.network = network_width_for(p.dtype, p.r.count);
+      return NDF_OK;
+    case Algo::kTileRank:
+      if (!rank_network_configure(p, smem_limit)) return fail(NDF_ERR_UNSUPPORTED, "window too large");
       return NDF_OK;
     case Algo::kTileRadix:
       set_tile(p, c.tw, c.th);
@@ -719,6 +730,9 @@ int run_plan(const Plan& p, const void* in, void* out, cudaStream_t s) {
       break;
     case Algo::kMomentsSlide:
       e = launch_moments_slide(p, in, out, s);
+      break;
+    case Algo::kTileRank:
+      e = launch_rank_network(p, in, out, s);
       break;
     case Algo::kExtremaTile:
     case Algo::kExtremaPasses:

@@ -128,6 +128,7 @@ enum class Algo {
   kBoxcarBand,    // exact rolling mean, column sums sliding down bands
   kExtremaPasses, // separable min / max, two transposing column passes
   kRobust,        // MAD, sigma clipping, mode, biweight: per-window float64
+  kTileRank,      // float32 register networks on 16-bit rank codes, two windows per thread
 };
 
 struct StripSet;  // row bands of host-buffer runs (capi.cu)
@@ -232,6 +233,8 @@ cudaError_t launch_histogram(const Plan& p, const void* in, void* out, cudaStrea
 cudaError_t launch_boxcar(const Plan& p, const void* in, void* out, cudaStream_t s);
 cudaError_t launch_moments_slide(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool moments_slide_configure(Plan& p, int smem_limit);
+cudaError_t launch_rank_network(const Plan& p, const void* in, void* out, cudaStream_t s);
+bool rank_network_configure(Plan& p, int smem_limit);
 cudaError_t launch_extrema(const Plan& p, const void* in, void* out, cudaStream_t s);
 bool extrema_configure(Plan& p, int smem_limit);
 bool extrema_passes_configure(Plan& p, int smem_limit);

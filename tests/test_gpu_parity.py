@@ -117,6 +117,52 @@ def test_every_network_width_and_radix(gpu, oracle, dtype) -> None:
                 _assert_bits(_gpu(*args), _oracle(oracle, *args), (count, kind, omit))
 
 
+@pytest.mark.parametrize("family,algorithm", [("ranked", "rank_network"), ("network", "tile_network")])
+def test_ranked_and_plain_networks_every_width(gpu, oracle, family, algorithm) -> None:
+    """Float32 windows of 33 to 128 taps on the ranked network kernel (16-bit
+    rank codes, two windows per thread; 2-D windows) and, pinned, on the plain
+    register network: rings, random footprints, boxes and a 3-D box, every selection
+    kind, both NaN policies with ignore_inf and min_count, boundary modes with
+    a non-zero cval, arrays of several 64-wide tiles with ragged edges; bit
+    for bit against the oracle."""
+    from ndfiltrs_gb300 import _core, kernels
+
+    rng = np.random.default_rng(19)
+    plane = _special_values((150, 171), np.float32, seed=21, fraction=0.05)
+    cube = _special_values((5, 70, 97), np.float32, seed=22, fraction=0.05)
+    windows = [(plane, kernels.ring(4, 6, 2) != 0, None), (plane, None, (7, 9)), (plane, None, (9, 9)),
+               (plane, None, (11, 11)), (cube, None, (3, 5, 5))]
+    for count in (33, 49, 75, 100, 128):
+        flat = np.zeros(13 * 13, dtype=bool)
+        flat[rng.choice(13 * 13, size=count, replace=False)] = True
+        windows.append((plane, flat.reshape(13, 13), None))
+    cases = [("median", 0, True, False, 1, ("reflect", "mirror")), ("median", 0, False, False, 1, ("nearest", "wrap")),
+             ("median", 0, True, True, 20, ("constant", "reflect")), ("rank", 7, True, False, 1, ("wrap", "nearest")),
+             ("percentile", 0, True, False, 1, ("mirror", "constant")), ("min", 0, False, False, 1, ("reflect",) * 2),
+             ("max", 0, True, True, 1, ("nearest", "mirror"))]
+    _core.pin_kernel(family)
+    try:
+        for values, footprint, size in windows:
+            for kind, parameter, omit, ignore_inf, min_count, mode2 in cases:
+                mode = mode2 if values.ndim == 2 else ("reflect",) + mode2
+                origin = (0,) * values.ndim
+                if kind != "percentile":
+                    shape = size if footprint is None else footprint.shape
+                    with _core.Plan(values.shape, np.float32, kind, shape, footprint=footprint, origin=origin,
+                                    mode=mode, cval=-0.75, omit_nan=omit, ignore_inf=ignore_inf,
+                                    min_count=min_count, parameter=parameter) as plan:
+                        # 3-D windows keep the plain network (the ranked kernel
+                        # would rank kd planes of support per output plane).
+                        expected = algorithm if values.ndim == 2 else "tile_network"
+                        assert plan.algorithm == expected, (plan.algorithm, kind, size)
+                args = (kind, values, size, footprint, origin, mode, -0.75, omit, ignore_inf, min_count, parameter,
+                        84.0)
+                context = (family, kind, size, None if footprint is None else int(footprint.sum()), omit)
+                _assert_bits(_gpu(*args), _oracle(oracle, *args), context)
+    finally:
+        _core.pin_kernel(None)
+
+
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_ranks_one_to_five(gpu, oracle, dtype) -> None:
     cases = [
