@@ -7,7 +7,8 @@
 // comparator. Here a tile of 64 x TH outputs first ranks its staged support:
 // the retained keys are compacted in support order and sorted by a block LSD
 // radix sort in shared memory (8-bit digits, only over the bits on which the
-// retained keys differ; stable, so equal keys keep their support order), and
+// retained keys differ; stable, so equal keys keep their support order: lanes
+// with equal digits are found by ballots), and
 // every retained sample gets a 16-bit code, its position in that order, while
 // dropped samples get 0xFFFF. The codes of outputs x and x + 32 of a tile row
 // are packed into one 32-bit word, and the Batcher network runs on the packed
@@ -35,6 +36,34 @@ constexpr int kRWarps = kRThreads / 32;
 constexpr int kRankTW = 64;  // outputs per tile row: pairs (x, x + 32)
 constexpr uint16_t kDrop = 0xFFFF;
 constexpr int kMaxRankSupport = 65534;
+
+// Radix digits of the ranking sort: kDigitBits per pass; with more than 8
+// bits two 16-bit counters share a word (a support has at most 65,534
+// samples, so no count or offset reaches 2^16).
+constexpr int kDigitBits = 8;
+constexpr unsigned int kDigits = 1u << kDigitBits;
+constexpr bool kPacked = kDigitBits > 8;
+constexpr int kTableWords = kPacked ? (int)kDigits / 2 : (int)kDigits;  // per warp
+constexpr int kPerThread = (int)kDigits / kRThreads;
+
+__device__ __forceinline__ unsigned int word_of(unsigned int d) { return kPacked ? d >> 1 : d; }
+__device__ __forceinline__ unsigned int half_of(unsigned int d) { return kPacked ? (d & 1u) * 16u : 0u; }
+__device__ __forceinline__ unsigned int counter(const unsigned int* row, unsigned int d) {
+  return kPacked ? (row[d >> 1] >> ((d & 1u) * 16u)) & 0xFFFFu : row[d];
+}
+
+// The lanes of `active` whose digit equals this lane's, from one ballot per
+// digit bit (cheaper here than the match instruction).
+__device__ __forceinline__ unsigned int same_digit(unsigned int active, unsigned int dg) {
+  unsigned int peers = active;
+#pragma unroll
+  for (int b = 0; b < kDigitBits; ++b) {
+    const bool set = (dg >> b) & 1u;
+    const unsigned int bal = __ballot_sync(active, set);
+    peers &= set ? bal : ~bal;
+  }
+  return peers;
+}
 
 // Two 16-bit codes; the comparator orders both halves at once.
 struct Pair16 {
@@ -85,7 +114,7 @@ __host__ __device__ inline RankLayout rank_layout(const Tile& t, int kd) {
   l.ia = (l.kb + S * 4 + 15) & ~(size_t)15;
   l.codes = (l.ia + S * 4 + 15) & ~(size_t)15;
   l.table = (l.codes + S * 2 + 15) & ~(size_t)15;
-  l.total = l.table + (size_t)kRWarps * 256 * 4;
+  l.total = l.table + (size_t)kRWarps * kTableWords * 4;
   return l;
 }
 
@@ -93,7 +122,7 @@ __host__ __device__ inline RankLayout rank_layout(const Tile& t, int kd) {
 // the retained count R; codes[e] is sample e's position among the retained
 // keys in sorted order, or kDrop; the R sorted keys end in s (*sorted). kb
 // is a second key buffer, ia and ib S-entry index buffers, table kRWarps x
-// 256 counters.
+// kTableWords counters.
 __device__ int rank_support(uint32_t* s, uint32_t* kb, uint16_t* ia, uint16_t* ib, uint16_t* codes,
                             unsigned int* table, int S, const uint32_t** sorted) {
   __shared__ unsigned int warp_n[kRWarps];
@@ -162,33 +191,59 @@ __device__ int rank_support(uint32_t* s, uint32_t* kb, uint16_t* ia, uint16_t* i
     const int hi = 31 - __clz((int)varying);
     const int C2 = ((int)R + kRWarps * 32 - 1) / (kRWarps * 32) * 32;
     const int b2 = warp * C2, e2 = min((int)R, b2 + C2);
-    unsigned int* mine = table + warp * 256;
-    for (int shift = lo; shift <= hi; shift += 8) {
-      for (int d = lane; d < 256; d += 32) mine[d] = 0u;
+    unsigned int* mine = table + warp * kTableWords;
+    for (int shift = lo; shift <= hi; shift += kDigitBits) {
+      for (int w = lane; w < kTableWords; w += 32) mine[w] = 0u;
       __syncwarp();
       for (int base = b2; base < e2; base += 32) {
         const int e = base + lane;
-        if (e < e2) atomicAdd(&mine[(src_k[e] >> shift) & 255u], 1u);
+        if (e < e2) {
+          const unsigned int dg = (src_k[e] >> shift) & (kDigits - 1u);
+          atomicAdd(&mine[word_of(dg)], 1u << half_of(dg));
+        }
       }
       __syncthreads();
-      // Exclusive offsets in (digit, warp) order; thread d owns digit d.
+      // Exclusive offsets in (digit, warp) order; thread t owns digits
+      // [t kPerThread, (t + 1) kPerThread), in pairs when counters are packed.
       {
-        const int d = threadIdx.x;
-        unsigned int col = 0;
-        for (int w = 0; w < kRWarps; ++w) col += table[w * 256 + d];
-        unsigned int incl = col;
+        const int d0 = threadIdx.x * kPerThread;
+        unsigned int col[kPerThread];
+        unsigned int total = 0;
+#pragma unroll
+        for (int j = 0; j < kPerThread; ++j) {
+          col[j] = 0;
+          for (int w = 0; w < kRWarps; ++w) col[j] += counter(table + w * kTableWords, d0 + j);
+          total += col[j];
+        }
+        unsigned int incl = total;
         for (int o = 1; o < 32; o <<= 1) {
           const unsigned int t = __shfl_up_sync(0xffffffffu, incl, o);
           if (lane >= o) incl += t;
         }
         if (lane == 31) warp_n[warp] = incl;
         __syncthreads();
-        unsigned int run = incl - col;
+        unsigned int run = incl - total;
         for (int w = 0; w < warp; ++w) run += warp_n[w];
+        unsigned int first[kPerThread];
+#pragma unroll
+        for (int j = 0; j < kPerThread; ++j) {
+          first[j] = run;
+          run += col[j];
+        }
         for (int w = 0; w < kRWarps; ++w) {
-          const unsigned int c = table[w * 256 + d];
-          table[w * 256 + d] = run;
-          run += c;
+          unsigned int* row = table + w * kTableWords;
+          unsigned int next[kPerThread];
+#pragma unroll
+          for (int j = 0; j < kPerThread; ++j) next[j] = first[j] + counter(row, d0 + j);
+#pragma unroll
+          for (int j = 0; j < kPerThread; j += (kPacked ? 2 : 1)) {
+            if constexpr (kPacked)
+              row[(d0 + j) >> 1] = first[j] | (first[j + 1] << 16);
+            else
+              row[d0 + j] = first[j];
+          }
+#pragma unroll
+          for (int j = 0; j < kPerThread; ++j) first[j] = next[j];
         }
       }
       __syncthreads();
@@ -200,13 +255,14 @@ __device__ int rank_support(uint32_t* s, uint32_t* kb, uint16_t* ia, uint16_t* i
         const unsigned int active = __ballot_sync(0xffffffffu, in);
         if (in) {
           const uint32_t key = src_k[e];
-          const unsigned int dg = (key >> shift) & 255u;
-          const unsigned int peers = __match_any_sync(active, dg);
-          const unsigned int pos = mine[dg] + __popc(peers & below);
+          const unsigned int dg = (key >> shift) & (kDigits - 1u);
+          const unsigned int peers = same_digit(active, dg);
+          const unsigned int pos = counter(mine, dg) + __popc(peers & below);
           dst_k[pos] = key;
           dst_i[pos] = src_i[e];
           __syncwarp(active);
-          if (lane == 31 - __clz((int)peers)) mine[dg] += __popc(peers);
+          // Atomic: with packed counters two digits of the group can share a word.
+          if (lane == 31 - __clz((int)peers)) atomicAdd(&mine[word_of(dg)], (unsigned int)__popc(peers) << half_of(dg));
         }
         __syncwarp();
       }
