@@ -443,18 +443,23 @@ cudaError_t dispatch_rank(const Plan& p, const float* in, float* out, cudaStream
 
 }  // namespace
 
-// Tile of the ranked network kernel: 64 x TH outputs, TH the largest of 32,
-// 16, 8 whose shared memory fits two blocks per SM (112 KB), else the device
-// limit. False for float64, single-row arrays, 3-D windows (a tile would rank
-// kd planes of support for one plane of outputs), widths below 48 or
+// Tile of the ranked network kernel: 64 x TH outputs, TH the largest of
+// 64, 48, 32, 16, 8 whose shared memory still lets as many blocks reside on
+// an SM as the kernel's registers do (rank_min_blocks), else the largest
+// within the device limit: a taller tile ranks fewer support samples per
+// output. False for float64, single-row arrays, 3-D windows (a tile would
+// rank kd planes of support for one plane of outputs), widths below 48 or
 // supports beyond 16-bit codes.
 bool rank_network_configure(Plan& p, int smem_limit) {
   const Geom3& g = p.tile.g;
   const int width = network_width_for(p.dtype, p.r.count);
   if (p.dtype != 0 || width < 48 || g.H == 1 || g.kd > 1) return false;
-  const size_t budget = std::min<size_t>(112 * 1024, (size_t)smem_limit);
+  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork || p.r.kind == kMedianHistogram;
+  const int blocks = (width <= 80 && median) ? 3 : (width <= 96 ? 2 : 1);
+  constexpr size_t kSmPerSm = 233472, kReserved = 1024;  // bytes per SM, reserved per block
+  const size_t budget = std::min<size_t>(kSmPerSm / blocks - kReserved, (size_t)smem_limit);
   for (size_t limit : {budget, (size_t)smem_limit}) {
-    for (int th : {32, 16, 8}) {
+    for (int th : {64, 48, 32, 16, 8}) {
       Tile t = p.tile.t;
       t.TW = kRankTW;
       t.TH = th;
