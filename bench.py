@@ -199,7 +199,7 @@ DEFAULT_WORKLOAD = "nanmedian_sortnet_5x5_4096_f32"
 MEASURED_TRAFFIC = {
     "nanmedian_sortnet_5x5_4096_f32": (67.182592e6 + 29.531392e6, "profiles/tile_box_kernel_nanmedian_sortnet_5x5_4096_f32.md"),
     "nanmedian_hist_65x65_4096_f32": (116.748544e6 + 127.178752e6, "profiles/histogram_kernel_nanmedian_hist_65x65_4096_f32.md"),
-    "nanmedian_ring_4_6_4096_f32": (67.187968e6 + 32.040704e6, "profiles/tile_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
+    "nanmedian_ring_4_6_4096_f32": (67.191808e6 + 28.039424e6, "profiles/rank_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
     "nanstd_31x31_4096_f32": (67.200512e6 + 30.526208e6, "profiles/moments_slide_kernel_nanstd_31x31_4096_f32.md"),
     "nanmin_31x31_4096_f32": (67.144192e6 + 21.329152e6, "profiles/extrema_pass_kernel_nanmin_31x31_4096_f32.md"),
     "nanmad_5x5_4096_f32": (73.826048e6 + 668.445440e6, "profiles/robust_kernel_nanmad_5x5_4096_f32.md"),
@@ -212,7 +212,7 @@ MEASURED_TRAFFIC = {
 MEASURED_INSTRUCTIONS = {
     "nanmedian_sortnet_5x5_4096_f32": (211559951, "profiles/tile_box_kernel_nanmedian_sortnet_5x5_4096_f32.md"),
     "nanmedian_hist_65x65_4096_f32": (4046466587, "profiles/histogram_kernel_nanmedian_hist_65x65_4096_f32.md"),
-    "nanmedian_ring_4_6_4096_f32": (1541069691, "profiles/tile_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
+    "nanmedian_ring_4_6_4096_f32": (875186480, "profiles/rank_network_kernel_nanmedian_ring_4_6_4096_f32.md"),
     "nanstd_31x31_4096_f32": (418849122, "profiles/moments_slide_kernel_nanstd_31x31_4096_f32.md"),
     "nanmin_31x31_4096_f32": (60.5e6 + 57.8e6, "profiles/extrema_pass_kernel_nanmin_31x31_4096_f32.md"),
     "nanmean_boxcar_31x31_4096_f32": (501907311, "profiles/boxcar_band_kernel_nanmean_boxcar_31x31_4096_f32.md"),
