@@ -196,11 +196,15 @@ struct FamilyState {
 };
 
 // A family of a specialised kernel reached through FamilyOps (box pair,
-// sliding histogram, sliding moments): one (kind, variant) pair.
-constexpr int kOpsKinds = 3;
+// sliding histogram, sliding moments, ranked networks): one (kind, variant)
+// pair.
+constexpr int kOpsKinds = 4;
 
 const FamilyOps& ops_of(int kind) {
-  return kind == 0 ? box_family_ops() : kind == 1 ? histogram_family_ops() : slide_family_ops();
+  return kind == 0 ? box_family_ops()
+         : kind == 1 ? histogram_family_ops()
+         : kind == 2 ? slide_family_ops()
+                     : rank_family_ops();
 }
 
 struct OpsFamily {
@@ -218,7 +222,7 @@ struct OpsFamily {
 struct Segment {
   std::vector<int> images;  // batch image indices, ascending
   FamilyState families[kFamilies];
-  std::vector<OpsFamily> ops;  // box pair, histogram and sliding moments families
+  std::vector<OpsFamily> ops;  // box pair, histogram, sliding moments and ranked network families
   std::vector<int> own;     // images launched through their own plan
   std::vector<const void*> in_ptrs;
   std::vector<void*> out_ptrs;

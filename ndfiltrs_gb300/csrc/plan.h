@@ -275,5 +275,6 @@ struct FamilyOps {
 const FamilyOps& histogram_family_ops();  // sliding histogram (histogram.cu), 4 variants
 const FamilyOps& box_family_ops();        // box pair 3x3 / 5x5 / 7x7 (box.cu), 6 variants
 const FamilyOps& slide_family_ops();      // sliding exact moments (moments_slide.cu), 1 variant
+const FamilyOps& rank_family_ops();       // ranked networks (rank_network.cu), 13 variants
 
 }  // namespace ndf

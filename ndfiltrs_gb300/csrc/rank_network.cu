@@ -19,6 +19,7 @@
 // src/histogram.rs:302-486; the statistic is Reduction::finish,
 // src/reduction.rs:78-130).
 #include <algorithm>
+#include <cstring>
 #include <utility>
 
 #include "network.cuh"
@@ -346,11 +347,15 @@ constexpr int rank_min_blocks() {
   return (N <= 80 && MODE == 1) ? 3 : (N <= 96 ? 2 : 1);
 }
 
-template <int N, int VFIX, int MODE>
-__global__ void __launch_bounds__(kRThreads, rank_min_blocks<N, MODE>())
-    rank_network_kernel(const float* __restrict__ in, float* __restrict__ out, const __grid_constant__ TileArgs a,
-                        const __grid_constant__ TapTable<N> taps, const __grid_constant__ CUtensorMap tmap) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// One output tile (index `tile`) of the ranked network kernel; off(i) is tap
+// i's offset in the staged support (a kernel parameter, which the compiler
+// uses as a constant operand, or a volatile read of shared memory so that
+// the offsets are read where they are used instead of being held in
+// registers), `tmap` the launch's tensor map (nullptr: remapped staging only).
+template <int N, int VFIX, int MODE, typename Off>
+__device__ __forceinline__ void rank_network_body(const float* __restrict__ in, float* __restrict__ out,
+                                                  const TileArgs& a, Off off, long long tile,
+                                                  unsigned char* smem_raw, const CUtensorMap* tmap) {
   const Geom3& g = a.g;
   const Tile& t = a.t;
   const RankLayout L = rank_layout(t, g.kd);
@@ -363,10 +368,10 @@ __global__ void __launch_bounds__(kRThreads, rank_min_blocks<N, MODE>())
   uint16_t* codes = reinterpret_cast<uint16_t*>(smem_raw + L.codes);
   unsigned int* table = reinterpret_cast<unsigned int*>(smem_raw + L.table);
   long long z, y0, x0;
-  tile_coords(a, blockIdx.x, z, y0, x0);
+  tile_coords(a, tile, z, y0, x0);
   const bool drop_inf = a.r.drop_inf;
   const uint32_t outside = sample_key<float>((float)a.r.cval, drop_inf);
-  if (!stage_tile(s, maps, smem_raw, in, a, &tmap, z, y0, x0, outside,
+  if (!stage_tile(s, maps, smem_raw, in, a, tmap, z, y0, x0, outside,
                   [&](float v) { return sample_key<float>(v, drop_inf); }))
     return;
   __syncthreads();
@@ -391,7 +396,7 @@ __global__ void __launch_bounds__(kRThreads, rank_min_blocks<N, MODE>())
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       if (i < V) {
-        const uint2 e = pv[base + taps.off[i]];
+        const uint2 e = pv[base + off(i)];
         k[i].v = e.x;
         cnt += e.y;
       } else {
@@ -402,6 +407,67 @@ __global__ void __launch_bounds__(kRThreads, rank_min_blocks<N, MODE>())
     float* row = out + (z * g.H + y) * g.W;
     row[x] = canonical(finish_half<N, VFIX, MODE, 0>(k, (int)(cnt & 0xFFFFu), a.r, sorted));
     if (x + 32 < g.W) row[x + 32] = canonical(finish_half<N, VFIX, MODE, 1>(k, (int)(cnt >> 16), a.r, sorted));
+  }
+}
+
+template <int N, int VFIX, int MODE>
+__global__ void __launch_bounds__(kRThreads, rank_min_blocks<N, MODE>())
+    rank_network_kernel(const float* __restrict__ in, float* __restrict__ out, const __grid_constant__ TileArgs a,
+                        const __grid_constant__ TapTable<N> taps, const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  rank_network_body<N, VFIX, MODE>(in, out, a, [&](int i) { return taps.off[i]; }, blockIdx.x, smem_raw, &tmap);
+}
+
+// Batched float32 images: one persistent launch per (width, tap count,
+// mode) over the concatenated tile lists; a block finds a tile's image by
+// binary search over the images' first tiles and keeps its arguments and
+// tap offsets in shared memory until the image changes. Staging is the
+// remapped path.
+struct RankTask {
+  const float* in;
+  float* out;
+  long long first_tile;
+  TileArgs a;
+  int32_t off[kMaxNetwork32];
+};
+
+// The family kernels read the tap offsets from shared memory; with a
+// run-time tap count the 80-wire median then spills about 600 bytes at the
+// three-block cap, so only its fixed-count form keeps three blocks.
+template <int N, int VFIX, int MODE>
+__global__ void __launch_bounds__(kRThreads, (N <= 80 && MODE == 1 && VFIX > 0) ? 3 : (N <= 96 ? 2 : 1))
+    rank_family_kernel(const RankTask* __restrict__ tasks, int ntasks, long long total_tiles) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ RankTask task;
+  __shared__ int current, found;
+  if (threadIdx.x == 0) current = -1;
+  __syncthreads();
+  for (long long tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = ntasks - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].first_tile <= tile)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      found = lo;
+    }
+    __syncthreads();
+    const int index = found;
+    if (index != current) {
+      const long long* src = reinterpret_cast<const long long*>(tasks + index);
+      long long* dst = reinterpret_cast<long long*>(&task);
+      for (int i = threadIdx.x; i < (int)(sizeof(RankTask) / 8); i += blockDim.x) dst[i] = src[i];
+      __syncthreads();
+      if (threadIdx.x == 0) current = index;
+    }
+    __syncthreads();
+    const volatile int32_t* off = task.off;
+    rank_network_body<N, VFIX, MODE>(task.in, task.out, task.a, [off](int i) { return (int)off[i]; },
+                                     tile - task.first_tile, smem_raw, nullptr);
+    __syncthreads();
   }
 }
 
@@ -437,7 +503,6 @@ cudaError_t dispatch_rank(const Plan& p, const float* in, float* out, cudaStream
   const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork || p.r.kind == kMedianHistogram;
   if (!median) return launch_rank<N, 0, 0>(p, in, out, s);
   if (N == 80 && p.r.count == 68) return launch_rank<80, 68, 1>(p, in, out, s);
-  if (N == 80 && p.r.count == 75) return launch_rank<80, 75, 1>(p, in, out, s);
   return launch_rank<N, 0, 1>(p, in, out, s);
 }
 
@@ -499,6 +564,75 @@ cudaError_t launch_rank_network(const Plan& p, const void* in, void* out, cudaSt
     default:
       return cudaErrorInvalidValue;
   }
+}
+
+namespace {
+
+// Batch family variants: (width, fixed tap count, mode).
+constexpr int kRankVariants[][3] = {{48, 0, 0},  {48, 0, 1},  {64, 0, 0},  {64, 0, 1},  {80, 0, 0},
+                                    {80, 0, 1},  {80, 68, 1}, {96, 0, 0},  {96, 0, 1},  {112, 0, 0},
+                                    {112, 0, 1}, {128, 0, 0}, {128, 0, 1}};
+constexpr int kNumRankVariants = (int)(sizeof(kRankVariants) / sizeof(kRankVariants[0]));
+
+int rank_family_variant(const Plan& p) {
+  if (p.algo != Algo::kTileRank || p.dtype != 0) return -1;
+  const bool median = p.r.kind == kMedian || p.r.kind == kMedianNetwork || p.r.kind == kMedianHistogram;
+  const int vfix = median && p.network == 80 && p.r.count == 68 ? 68 : 0;
+  for (int v = 0; v < kNumRankVariants; ++v)
+    if (kRankVariants[v][0] == p.network && kRankVariants[v][1] == vfix && kRankVariants[v][2] == (median ? 1 : 0))
+      return v;
+  return -1;
+}
+
+long long rank_family_tiles(const Plan& p) { return p.tile.t.tiles; }
+
+long long rank_family_slot_bytes(const Plan&) { return 0; }
+
+void rank_family_write_task(const Plan& p, const void* in, void* out, long long first_tile, void* task) {
+  RankTask t{};
+  t.in = (const float*)in;
+  t.out = (float*)out;
+  t.first_tile = first_tile;
+  t.a = p.tile;
+  t.a.r = p.r;
+  t.a.tma_bw = 0;
+  for (int i = 0; i < p.r.count && i < kMaxNetwork32; ++i) {
+    const int* bt = &p.box_taps[(size_t)i * 3];
+    t.off[i] = (bt[0] * p.tile.t.SH + bt[1]) * p.tile.t.SW + bt[2];
+  }
+  std::memcpy(task, &t, sizeof(t));
+}
+
+const void* rank_family_kernel_of(int variant) {
+  switch (variant) {
+    case 0: return (const void*)rank_family_kernel<48, 0, 0>;
+    case 1: return (const void*)rank_family_kernel<48, 0, 1>;
+    case 2: return (const void*)rank_family_kernel<64, 0, 0>;
+    case 3: return (const void*)rank_family_kernel<64, 0, 1>;
+    case 4: return (const void*)rank_family_kernel<80, 0, 0>;
+    case 5: return (const void*)rank_family_kernel<80, 0, 1>;
+    case 6: return (const void*)rank_family_kernel<80, 68, 1>;
+    case 7: return (const void*)rank_family_kernel<96, 0, 0>;
+    case 8: return (const void*)rank_family_kernel<96, 0, 1>;
+    case 9: return (const void*)rank_family_kernel<112, 0, 0>;
+    case 10: return (const void*)rank_family_kernel<112, 0, 1>;
+    case 11: return (const void*)rank_family_kernel<128, 0, 0>;
+    default: return (const void*)rank_family_kernel<128, 0, 1>;
+  }
+}
+
+cudaError_t rank_family_launch(int variant, const void* d_tasks, int ntasks, long long tiles, unsigned char*, long long,
+                               size_t smem, int grid, cudaStream_t s) {
+  void* args[] = {(void*)&d_tasks, &ntasks, &tiles};
+  return cudaLaunchKernel(rank_family_kernel_of(variant), dim3(grid), dim3(kRThreads), args, smem, s);
+}
+
+}  // namespace
+
+const FamilyOps& rank_family_ops() {
+  static const FamilyOps ops{sizeof(RankTask), rank_family_variant, rank_family_tiles, rank_family_slot_bytes,
+                             rank_family_write_task, rank_family_kernel_of, rank_family_launch};
+  return ops;
 }
 
 }  // namespace ndf

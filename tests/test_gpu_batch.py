@@ -154,19 +154,20 @@ def test_batch_with_rolling_means_extrema_and_robust_kinds(gpu) -> None:
 
 
 def test_specialised_kernels_run_as_one_persistent_launch_per_family(gpu) -> None:
-    """Images whose plans take the box-pair kernel, the sliding histogram or
-    the sliding exact moments join one persistent launch per family (kernel
-    and variant) instead of launching per image; results equal per-image
-    plans bit for bit."""
+    """Images whose plans take the box-pair kernel, the sliding histogram,
+    the sliding exact moments or the ranked network join one persistent
+    launch per family (kernel and variant) instead of launching per image;
+    results equal per-image plans bit for bit."""
     import torch
 
     from ndfiltrs_gb300 import _core
 
     rng = np.random.default_rng(11)
     specs, images = [], []
-    families = [("median", (5, 5)), ("median_histogram", (33, 31)), ("std", (9, 9))]
-    for i in range(12):
-        kind, size = families[i % 3]
+    families = [("median", (5, 5), "tile_box"), ("median_histogram", (33, 31), "histogram"),
+                ("std", (9, 9), "moments_slide"), ("median", (9, 9), "rank_network")]
+    for i in range(16):
+        kind, size, _ = families[i % 4]
         image = rng.normal(1000, 10, size=(int(rng.integers(60, 260)), int(rng.integers(60, 260))))
         image = image.astype(np.float32)
         image[rng.random(image.shape) < 0.02] = np.nan
@@ -174,12 +175,11 @@ def test_specialised_kernels_run_as_one_persistent_launch_per_family(gpu) -> Non
                           ignore_inf=kind == "std", min_count=1, parameter=1 if kind == "std" else 0,
                           percentile=50.0, mode=["reflect", "nearest", "wrap"][i % 3]))
         images.append(image)
-    expected_algorithms = {"median": "tile_box", "median_histogram": "histogram", "std": "moments_slide"}
     wants = []
-    for spec, image in zip(specs, images):
+    for i, (spec, image) in enumerate(zip(specs, images)):
         with _core.Plan(image.shape, np.float32, spec["kind"], spec["size"], mode=[spec["mode"]] * 2,
                         omit_nan=True, ignore_inf=spec["ignore_inf"], parameter=spec["parameter"]) as plan:
-            assert plan.algorithm == expected_algorithms[spec["kind"]], spec["kind"]
+            assert plan.algorithm == families[i % 4][2], (spec["kind"], spec["size"], plan.algorithm)
             wants.append(plan.run_host(image))
     batch = _core.Batch(specs)
     d_in = [torch.from_numpy(im).cuda() for im in images]
@@ -188,7 +188,7 @@ def test_specialised_kernels_run_as_one_persistent_launch_per_family(gpu) -> Non
     for _ in range(2):
         batch.run_device([t.data_ptr() for t in d_in], [t.data_ptr() for t in d_out], stream)
     torch.cuda.synchronize()
-    assert batch.launches == 3
+    assert batch.launches == 4
     for spec, out, want in zip(specs, d_out, wants):
         np.testing.assert_array_equal(bits(out.cpu().numpy()), bits(want), err_msg=spec["kind"])
     hosts = batch.run_host(images)
