@@ -339,9 +339,9 @@ __device__ __forceinline__ float finish_half(const Pair16 (&k)[N], int nv, const
 }
 
 // Resident blocks per SM the register allocation must allow: three for the
-// median networks up to 80 wires (80 registers, a spill of about 130 bytes,
-// against two blocks at 96), two for the general selections (whose
-// run-time picks spill kilobytes at 80 registers) and 96 wires, else one.
+// median networks up to 80 wires (at most 80 registers; ring(4, 6) needs
+// 77), two for the general selections (whose run-time picks spill
+// kilobytes at 80 registers) and 96 wires, else one.
 template <int N, int MODE>
 constexpr int rank_min_blocks() {
   return (N <= 80 && MODE == 1) ? 3 : (N <= 96 ? 2 : 1);
