@@ -157,6 +157,8 @@ WORKLOADS = {
     "nanmedian_direct_3x3_2048_f32": Workload(lambda: gaussian_image(2048), "median", (3, 3), "reflect"),
     # Sky image, histogram method, mode nearest.
     "nanmedian_hist_65x65_4096_f32": Workload(lambda: sky_image(4096), "median_histogram", (65, 65), "nearest"),
+    # The mixed batch's largest boxes (13 x 13 and 15 x 15 run on the sliding histogram).
+    "nanmedian_hist_13x13_4096_f32": Workload(lambda: sky_image(4096), "median_histogram", (13, 13), "nearest"),
     "nanmedian_hist_65x65_8192_f32": Workload(lambda: sky_image(8192), "median_histogram", (65, 65), "nearest"),
     "nanmedian_hist_129x129_8192_f32": Workload(lambda: sky_image(8192), "median_histogram", (129, 129), "nearest"),
     "nanmedian_hist_65x65_8192_f64": Workload(lambda: sky_image(8192, dtype=np.float64), "median_histogram",
