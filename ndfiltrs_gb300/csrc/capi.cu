@@ -547,7 +547,25 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
   }
   if (passes_ok && p.r.count > 25) out.push_back({Algo::kExtremaPasses, 0, 0});
   if (extrema_ok && p.r.count > 25) out.push_back({Algo::kExtremaTile, 0, 0});
-  if (hist_ok && (hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
+  // Sliding-histogram tiles besides the cost model's for windows of up to
+  // 2,048 samples, whose sparse bitsets favour other tile shapes (measured
+  // by the autotuner; every tile gives the same result).
+  std::vector<Candidate> hist_tiles;
+  if (hist_ok) {
+    hist_tiles.push_back({Algo::kHistogram, 0, 0});
+    if (p.r.count <= 2048 && g.kd == 1 && !line) {
+      Plan probe = p;
+      histogram_configure(probe);
+      const int dw = probe.hist_block_w, dh = probe.hist_block_h;
+      for (auto [tw, th] : {std::pair<int, int>{32, 128}, {128, 64}, {64, 64}}) {
+        if (tw == dw && th == dh) continue;
+        Plan q = p;
+        histogram_configure(q, tw, th);
+        if (q.hist_block_w == tw && histogram_smem(q) <= (size_t)smem_limit) hist_tiles.push_back({Algo::kHistogram, tw, th});
+      }
+    }
+  }
+  if (hist_ok && (hist_kind || width == 0)) out.insert(out.end(), hist_tiles.begin(), hist_tiles.end());
   if (p.footprint.empty() && g.kd == 1 && !line && box_supported(p.dtype, g.kh, g.kw)) {
     Tile bt = box_tile(g);
     if (tile_select_smem(p, bt) <= (size_t)smem_limit) out.push_back({Algo::kTileBox, bt.TW, bt.TH});
@@ -565,7 +583,7 @@ std::vector<Candidate> plan_candidates_impl(Plan& p, int smem_limit) {
     else if (!hist_ok)
       out.push_back({Algo::kTileRadix, tw, th});
   }
-  if (hist_ok && !(hist_kind || width == 0)) out.push_back({Algo::kHistogram, 0, 0});
+  if (hist_ok && !(hist_kind || width == 0)) out.insert(out.end(), hist_tiles.begin(), hist_tiles.end());
   if (passes_ok && p.r.count <= 25) out.push_back({Algo::kExtremaPasses, 0, 0});
   if (extrema_ok && p.r.count <= 25) out.push_back({Algo::kExtremaTile, 0, 0});
   if (out.empty() && fits_tile(tiles[0].first, tiles[0].second, false))
@@ -577,7 +595,7 @@ int apply_candidate_impl(Plan& p, const Candidate& c, int smem_limit) {
   p.algo = c.algo;
   switch (c.algo) {
     case Algo::kHistogram: {
-      histogram_configure(p);
+      histogram_configure(p, c.tw, c.th);
       p.smem_bytes = histogram_smem(p);
       if (p.smem_bytes > (size_t)smem_limit) return fail(NDF_ERR_UNSUPPORTED, "window too large");
       cudaError_t e = histogram_allocate(p);

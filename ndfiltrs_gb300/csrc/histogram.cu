@@ -947,7 +947,10 @@ Runs count_runs(const std::vector<uint8_t>& mask, int kd, int kh, int kw) {
 // output: vertical steps (2 kw), the first window of each warp's walk, the
 // column moves, the block sort (about 8 units per support sample) and a
 // global decode when the sorted keys do not fit in shared memory.
-HistChoice choose_tile(const Geom3& g, size_t key_bytes, const Runs& runs = Runs{}) {
+// The tile of a sliding-histogram plan: by the cost model, or the given
+// tw x th when it fits (an autotuner candidate; 0 when it does not).
+HistChoice choose_tile(const Geom3& g, size_t key_bytes, const Runs& runs = Runs{}, int force_tw = 0,
+                       int force_th = 0) {
   HistChoice best;
   if ((long long)g.kw > kMaxSupport || (long long)g.kh > kMaxSupport || (long long)g.kd > kMaxSupport)
     return best;
@@ -979,6 +982,10 @@ HistChoice choose_tile(const Geom3& g, size_t key_bytes, const Runs& runs = Runs
       return;
     }
   };
+  if (force_tw > 0) {
+    consider(force_tw, force_th);
+    return best;
+  }
   if (g.H == 1 && g.kh == 1) {
     for (int tw : {8192, 4096, 2048, 1024, 512, 256, 128, 64, 32})
       if (tw <= 32 || tw / 2 < g.W) consider(tw, 1);
@@ -1114,9 +1121,9 @@ bool histogram_supported(const Plan& p) {
   return c.TW > 0;
 }
 
-void histogram_configure(Plan& p) {
+void histogram_configure(Plan& p, int tw, int th) {
   const Runs runs = runs_of(p);
-  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8, runs);
+  HistChoice c = choose_tile(p.tile.g, p.dtype == 0 ? 4 : 8, runs, tw, th);
   p.hist_block_w = c.TW;
   p.hist_block_h = c.TH;
   p.hist_sdec = c.sdec;

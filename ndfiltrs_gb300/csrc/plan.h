@@ -251,7 +251,8 @@ size_t tile_select_smem(const Plan& p, const Tile& t);
 size_t tile_moments_smem(const Plan& p, const Tile& t);
 size_t histogram_smem(const Plan& p);
 bool histogram_supported(const Plan& p);
-void histogram_configure(Plan& p);
+// The cost model's tile, or tw x th (an autotuner candidate) when given.
+void histogram_configure(Plan& p, int tw = 0, int th = 0);
 cudaError_t histogram_allocate(Plan& p);
 int network_width_for(int dtype, int count);
 bool box_supported(int dtype, int kh, int kw);
