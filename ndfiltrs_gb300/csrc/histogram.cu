@@ -248,14 +248,15 @@ __device__ __forceinline__ int select_in_word32(unsigned int word, int k) {
 // word, so the walk costs what one thread's would); the next window's order
 // statistic is usually a few window samples away, within a word or two. A
 // walk longer than kSeqWords words continues as a parallel scan of 16 words
-// per iteration (eight sequential words measured 1-3% faster than four, and
-// four faster than one or two, from 13 x 13 to 65 x 65 windows). Every loop
+// per iteration (sixteen sequential words measured 2-5% faster than four,
+// and four faster than one or two, from 13 x 13 to 65 x 65 windows; 32 no
+// faster than 16). Every loop
 // that contains warp-synchronous operations runs until both segments of the
 // warp are done, so the two halves stay converged.
 constexpr int kSeg = 16;
 constexpr int kSegs = kHThreads / kSeg;
 constexpr unsigned int kFull = 0xffffffffu;
-constexpr int kSeqWords = 8;
+constexpr int kSeqWords = 16;
 
 struct SegHist {
   unsigned int* words;
